@@ -1,0 +1,404 @@
+"""Benchmark: permutations per second of the DTO permutation null on one GB300.
+
+Workload: one list pair of N = 20,000 features, list 2 from a Gaussian copula
+with rho = 0.2 to list 1, no ties; 100,000 on-device Philox permutations per
+step (plus the unpermuted task); the FP32-screen + FP64-refine path.  Inputs
+are seeded synthetic lists (the reference's own profiling inputs are not
+shipped).
+
+Printed JSON line (one, from rank 0):
+  value       perms/s over K timed steps, pair resident on the device, CUDA
+              events on the library's stream around the K steps.
+  e2e         the same metric through the C ABI with host buffers: every step
+              creates the pair from host arrays (host-to-device copy of the
+              pair tables) and returns the per-permutation minimum p-values to
+              host memory.
+  roofline    the grid kernel (the threshold-pair search): algorithmic work =
+              8 FP32-class operations per grid cell per permutation (the
+              nine-term log-pmf sum of the screen), over its CUDA-event time,
+              against the measured FP32 peak (cuBLAS SGEMM on this GPU).
+  cpu_baseline the reference algorithm restated in C (string hash-set
+              intersection per cell, FP64 tail per cell, tasks over threads),
+              timed on a row sample of one task per host thread.
+  fp64_gpu    the plain FP64 GPU path (every cell's FP64 tail) on a sample.
+
+--impl reference times the reference-algorithm CPU restatement alone, with all
+host threads, on the same workload and metric.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+METRIC = "perms/s on 1 GB300 at N=20k (FP32-screen vs plain FP64, same argmin); p50/p99 lat"
+N_FEATURES = 20000
+RHO = 0.2
+PERMS_PER_STEP = 100000
+WORKLOAD = ("single pair, N=20000 features, list 2 Gaussian copula rho=0.2 to list 1, no ties, "
+            "100000 on-device Philox permutations per step + the unpermuted task, "
+            "FP32 screen + FP64 refine")
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def host_threads():
+    try:
+        return len(os.sched_getaffinity(0))
+    except Exception:
+        return os.cpu_count() or 1
+
+
+# ---------------------------------------------------------------------------
+# clocks sampled during the timed region
+# ---------------------------------------------------------------------------
+class ClockSampler:
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device_index):
+        self.device_index = device_index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device_index), "--query-gpu=" + self.QUERY,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for ln in self.proc.stdout:
+            self.lines.append(ln.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ---------------------------------------------------------------------------
+# measured FP32 / FP64 peaks (cuBLAS GEMM without tensor-core math)
+# ---------------------------------------------------------------------------
+def measured_peaks(torch, device):
+    out = {}
+    old = torch.backends.cuda.matmul.allow_tf32
+    torch.backends.cuda.matmul.allow_tf32 = False
+    try:
+        for name, dt, n in (("fp32_tflops", torch.float32, 8192), ("fp64_tflops", torch.float64, 4096)):
+            a = torch.randn(n, n, device=device, dtype=dt)
+            b = torch.randn(n, n, device=device, dtype=dt)
+            torch.matmul(a, b)
+            torch.cuda.synchronize()
+            best = 0.0
+            for _ in range(3):
+                e0 = torch.cuda.Event(enable_timing=True)
+                e1 = torch.cuda.Event(enable_timing=True)
+                e0.record()
+                torch.matmul(a, b)
+                e1.record()
+                torch.cuda.synchronize()
+                ms = e0.elapsed_time(e1)
+                best = max(best, 2.0 * n ** 3 / (ms * 1e-3) / 1e12)
+            out[name] = best
+            del a, b
+    finally:
+        torch.backends.cuda.matmul.allow_tf32 = old
+    return out
+
+
+def load_peaks_file():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as fh:
+            return json.load(fh)
+    except Exception:
+        return {}
+
+
+# ---------------------------------------------------------------------------
+# CPU legs (oracle = the C restatement; test infrastructure)
+# ---------------------------------------------------------------------------
+def cpu_reference_rate(pair, threads, target_s=12.0):
+    """Reference algorithm (per-cell string hash-set intersection + FP64 tail),
+    one permuted task per thread, every row_stride-th list-1 threshold.
+    Returns (perms/s extrapolated to whole tasks, sample description)."""
+    import numpy as np
+    from oracle import oracle as O
+    (r1, f1), (r2, f2) = pair.sorted_lists()
+    names = pair.feature_names()
+    g1 = [names[f] for f in f1]
+    g2 = [names[f] for f in f2]
+    n1 = len(O.thresholds(int(r1[-1])))
+    n2 = len(O.thresholds(int(r2[-1])))
+    rng = np.random.default_rng(123)
+    idx1 = np.stack([rng.permutation(len(r1)) for _ in range(threads)]).astype(np.int32)
+    idx2 = np.stack([rng.permutation(len(r2)) for _ in range(threads)]).astype(np.int32)
+    # calibrate the row stride on a tiny sample
+    stride = max(1, n1 // 4)
+    t0 = time.perf_counter()
+    _, cells = O.ref_run(g1, r1, g2, r2, pair.population, idx1[:1], idx2[:1], 1, stride, 1)
+    dt = time.perf_counter() - t0
+    per_cell = dt / max(cells, 1)
+    want_cells = target_s / per_cell
+    stride = int(max(1, min(n1, n1 * n2 / max(want_cells, 1.0))))
+    t0 = time.perf_counter()
+    _, cells = O.ref_run(g1, r1, g2, r2, pair.population, idx1, idx2, threads, stride, threads)
+    dt = time.perf_counter() - t0
+    cells_per_task = n1 * n2
+    rate = cells / dt / cells_per_task
+    sample = ("%d permuted tasks on %d threads, every %d-th list-1 threshold (%d of %d grid cells "
+              "per task), %.1f s; perms/s extrapolated from cells/s" %
+              (threads, threads, stride, cells // max(threads, 1), cells_per_task, dt))
+    return rate, sample, dt
+
+
+def cpu_fast_oracle_rate(pair, seconds=3.0):
+    """The histogram-formulation FP64 oracle, single thread (second CPU column)."""
+    import numpy as np
+    from oracle import oracle as O
+    (r1, f1), (r2, f2) = pair.sorted_lists()
+    rng = np.random.default_rng(7)
+    done = 0
+    t0 = time.perf_counter()
+    while time.perf_counter() - t0 < seconds or done == 0:
+        O.optimize(r1, f1, r2, f2, pair.n_features, pair.population,
+                   rng.permutation(len(r1)).astype(np.int32), rng.permutation(len(r2)).astype(np.int32))
+        done += 1
+    return done / (time.perf_counter() - t0), done
+
+
+# ---------------------------------------------------------------------------
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return 0
+    from dual_threshold_optimization_gb300 import synth
+    pair = synth.copula_pair(N_FEATURES, RHO, seed=2)
+    threads = host_threads()
+    for _ in range(args.warmup):
+        cpu_reference_rate(pair, threads, target_s=2.0)
+    rates, total = [], 0.0
+    sample = ""
+    for _ in range(args.steps):
+        r, sample, dt = cpu_reference_rate(pair, threads, target_s=args.ref_seconds)
+        rates.append(r)
+        total += dt
+    value = statistics.mean(rates)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "perms/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total / max(args.steps, 1),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded Gaussian-copula lists)",
+        "config": {"workload": WORKLOAD, "n_features": N_FEATURES, "rho": RHO,
+                   "permutations": PERMS_PER_STEP},
+        "cpu_baseline": {"value": value, "unit": "perms/s", "cores": threads, "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": value, "unit": "perms/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": ("the reference is a Rust crate and cargo is not available: this times the C "
+                 "restatement of its algorithm (oracle/dto_oracle.c or_ref_run)"),
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_gpu(args):
+    import numpy as np
+    import torch
+    rank, world, local = dist_env()
+    dev = local if torch.cuda.device_count() > local else 0
+    torch.cuda.set_device(dev)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    from dual_threshold_optimization_gb300 import Engine, synth
+    from dual_threshold_optimization_gb300._lib import RESULT_DTYPE  # noqa: F401
+
+    pair = synth.copula_pair(N_FEATURES, RHO, seed=2)
+    eng = Engine(dev)
+    dp = eng.pair(pair.ranks1, pair.feat1, pair.ranks2, pair.feat2, pair.n_features, pair.population)
+    P = args.perms
+    seed = 0x5EED0000 + rank  # disjoint streams per rank (weak scaling)
+    stream = torch.cuda.ExternalStream(eng.stream)
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+
+    # ---- device-resident throughput ----
+    for w in range(args.warmup):
+        dp.run(P, seed=seed + 1000 + w, precision="screen")
+    barrier()
+    sampler = ClockSampler(dev)
+    sampler.start()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    step_ms, grid_ms, launches, summaries = [], [], 0, []
+    for s in range(args.steps):
+        t0 = time.perf_counter()
+        r = dp.run(P, seed=seed + s, precision="screen")
+        step_ms.append((time.perf_counter() - t0) * 1e3)
+        grid_ms.append(r.summary["grid_ms"])
+        launches += r.summary["n_launches"]
+        summaries.append(r.summary)
+    e1.record(stream)
+    barrier()
+    clocks = sampler.stop()
+    total_ms = e0.elapsed_time(e1)
+    t_max = total_ms
+    if world > 1:
+        t = torch.tensor([total_ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        t_max = float(t.item())
+    value = world * P * args.steps / (t_max * 1e-3)
+
+    # ---- end to end through the C ABI with host buffers ----
+    barrier()
+    e2e_ms, h2d, d2h = [], 0, 0
+    for s in range(args.e2e_steps):
+        t0 = time.perf_counter()
+        dq = eng.pair(pair.ranks1, pair.feat1, pair.ranks2, pair.feat2, pair.n_features, pair.population)
+        rr = dq.run(P, seed=seed + 500 + s, precision="screen")
+        h2d = dq.upload_bytes + rr.summary["h2d_bytes"]
+        d2h = rr.summary["d2h_bytes"]
+        dq.close()
+        e2e_ms.append((time.perf_counter() - t0) * 1e3)
+    barrier()
+    e2e_value = world * P / (statistics.mean(e2e_ms) * 1e-3) if e2e_ms else None
+
+    if rank != 0:
+        if world > 1:
+            torch.distributed.destroy_process_group()
+        return 0
+
+    # ---- roofline of the grid kernel ----
+    cells = dp.n1 * dp.n2
+    grid_s = sum(grid_ms) * 1e-3
+    tasks = args.steps * (P + 1)
+    achieved_tflops = 8.0 * cells * tasks / grid_s / 1e12
+    peaks = measured_peaks(torch, "cuda")
+    fp32_peak = peaks.get("fp32_tflops")
+    roofline = {"bound": "fp32", "achieved": achieved_tflops, "peak": fp32_peak, "unit": "TFLOP/s",
+                "frac": (achieved_tflops / fp32_peak) if fp32_peak else None,
+                "traffic": args.traffic,
+                "kernel": "grid_kernel<20> (threshold-pair search)",
+                "work_per_task": "8 ops x %d cells" % cells,
+                "peak_source": "measured: cuBLAS SGEMM 8192^3 without TF32 on this GPU (FP32 pipe)",
+                "grid_ms_per_step": statistics.mean(grid_ms),
+                "perm_ms_per_step": statistics.mean(s_["perm_ms"] for s_ in summaries)}
+
+    # ---- plain FP64 GPU path on a sample ----
+    fp64 = None
+    if args.fp64_perms > 0:
+        r64 = dp.run(args.fp64_perms, seed=seed + 777, precision="fp64")
+        r32 = dp.run(args.fp64_perms, seed=seed + 777, precision="screen")
+        fp64 = {"value": args.fp64_perms / (r64.summary["device_ms"] * 1e-3), "unit": "perms/s",
+                "perms": args.fp64_perms,
+                "same_argmin_as_screen": bool(np.array_equal(r64.minp, r32.minp)
+                                              and r64.unpermuted == r32.unpermuted)}
+
+    # ---- CPU baseline (reference algorithm restated) ----
+    cpu = None
+    if not args.no_cpu:
+        threads = host_threads()
+        rate, sample, _ = cpu_reference_rate(pair, threads, target_s=args.ref_seconds)
+        fast, ndone = cpu_fast_oracle_rate(pair)
+        cpu = {"value": rate, "unit": "perms/s", "cores": threads, "kind": "port", "sample": sample,
+               "fast_oracle_1thread": {"value": fast, "unit": "perms/s", "tasks": ndone,
+                                       "note": "histogram-formulation FP64 oracle"}}
+
+    s0 = summaries[-1]
+    line = {
+        "metric": METRIC, "value": value, "unit": "perms/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": t_max / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "int32+f32 screen, f64 refine",
+        "data": "synthetic (seeded Gaussian-copula lists)",
+        "config": {"workload": WORKLOAD, "n_features": N_FEATURES, "rho": RHO, "permutations": P,
+                   "grid": [dp.n1, dp.n2],
+                   "l2": "inputs larger than L2: each step streams %d MB of permutation labels"
+                         % (P * N_FEATURES * 2 // 1000000)},
+        "latency_ms": {"p50": statistics.median(step_ms),
+                       "p99": sorted(step_ms)[min(len(step_ms) - 1, int(0.99 * len(step_ms)))]},
+        "e2e": {"value": e2e_value, "unit": "perms/s", "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h},
+        "roofline": roofline,
+        "cpu_baseline": cpu,
+        "fp64_gpu": fp64,
+        "clocks": clocks,
+        "gpu_launches": launches,
+        "screen": {"fp64_refines_per_task": s0["n_refined"] / (P + 1),
+                   "stage2_per_task": s0["n_stage2"] / (P + 1),
+                   "logp_err_bound_screen": s0["logp_err_bound_screen"],
+                   "logp_err_bound_fp64": s0["logp_err_bound_fp64"],
+                   "empirical_pvalue": s0["empirical_pvalue"], "fdr": s0["fdr"]},
+        "peaks": {"fp32_tflops": fp32_peak, "fp64_tflops": peaks.get("fp64_tflops"),
+                  "hbm_gbs": load_peaks_file().get("hbm_gbs")},
+    }
+    print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--perms", type=int, default=PERMS_PER_STEP)
+    ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--fp64-perms", type=int, default=2432)
+    ap.add_argument("--ref-seconds", type=float, default=12.0)
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--traffic", type=float, default=None,
+                    help="DRAM bytes per grid-kernel launch from an ncu capture")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_gpu(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

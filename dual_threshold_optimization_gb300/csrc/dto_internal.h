@@ -1,0 +1,106 @@
+// dto_internal.h -- types shared by the kernels and the host side of libdto.so.
+#pragma once
+#include <cuda_runtime.h>
+#include <cstdint>
+
+namespace dto {
+
+#ifndef DTO_GRID_WARPS
+#define DTO_GRID_WARPS 12
+#endif
+constexpr int kGridWarps = DTO_GRID_WARPS;  // warps per CTA of the grid kernel (one task per warp)
+constexpr int kCandCap = 64;         // per-warp candidate buffer of the screen
+constexpr int kPermThreads = 1024;   // threads per CTA of the permutation kernel
+constexpr int kBuckets = 1024;       // Rao-Sandelius buckets (one per thread)
+constexpr int kMaxListLen = 65536;   // positions are stored as uint16 in shared memory
+constexpr int kScreenSlack = 5;      // fixed-point units added to the screen threshold
+constexpr int kSurvCap = 256;        // per-warp survivors of the FP32 stage
+
+// Per-warp shared-memory layout of the grid kernel, in ints: the column
+// counters (32 lanes x (C|1) slots, rounded to even), the candidate buffer
+// (kCandCap int2) and the survivor list (cell, overlap, lo per entry).
+__host__ __device__ constexpr int grid_cnt_ints(int C) { return (32 * (C | 1) + 1) & ~1; }
+__host__ __device__ constexpr int grid_warp_ints(int C) { return grid_cnt_ints(C) + 2 * kCandCap + 3 * kSurvCap; }
+
+// Device view of one list pair.  Rows are list-1 thresholds, columns list-2
+// thresholds.  A "label" is the shared-memory slot of a list-2 threshold
+// column in the grid kernel's per-warp counter array (column j of lane
+// j / C lives at slot lane * (C|1) + j % C); -1 means the feature never
+// enters a list-2 set (absent from list 2, or rank above the last threshold).
+struct PairDev {
+  int n1, n2;            // thresholds per list (grid rows, columns)
+  int N1, N2;            // list lengths
+  long long Npop;        // population size N of the hypergeometric
+  int C;                 // columns per lane
+  int fshift;            // fixed-point fraction bits of the screen table
+  const int* rowstart;   // [n1+1]: list-1 positions of row i are [rowstart[i], rowstart[i+1])
+  const int* ncnt;       // [n2]: set size of list 2 at threshold j
+  const uint32_t* F;     // [Npop+1]: round(ln(m!) * 2^fshift) modulo 2^32
+  const double2* LF;     // [>= Npop+1]: ln(m!) as double-double (hi, lo)
+  const int16_t* Ylab;   // [N1]: label of the list-2 column of the feature at list-1 position p
+  const int16_t* lab2;   // [N2]: label of list-2 position q
+  const int* map12;      // [N1]: list-2 position of the feature at list-1 position p, or -1
+};
+
+// One task's optimum.
+struct TaskResult {
+  double p;
+  int i, j, k;
+  int status;
+};
+
+enum GridMode { kModeFull64 = 0, kModeScreen = 1, kModeDump = 2 };
+
+struct GridArgs {
+  PairDev P;
+  const int16_t* X;      // [ntask][xstride] labels per list-1 position
+  long long xstride;
+  int ntask;
+  int mode;
+  int smemF;             // 1: the fixed-point table is staged in shared memory
+  TaskResult* out;       // [ntask]
+  int* work;             // task counter (zeroed before the launch)
+  unsigned long long* n_refined;  // [3]: FP64 tails, FP32 tails, speculative sweeps rejected
+  unsigned* guess_hist;  // nullable: [257] histogram of finished tasks' bounds (screen mode)
+  int* dump_k;           // kModeDump: [n1*n2] overlaps
+  double* dump_p;        // kModeDump: [n1*n2] p-values
+};
+
+struct PermArgs {
+  int L;                 // list length
+  uint64_t seed;
+  uint32_t pair_id;
+  uint32_t perm_base;    // permutation id of CTA 0
+  uint32_t list_tag;     // 1 or 2
+  const int16_t* Ylab;   // nullable: write labels X[p] = Ylab[sigma[p]]
+  int16_t* X;
+  long long xstride;
+  int* sigma;            // nullable: write sigma [count][sstride]
+  long long sstride;
+};
+
+struct ComposeArgs {
+  int N1, N2;
+  const int* idx1;       // row b at idx1 + b * stride, N1 entries
+  const int* idx2;       // row b at idx2 + b * stride, N2 entries, or nullptr (identity)
+  long long stride;
+  const int* map12;
+  const int16_t* lab2;
+  int16_t* X;
+  long long xstride;
+};
+
+size_t grid_smem_bytes(int C, int n1, long long Npop, int smemF);
+cudaError_t launch_grid(const GridArgs& a, int grid_ctas, cudaStream_t s);
+cudaError_t launch_perm(const PermArgs& a, int count, cudaStream_t s);
+cudaError_t launch_compose(const ComposeArgs& a, int count, cudaStream_t s);
+cudaError_t launch_sf_batch(const double2* LF, const long long* q, double* out, long long count,
+                            cudaStream_t s);
+
+// Per-C instantiations of the grid kernel (one translation unit each).
+#define DTO_FOR_EACH_C(X) X(4) X(8) X(12) X(16) X(20) X(24) X(28) X(32)
+#define DTO_DECLARE_GRID(CC) cudaError_t launch_grid_c##CC(const GridArgs& a, int ctas, size_t smem, cudaStream_t s);
+DTO_FOR_EACH_C(DTO_DECLARE_GRID)
+#undef DTO_DECLARE_GRID
+
+}  // namespace dto

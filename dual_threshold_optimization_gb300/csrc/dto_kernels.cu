@@ -1,0 +1,232 @@
+// dto_kernels.cu -- permutation, composition and tail kernels, and the grid
+// kernel dispatcher.
+//
+// Permutations replace PermutedRankedFeatureList::new
+// (src/collections/permuted.rs:56-60: a uniform shuffle of 0..len with
+// rand's thread_rng).  Here a permutation is a deterministic function of
+// (seed, pair id, permutation id, list tag):
+//   1. every element e draws a bucket in [0, 1024) from the top 10 bits of one
+//      Philox4x32-10 word (counter (e/4, perm, pair, 0x10000000 | tag<<24),
+//      word e%4, key = the two halves of the seed);
+//   2. elements are grouped by bucket, in increasing element order inside a
+//      bucket;
+//   3. each bucket b is shuffled by Fisher-Yates, drawing j uniform in [0, i]
+//      with Lemire's multiply-shift method and rejection (exactly unbiased)
+//      from the Philox stream counter (call, perm, pair,
+//      0x20000000 | tag<<24 | b).
+// One level of Rao-Sandelius bucketing followed by uniform shuffles of the
+// buckets gives an exactly uniform permutation.
+#include "dto_grid.cuh"
+#include "dto_internal.h"
+#include "dto_math.cuh"
+
+namespace dto {
+
+struct PhiloxStream {
+  uint4 ctr;
+  uint32_t k0, k1;
+  uint4 buf;
+  int used;
+  __device__ __forceinline__ uint32_t next() {
+    if (used == 4) {
+      buf = philox4x32_10(ctr, k0, k1);
+      ctr.x += 1;
+      used = 0;
+    }
+    uint32_t w = (used == 0) ? buf.x : (used == 1) ? buf.y : (used == 2) ? buf.z : buf.w;
+    ++used;
+    return w;
+  }
+  __device__ __forceinline__ uint32_t bounded(uint32_t range) {
+    uint32_t xw = next();
+    unsigned long long m = (unsigned long long)xw * range;
+    uint32_t l = (uint32_t)m;
+    if (l < range) {
+      uint32_t thr = (0u - range) % range;
+      while (l < thr) {
+        xw = next();
+        m = (unsigned long long)xw * range;
+        l = (uint32_t)m;
+      }
+    }
+    return (uint32_t)(m >> 32);
+  }
+};
+
+__device__ __forceinline__ uint32_t bucket_of(uint4 w, int q) {
+  uint32_t v = (q == 0) ? w.x : (q == 1) ? w.y : (q == 2) ? w.z : w.w;
+  return v >> 22;
+}
+
+__global__ void __launch_bounds__(kPermThreads) perm_kernel(const PermArgs A) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  uint16_t* sA = reinterpret_cast<uint16_t*>(smem_raw);
+  __shared__ int cnt[kBuckets];
+  __shared__ int start[kBuckets + 1];
+  __shared__ int warpSum[kPermThreads / 32];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int L = A.L;
+  const uint32_t perm = A.perm_base + blockIdx.x;
+  const uint32_t k0 = (uint32_t)A.seed, k1 = (uint32_t)(A.seed >> 32);
+  const uint32_t tagB = 0x10000000u | (A.list_tag << 24);
+
+  cnt[tid] = 0;
+  __syncthreads();
+  const int groups = (L + 3) >> 2;
+  for (int g = tid; g < groups; g += kPermThreads) {
+    uint4 w = philox4x32_10(make_uint4((uint32_t)g, perm, A.pair_id, tagB), k0, k1);
+#pragma unroll
+    for (int q = 0; q < 4; ++q)
+      if (4 * g + q < L) atomicAdd(&cnt[bucket_of(w, q)], 1);
+  }
+  __syncthreads();
+  // exclusive scan of the 1024 bucket counts
+  int v = cnt[tid];
+  int incl = v;
+#pragma unroll
+  for (int d = 1; d < 32; d <<= 1) {
+    int y = __shfl_up_sync(0xffffffffu, incl, d);
+    if (lane >= d) incl += y;
+  }
+  if (lane == 31) warpSum[warp] = incl;
+  __syncthreads();
+  if (warp == 0) {
+    int ws = warpSum[lane];
+    int wi = ws;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+      int y = __shfl_up_sync(0xffffffffu, wi, d);
+      if (lane >= d) wi += y;
+    }
+    warpSum[lane] = wi - ws;
+  }
+  __syncthreads();
+  int excl = incl - v + warpSum[warp];
+  start[tid] = excl;
+  if (tid == kPermThreads - 1) start[kBuckets] = excl + v;
+  cnt[tid] = excl;  // reused as the fill cursor
+  __syncthreads();
+  for (int g = tid; g < groups; g += kPermThreads) {
+    uint4 w = philox4x32_10(make_uint4((uint32_t)g, perm, A.pair_id, tagB), k0, k1);
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      int e = 4 * g + q;
+      if (e < L) {
+        int pos = atomicAdd(&cnt[bucket_of(w, q)], 1);
+        sA[pos] = (uint16_t)e;
+      }
+    }
+  }
+  __syncthreads();
+  {
+    const int s0 = start[tid], sz = start[tid + 1] - s0;
+    uint16_t* a = sA + s0;
+    // canonical (increasing) order inside the bucket
+    for (int i = 1; i < sz; ++i) {
+      uint16_t key = a[i];
+      int j = i - 1;
+      while (j >= 0 && a[j] > key) {
+        a[j + 1] = a[j];
+        --j;
+      }
+      a[j + 1] = key;
+    }
+    PhiloxStream st;
+    st.ctr = make_uint4(0u, perm, A.pair_id, 0x20000000u | (A.list_tag << 24) | (uint32_t)tid);
+    st.k0 = k0;
+    st.k1 = k1;
+    st.used = 4;
+    for (int i = sz - 1; i >= 1; --i) {
+      uint32_t j = st.bounded((uint32_t)(i + 1));
+      uint16_t tmp = a[i];
+      a[i] = a[j];
+      a[j] = tmp;
+    }
+  }
+  __syncthreads();
+  if (A.X) {
+    int16_t* xo = A.X + (long long)blockIdx.x * A.xstride;
+    for (int p = tid; p < L; p += kPermThreads) xo[p] = __ldg(A.Ylab + sA[p]);
+  }
+  if (A.sigma) {
+    int* so = A.sigma + (long long)blockIdx.x * A.sstride;
+    for (int p = tid; p < L; p += kPermThreads) so[p] = sA[p];
+  }
+}
+
+// X[p1] = label of the list-2 position holding the feature at list-1 position
+// p1: the permuted view of list 1 puts feature idx1[p1] at p1
+// (src/collections/permuted.rs:90-101); that feature sits at list-2 original
+// position q = map12[idx1[p1]], which the list-2 view shows at the position
+// p2 with idx2[p2] = q.
+__global__ void __launch_bounds__(1024) compose_kernel(const ComposeArgs A) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  uint16_t* inv2 = reinterpret_cast<uint16_t*>(smem_raw);
+  const int* idx1 = A.idx1 + (long long)blockIdx.x * A.stride;
+  if (A.idx2) {
+    const int* idx2 = A.idx2 + (long long)blockIdx.x * A.stride;
+    for (int p = threadIdx.x; p < A.N2; p += blockDim.x) inv2[__ldg(idx2 + p)] = (uint16_t)p;
+  }
+  __syncthreads();
+  int16_t* xo = A.X + (long long)blockIdx.x * A.xstride;
+  for (int p = threadIdx.x; p < A.N1; p += blockDim.x) {
+    int q = __ldg(A.map12 + __ldg(idx1 + p));
+    int16_t lab = -1;
+    if (q >= 0) lab = __ldg(A.lab2 + (A.idx2 ? (int)inv2[q] : q));
+    xo[p] = lab;
+  }
+}
+
+// hypergeometric_pvalue for a batch of (N, K, n, k) quadruples.
+__global__ void sf_batch_kernel(const double2* __restrict__ LF, const long long* __restrict__ q,
+                                double* __restrict__ out, long long count) {
+  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= count) return;
+  out[t] = sf64(LF, q[4 * t], q[4 * t + 1], q[4 * t + 2], q[4 * t + 3]);
+}
+
+size_t grid_smem_bytes(int C, int n1, long long Npop, int smemF) {
+  size_t f = smemF ? (size_t)(((Npop + 1 + 3) & ~3LL)) * 4 : 0;
+  return f + (size_t)((n1 + 1 + 3) & ~3) * 4 + (size_t)kGridWarps * grid_warp_ints(C) * 4;
+}
+
+cudaError_t launch_grid(const GridArgs& a, int ctas, cudaStream_t s) {
+  size_t smem = grid_smem_bytes(a.P.C, a.P.n1, a.P.Npop, a.smemF);
+  switch (a.P.C) {
+#define DTO_CASE(CC) \
+  case CC:           \
+    return launch_grid_c##CC(a, ctas, smem, s);
+    DTO_FOR_EACH_C(DTO_CASE)
+#undef DTO_CASE
+    default:
+      return cudaErrorInvalidValue;
+  }
+}
+
+cudaError_t launch_perm(const PermArgs& a, int count, cudaStream_t s) {
+  if (count <= 0) return cudaSuccess;
+  size_t smem = ((size_t)a.L * 2 + 15) & ~(size_t)15;
+  cudaError_t e = cudaFuncSetAttribute(perm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  perm_kernel<<<count, kPermThreads, smem, s>>>(a);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_compose(const ComposeArgs& a, int count, cudaStream_t s) {
+  if (count <= 0) return cudaSuccess;
+  size_t smem = a.idx2 ? (((size_t)a.N2 * 2 + 15) & ~(size_t)15) : 16;
+  cudaError_t e = cudaFuncSetAttribute(compose_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  compose_kernel<<<count, 1024, smem, s>>>(a);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_sf_batch(const double2* LF, const long long* q, double* out, long long count, cudaStream_t s) {
+  if (count <= 0) return cudaSuccess;
+  int threads = 128;
+  long long blocks = (count + threads - 1) / threads;
+  sf_batch_kernel<<<(unsigned)blocks, threads, 0, s>>>(LF, q, out, count);
+  return cudaGetLastError();
+}
+
+}  // namespace dto

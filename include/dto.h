@@ -1,0 +1,173 @@
+/*
+ * dto.h -- C ABI of the GB300 Dual Threshold Optimization engine (libdto.so).
+ *
+ * Plain pointers and sizes only.  Every entry point returns a status code
+ * (DTO_OK on success); dto_last_error() gives the message of the last failure
+ * on a context.  Each declaration names the reference interface it replaces
+ * (paths relative to the reference project).
+ *
+ * Vocabulary:
+ *   list        a ranked feature list: (rank, feature id) per feature.  Feature
+ *               ids are dense integers in [0, n_features) shared by both lists.
+ *   position    index into a list after the stable sort by rank
+ *               (src/collections/ranked.rs:527-542).
+ *   thresholds  the reference's grid T1 = 1, T(k+1) = floor(T(k)*1.01 + 1) while
+ *               T <= max rank (src/collections/ranked.rs:359-375).
+ *   cell        one (threshold1, threshold2) pair of the grid.
+ *   task        one optimize() call: the unpermuted task or one permutation
+ *               (src/run/task.rs:3-9).
+ */
+#ifndef DTO_H
+#define DTO_H
+
+#include <stdint.h>
+
+#if defined(__GNUC__)
+#define DTO_API __attribute__((visibility("default")))
+#else
+#define DTO_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define DTO_OK 0
+#define DTO_ERR_INVALID 1  /* bad arguments; the reference panics in these cases */
+#define DTO_ERR_OOM 2      /* device or host allocation failed */
+#define DTO_ERR_TIMEOUT 3  /* a bounded device wait gave up */
+#define DTO_ERR_CUDA 4     /* any other CUDA runtime failure */
+#define DTO_ERR_NOT_FOUND 5
+
+/* Precision of the threshold-pair search. */
+#define DTO_PRECISION_FP64 0   /* plain FP64: the FP64 tail of every cell (drop-in path) */
+#define DTO_PRECISION_SCREEN 1 /* 32-bit log-space screen of every cell, FP64 refine of the
+                                  cells within the proven margin; same argmin, same p */
+
+typedef struct dto_ctx dto_ctx;
+typedef struct dto_pair dto_pair;
+
+/* One task's optimum: OptimizationResultRecord (src/dto/results_objects.rs:14-24),
+ * plus the grid indices of the chosen cell. */
+typedef struct {
+    uint32_t rank1;              /* threshold of list 1 */
+    uint32_t rank2;              /* threshold of list 2 */
+    int64_t set1_len;            /* #{rank1 <= threshold1} */
+    int64_t set2_len;            /* #{rank2 <= threshold2} */
+    int64_t population_size;
+    int64_t intersection_size;
+    double pvalue;               /* P(X >= k), X ~ Hypergeometric(N, set1_len, set2_len) */
+    int32_t permuted;            /* 0 for the unpermuted task */
+    int32_t i, j;                /* grid indices of (rank1, rank2) */
+    int32_t status;              /* 0, or DTO_ERR_* for this task */
+} dto_result;
+
+/* Summary of a permutation run: the inputs of empirical_pvalue()
+ * (src/stat_operations/empirical_pvalue.rs:109-187). */
+typedef struct {
+    int64_t n_perm;
+    int64_t count_le;              /* #{permutation min-p <= unpermuted p} */
+    double empirical_pvalue;       /* count_le / n_perm, or 1.0 when n_perm == 0 */
+    double fdr;                    /* fdr(set1_len, set2_len, overlap, N, 0.8) */
+    double logp_err_bound_screen;  /* |error| bound of the screen's log-pmf, in nats */
+    double logp_err_bound_fp64;    /* relative error bound of an FP64 p-value */
+    int64_t n_fallback;            /* tasks re-run by a slower exact path */
+    int64_t n_refined;             /* FP64 tail evaluations */
+    int64_t n_stage2;              /* FP32 tail evaluations of screened cells */
+    double device_ms;              /* CUDA-event time of the device work */
+    double grid_ms;                /* CUDA-event time of the grid (search) kernels */
+    double perm_ms;                /* CUDA-event time of the permutation kernels */
+    int64_t n_launches;            /* kernels launched */
+    int64_t h2d_bytes;             /* host-to-device bytes copied by this call */
+    int64_t d2h_bytes;             /* device-to-host bytes copied by this call */
+} dto_summary;
+
+DTO_API int dto_version(void);
+DTO_API const char* dto_status_string(int status);
+
+/* Context: one CUDA device, one stream, the device-resident log-factorial
+ * tables and the per-batch scratch.  Replaces the thread pool and shared state
+ * of run_single_node (src/run/single_node.rs:83-137). */
+DTO_API int dto_ctx_create(int device, dto_ctx** out);
+DTO_API int dto_ctx_destroy(dto_ctx* ctx);
+DTO_API const char* dto_last_error(const dto_ctx* ctx);
+/* The context's CUDA stream (a cudaStream_t), for callers that time or order
+ * work around the library's launches. */
+DTO_API void* dto_ctx_stream(dto_ctx* ctx);
+
+/* RankedFeatureList::generate_thresholds (src/collections/ranked.rs:359-375),
+ * including its quirk: the last threshold is not clamped to max_rank.
+ * Writes min(count, cap) thresholds; returns count. */
+DTO_API int64_t dto_generate_thresholds(uint32_t max_rank, uint32_t* out, int64_t cap);
+
+/* A list pair, resident on the device.  Replaces RankedFeatureList::from for
+ * both lists (src/collections/ranked.rs:176-191: stable sort by rank, then the
+ * thresholds) and the per-task set extraction (ranked.rs:561-568).
+ *   ranks*, feat*: per input feature, in input order.  feat ids are unique in a
+ *   list and lie in [0, n_features).
+ *   population:   N of the hypergeometric (compute_population_size,
+ *                 src/dto/compute_population_size.rs:66-104, done by the caller).
+ * Errors: empty lists or no thresholds, duplicate or out-of-range ids,
+ * population smaller than a list -> DTO_ERR_INVALID. */
+DTO_API int dto_pair_create(dto_ctx* ctx, const uint32_t* ranks1, const int32_t* feat1, int64_t n1,
+                    const uint32_t* ranks2, const int32_t* feat2, int64_t n2,
+                    int64_t n_features, int64_t population, dto_pair** out);
+DTO_API int dto_pair_destroy(dto_pair* pair);
+/* Grid shape and the sorted order: order*[position] = input index. Any output
+ * pointer may be NULL. */
+DTO_API int dto_pair_info(const dto_pair* pair, int64_t* n_thresholds1, int64_t* n_thresholds2,
+                  int64_t* n_common);
+DTO_API int dto_pair_thresholds(const dto_pair* pair, uint32_t* t1, uint32_t* t2);
+/* Host-to-device bytes that dto_pair_create copied (the pair's device tables). */
+DTO_API int64_t dto_pair_upload_bytes(const dto_pair* pair);
+DTO_API int dto_pair_order(const dto_pair* pair, int32_t* order1, int32_t* order2);
+
+/* The permutation null: the unpermuted task plus n_perm permuted tasks
+ * (src/main.rs:122-126, src/run/single_node.rs:83-137), all on the device.
+ *   seed:      Philox4x32-10 key of the on-device permutations; task t >= 1 uses
+ *              permutation id t.
+ *   perm_idx:  NULL, or the permuted views' index arrays to use instead
+ *              (src/collections/permuted.rs:34), host memory laid out
+ *              [n_perm][n1 + n2]: idx1 (positions of list 1) then idx2.
+ *   out_unpermuted: the unpermuted optimum (required).
+ *   out_minp:  NULL or [n_perm] per-permutation minimum p-values.
+ *   out_perm:  NULL or [n_perm] per-permutation optima.
+ *   out_summary: NULL or the empirical p-value, FDR and error bounds. */
+DTO_API int dto_run(dto_ctx* ctx, dto_pair* pair, int64_t n_perm, uint64_t seed, const int32_t* perm_idx,
+            int precision, dto_result* out_unpermuted, double* out_minp, dto_result* out_perm,
+            dto_summary* out_summary);
+
+/* One task: optimize(list1, list2, permute, population, debug=false)
+ * (src/dto/optimize_main.rs:53-118).  permute != 0 uses permutation perm_id of
+ * seed, or idx1/idx2 when both are non-NULL. */
+DTO_API int dto_optimize(dto_ctx* ctx, dto_pair* pair, int permute, uint64_t seed, uint32_t perm_id,
+                 const int32_t* idx1, const int32_t* idx2, int precision, dto_result* out);
+
+/* OptimizationResult::Debug (src/dto/optimize_main.rs:68-70,
+ * src/dto/process_threshold_pairs.rs:111-127): every cell's record, in the
+ * reference's order (threshold1 major).  records holds n_thresholds1 *
+ * n_thresholds2 entries. idx1/idx2 as in dto_optimize (NULL: unpermuted). */
+DTO_API int dto_grid_dump(dto_ctx* ctx, dto_pair* pair, const int32_t* idx1, const int32_t* idx2,
+                  dto_result* records);
+
+/* hypergeometric_pvalue (src/stat_operations/hypergeometric_pvalue.rs:33-50)
+ * for count quadruples, evaluated on the device with the engine's FP64 tail.
+ * K > N or n > N -> DTO_ERR_INVALID (the reference panics). */
+DTO_API int dto_hypergeom_sf(dto_ctx* ctx, const int64_t* N, const int64_t* K, const int64_t* n,
+                     const int64_t* k, double* out, int64_t count);
+
+/* The on-device permutations of tasks perm_first .. perm_first+count-1 as the
+ * reference's index arrays (permuted.rs:34), so that dto_run with perm_idx
+ * reproduces them.  idx1: [count][n1], idx2: [count][n2]. */
+DTO_API int dto_export_permutations(dto_ctx* ctx, dto_pair* pair, uint64_t seed, uint32_t perm_first,
+                            int64_t count, int32_t* idx1, int32_t* idx2);
+
+/* fdr (src/stat_operations/fdr.rs:29-60). */
+DTO_API double dto_fdr(int64_t set1_len, int64_t set2_len, int64_t overlap, int64_t population,
+               double sensitivity);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* DTO_H */

@@ -156,6 +156,10 @@ static double or_exp_dd(dd_t L) {
 /* ------------------------------------------------------------------------- */
 /* FP64 tail specification: P(X >= k), X ~ Hypergeometric(N, K, n).           */
 /* (K, n) are canonicalised to a = min, b = max so the value is symmetric.    */
+/* Above the mode m = floor((a+1)(b+1)/(N+2)) every ratio pmf(j+1)/pmf(j) is  */
+/* below 1 and decreasing, so P = pmf(k) * sum of ratio products, summed      */
+/* upward; at or below the mode P = 1 - P(X <= k-1), the lower sum summed     */
+/* downward (its ratios pmf(j-1)/pmf(j) are below 1 and decreasing too).      */
 /* ------------------------------------------------------------------------- */
 static inline dd_t LFV(const double* h, const double* l, int64_t m) {
     dd_t r = {h[m], l[m]};
@@ -191,7 +195,9 @@ OR_EXPORT double or_sf64(const double* h, const double* l, int64_t N, int64_t K,
             t = t * r;
             S = S + t;
             j = j + 1;
-            if (r <= 0.5 && t <= S * 0x1p-54) break;
+            /* ratios decrease above the mode, so the remainder is at most
+             * t r / (1 - r): stop once that is below 2^-54 of the sum */
+            if (t * r <= (S * 0x1p-54) * (1.0 - r)) break;
         }
         double p = E * S;
         return p > 1.0 ? 1.0 : p;
@@ -206,7 +212,7 @@ OR_EXPORT double or_sf64(const double* h, const double* l, int64_t N, int64_t K,
             t = t * r;
             S = S + t;
             j = j - 1;
-            if (r <= 0.5 && t <= S * 0x1p-54) break;
+            if (t * r <= (S * 0x1p-54) * (1.0 - r)) break;
         }
         double p = 1.0 - E * S;
         return p < 0.0 ? 0.0 : p;
