@@ -33,7 +33,6 @@ struct dto_ctx {
   long long acc_launches = 0, acc_h2d = 0, acc_d2h = 0;
   std::string err;
   std::mutex mu;
-  uint32_t next_pair_id = 1;
   // ln(m!) as double-double, m = 0..lf_cap
   long long lf_cap = -1;
   std::vector<double> lf_hi, lf_lo;
@@ -450,7 +449,7 @@ int dto_pair_create(dto_ctx* ctx, const uint32_t* ranks1, const int32_t* feat1, 
   CK(cudaSetDevice(ctx->device));
   dto_pair* P = new dto_pair();
   P->ctx = ctx;
-  P->pair_id = ctx->next_pair_id++;
+  P->pair_id = 0;  // Philox stream id; dto_pair_set_stream changes it
   P->N1 = n1;
   P->N2 = n2;
   P->npop = population;
@@ -602,6 +601,12 @@ int dto_pair_thresholds(const dto_pair* P, uint32_t* t1, uint32_t* t2) {
 
 int64_t dto_pair_upload_bytes(const dto_pair* P) { return P ? (int64_t)P->upload_bytes : -1; }
 
+int dto_pair_set_stream(dto_pair* P, uint32_t stream_id) {
+  if (!P) return DTO_ERR_INVALID;
+  P->pair_id = stream_id;
+  return DTO_OK;
+}
+
 int dto_pair_order(const dto_pair* P, int32_t* o1, int32_t* o2) {
   if (!P) return DTO_ERR_INVALID;
   if (o1) std::copy(P->order1.begin(), P->order1.end(), o1);
@@ -612,8 +617,16 @@ int dto_pair_order(const dto_pair* P, int32_t* o1, int32_t* o2) {
 int dto_run(dto_ctx* ctx, dto_pair* P, int64_t n_perm, uint64_t seed, const int32_t* perm_idx,
             int precision, dto_result* out_unpermuted, double* out_minp, dto_result* out_perm,
             dto_summary* out_summary) {
+  return dto_run_range(ctx, P, 1u, n_perm, seed, perm_idx, precision, out_unpermuted, out_minp,
+                       out_perm, out_summary);
+}
+
+int dto_run_range(dto_ctx* ctx, dto_pair* P, uint32_t perm_first, int64_t n_perm, uint64_t seed,
+                  const int32_t* perm_idx, int precision, dto_result* out_unpermuted, double* out_minp,
+                  dto_result* out_perm, dto_summary* out_summary) {
   if (!ctx || !P || P->ctx != ctx || !out_unpermuted) return set_err(ctx, DTO_ERR_INVALID, "null argument");
-  if (n_perm < 0 || n_perm > 0x7fffffffLL) return set_err(ctx, DTO_ERR_INVALID, "n_perm out of range");
+  if (n_perm < 0 || n_perm > 0x7fffffffLL || (long long)perm_first + n_perm > 0xffffffffLL)
+    return set_err(ctx, DTO_ERR_INVALID, "n_perm out of range");
   if (precision != DTO_PRECISION_FP64 && precision != DTO_PRECISION_SCREEN)
     return set_err(ctx, DTO_ERR_INVALID, "unknown precision");
   std::lock_guard<std::mutex> g(ctx->mu);
@@ -664,7 +677,7 @@ int dto_run(dto_ctx* ctx, dto_pair* P, int64_t n_perm, uint64_t seed, const int3
       dI = (const int32_t*)dIdx;
     }
     if (cnt > 0) {
-      rc = make_labels(ctx, P, seed, (uint32_t)(b0 + 1), cnt, dI, row0);
+      rc = make_labels(ctx, P, seed, (uint32_t)(perm_first + b0), cnt, dI, row0);
       if (rc) return rc;
     } else {
       rc = grow(ctx, &ctx->dX, &ctx->xBytes, (size_t)xs * 2);

@@ -121,6 +121,10 @@ class DevicePair:
             raise RuntimeError("pair is closed")
         return self._pair
 
+    def set_stream(self, stream_id):
+        """Philox stream id of this pair's permutations (default 0)."""
+        check(lib().dto_pair_set_stream(self.handle, int(stream_id)))
+
     @property
     def upload_bytes(self):
         """Host-to-device bytes dto_pair_create copied for this pair."""
@@ -139,7 +143,7 @@ class DevicePair:
         return o1, o2
 
     def run(self, n_perm, seed=0, perm_idx=None, precision="screen", want_minp=True,
-            want_records=False):
+            want_records=False, first=1):
         ctx = self.engine.handle
         n_perm = int(n_perm)
         idx = None
@@ -151,9 +155,9 @@ class DevicePair:
         minp = np.empty(n_perm, np.float64) if want_minp else None
         recs = np.zeros(n_perm, RESULT_DTYPE) if want_records else None
         summ = DtoSummary()
-        check(lib().dto_run(ctx, self.handle, n_perm, int(seed) & (2**64 - 1), ptr(idx),
-                            precision_code(precision), C.byref(unp), ptr(minp), ptr(recs),
-                            C.byref(summ)), ctx)
+        check(lib().dto_run_range(ctx, self.handle, int(first), n_perm, int(seed) & (2**64 - 1),
+                                  ptr(idx), precision_code(precision), C.byref(unp), ptr(minp),
+                                  ptr(recs), C.byref(summ)), ctx)
         return RunResult(unp.as_dict(), minp, recs, summ.as_dict())
 
     def optimize(self, permute=False, seed=0, perm_id=1, idx1=None, idx2=None, precision="screen"):

@@ -118,6 +118,10 @@ DTO_API int dto_pair_destroy(dto_pair* pair);
 DTO_API int dto_pair_info(const dto_pair* pair, int64_t* n_thresholds1, int64_t* n_thresholds2,
                   int64_t* n_common);
 DTO_API int dto_pair_thresholds(const dto_pair* pair, uint32_t* t1, uint32_t* t2);
+/* Philox stream id of the pair's permutations (default 0): permutation t of a
+ * pair is a function of (seed, stream id, t).  Pairs that share a seed get
+ * independent permutations by taking different stream ids. */
+DTO_API int dto_pair_set_stream(dto_pair* pair, uint32_t stream_id);
 /* Host-to-device bytes that dto_pair_create copied (the pair's device tables). */
 DTO_API int64_t dto_pair_upload_bytes(const dto_pair* pair);
 DTO_API int dto_pair_order(const dto_pair* pair, int32_t* order1, int32_t* order2);
@@ -136,6 +140,16 @@ DTO_API int dto_pair_order(const dto_pair* pair, int32_t* order1, int32_t* order
 DTO_API int dto_run(dto_ctx* ctx, dto_pair* pair, int64_t n_perm, uint64_t seed, const int32_t* perm_idx,
             int precision, dto_result* out_unpermuted, double* out_minp, dto_result* out_perm,
             dto_summary* out_summary);
+
+/* dto_run over permutation ids perm_first .. perm_first + n_perm - 1 (dto_run
+ * is perm_first = 1).  A permutation depends only on (seed, pair, id), so
+ * processes that split an id range between them (one GPU each) reproduce a
+ * single run exactly; this replaces the MPI scatter of task chunks in
+ * run_multi_node (src/run/multi_node.rs:114-161). */
+DTO_API int dto_run_range(dto_ctx* ctx, dto_pair* pair, uint32_t perm_first, int64_t n_perm,
+                          uint64_t seed, const int32_t* perm_idx, int precision,
+                          dto_result* out_unpermuted, double* out_minp, dto_result* out_perm,
+                          dto_summary* out_summary);
 
 /* One task: optimize(list1, list2, permute, population, debug=false)
  * (src/dto/optimize_main.rs:53-118).  permute != 0 uses permutation perm_id of

@@ -1,0 +1,57 @@
+"""The C ABI library builds, loads and exports every symbol include/dto.h
+declares.  Only host-side utilities are called (no GPU needed)."""
+import os
+import re
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+@pytest.fixture(scope="module")
+def L():
+    from dual_threshold_optimization_gb300 import build
+    build.build()
+    from dual_threshold_optimization_gb300 import _lib
+    return _lib.lib()
+
+
+def declared():
+    src = open(os.path.join(ROOT, "include", "dto.h")).read()
+    return re.findall(r"DTO_API\s+[\w\s\*]+?\b(dto_\w+)\s*\(", src)
+
+
+def test_header_declarations_are_exported(L):
+    names = declared()
+    assert len(names) >= 20
+    from dual_threshold_optimization_gb300 import _lib
+    assert set(names) == set(_lib.EXPORTS), set(names) ^ set(_lib.EXPORTS)
+    for n in names:
+        assert hasattr(L, n), n
+
+
+def test_host_utilities(L):
+    import numpy as np
+    from oracle import oracle as O
+    from dual_threshold_optimization_gb300._lib import ptr
+    for mr in (0, 1, 5, 100, 101, 1000, 20000, 65535):
+        n = L.dto_generate_thresholds(mr, None, 0)
+        out = np.zeros(max(n, 1), np.uint32)
+        L.dto_generate_thresholds(mr, ptr(out), n)
+        assert out[:n].tolist() == O.thresholds(mr).tolist()
+    assert L.dto_fdr(200, 150, 50, 1000, 0.8) == O.fdr(200, 150, 50, 1000, 0.8)
+    assert L.dto_fdr(10, 10, 0, 100, 0.8) == 0.0
+    assert L.dto_status_string(0) == b"ok"
+    assert L.dto_version() >= 10000
+
+
+def test_no_oracle_in_product():
+    # the product package never imports, includes or links the oracle
+    pkg = os.path.join(ROOT, "dual_threshold_optimization_gb300")
+    pat = re.compile(r"^\s*(import\s+oracle|from\s+oracle|#\s*include\s*[<\"].*oracle)|liboracle",
+                     re.M)
+    for dp, _, files in os.walk(pkg):
+        for f in files:
+            if f.endswith((".py", ".cu", ".cuh", ".cpp", ".h")):
+                txt = open(os.path.join(dp, f), errors="ignore").read()
+                assert not pat.search(txt), f
