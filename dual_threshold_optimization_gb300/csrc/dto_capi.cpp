@@ -49,6 +49,9 @@ struct dto_ctx {
   int* dWork = nullptr;
   unsigned long long* dRefined = nullptr;
   unsigned* dGuess = nullptr;  // bound histogram shared by the batches of one run
+  void* dFall = nullptr;       // fallback task lists of the two table levels
+  size_t fallBytes = 0;
+  int* dNFall = nullptr;
 };
 
 struct dto_pair {
@@ -69,6 +72,9 @@ struct dto_pair {
   int16_t* dYlab = nullptr;
   int16_t* dLab2 = nullptr;
   int* dMap12 = nullptr;
+  uint16_t* dKthr[2] = {nullptr, nullptr};  // table screens, built for bounds kthr_tau
+  int kthr_tau[2] = {0, 0};
+  bool kthr_ok[2] = {false, false};
   PairDev dev{};
 };
 
@@ -271,6 +277,80 @@ int grid_tasks(dto_ctx* ctx, dto_pair* P, const int16_t* dX, long long xstride, 
   return DTO_OK;
 }
 
+// Table screen `level` for bound tau (fixed-point ln p), built on the device.
+int ensure_table(dto_ctx* ctx, dto_pair* P, int level, int tau) {
+  if (P->kthr_ok[level] && P->kthr_tau[level] == tau) return DTO_OK;
+  if (!P->dKthr[level]) CK(cudaMalloc(&P->dKthr[level], table_entries(P->C, P->dev.n1) * 2));
+  TableArgs t{};
+  t.n1 = P->dev.n1;
+  t.n2 = P->dev.n2;
+  t.N = (int)P->npop;
+  t.C = P->C;
+  t.rowstart = P->dRow;
+  t.ncnt = P->dNcnt;
+  t.F = P->dF;
+  t.fshift = P->fshift;
+  t.tau = tau;
+  t.kthr = P->dKthr[level];
+  CK(launch_table_build(t, ctx->nsm, ctx->stream));
+  ctx->acc_launches += 1;
+  P->kthr_tau[level] = tau;
+  P->kthr_ok[level] = true;
+  return DTO_OK;
+}
+
+// Tasks [0, ntask) of ctx->dX through the table ladder: level 0 (bound at the
+// first batch's 90th percentile), then its fallbacks through level 1 (bound
+// one nat above the first batch's largest minimum), then the rest through the
+// exhaustive screen.  Counts of each list stay on the device.
+int table_tasks(dto_ctx* ctx, dto_pair* P, long long xstride, int ntask, TaskResult* dOut) {
+  int rc = grow(ctx, &ctx->dFall, &ctx->fallBytes, (size_t)std::max(ntask, 1) * 8);
+  if (rc) return rc;
+  int* fall0 = (int*)ctx->dFall;
+  int* fall1 = fall0 + std::max(ntask, 1);
+  CK(cudaMemsetAsync(ctx->dWork, 0, 4 * sizeof(int), ctx->stream));
+  CK(cudaMemsetAsync(ctx->dNFall, 0, 2 * sizeof(int), ctx->stream));
+  CK(cudaEventRecord(ctx->evk[2], ctx->stream));
+  const int per_cta = kTableWarps;
+  for (int level = 0; level < 2; ++level) {
+    TableGridArgs a{};
+    a.P = P->dev;
+    a.P.LF = ctx->dLF;
+    a.X = (const int16_t*)ctx->dX;
+    a.xstride = xstride;
+    a.ntask = ntask;
+    a.tau = P->kthr_tau[level];
+    a.kthr = P->dKthr[level];
+    a.out = dOut;
+    a.work = ctx->dWork + level;
+    a.n_refined = ctx->dRefined;
+    a.fallback = level == 0 ? fall0 : fall1;
+    a.nfallback = ctx->dNFall + level;
+    a.task_list = level == 0 ? nullptr : fall0;
+    a.ntask_dev = level == 0 ? nullptr : ctx->dNFall;
+    int ctas = level == 0 ? std::max(1, std::min(2 * ctx->nsm, (ntask + per_cta - 1) / per_cta))
+                          : 2 * ctx->nsm;
+    CK(launch_table_grid(a, P->C, ctas, ctx->stream));
+  }
+  GridArgs g{};
+  g.P = P->dev;
+  g.P.LF = ctx->dLF;
+  g.X = (const int16_t*)ctx->dX;
+  g.xstride = xstride;
+  g.ntask = ntask;
+  g.mode = kModeScreen;
+  g.smemF = grid_smem_bytes(P->C, P->dev.n1, P->npop, 1) <= ctx->smem_optin ? 1 : 0;
+  g.out = dOut;
+  g.work = ctx->dWork + 2;
+  g.n_refined = ctx->dRefined;
+  g.task_list = fall1;
+  g.ntask_dev = ctx->dNFall + 1;
+  CK(launch_grid(g, ctx->nsm, ctx->stream));
+  CK(cudaEventRecord(ctx->evk[3], ctx->stream));
+  ctx->acc_launches += 3;
+  return DTO_OK;
+}
+
 // Labels of n_perm permutations starting at perm id `first` into ctx->dX.
 int make_labels_launch(dto_ctx* ctx, dto_pair* P, uint64_t seed, uint32_t first, int count,
                        const int32_t* dIdx, int16_t* X, long long xs);
@@ -391,6 +471,7 @@ int dto_ctx_create(int device, dto_ctx** out) {
   if ((e = cudaMalloc(&ctx->dWork, 256)) != cudaSuccess) return fail(e);
   if ((e = cudaMalloc(&ctx->dRefined, 256)) != cudaSuccess) return fail(e);
   if ((e = cudaMalloc(&ctx->dGuess, 2048)) != cudaSuccess) return fail(e);
+  if ((e = cudaMalloc(&ctx->dNFall, 256)) != cudaSuccess) return fail(e);
   *out = ctx;
   return DTO_OK;
 }
@@ -407,6 +488,8 @@ int dto_ctx_destroy(dto_ctx* ctx) {
   cudaFree(ctx->dWork);
   cudaFree(ctx->dRefined);
   cudaFree(ctx->dGuess);
+  cudaFree(ctx->dFall);
+  cudaFree(ctx->dNFall);
   if (ctx->ev0) cudaEventDestroy(ctx->ev0);
   if (ctx->ev1) cudaEventDestroy(ctx->ev1);
   for (int q = 0; q < 4; ++q)
@@ -580,6 +663,8 @@ int dto_pair_destroy(dto_pair* P) {
   cudaFree(P->dYlab);
   cudaFree(P->dLab2);
   cudaFree(P->dMap12);
+  cudaFree(P->dKthr[0]);
+  cudaFree(P->dKthr[1]);
   delete P;
   return DTO_OK;
 }
@@ -663,9 +748,16 @@ int dto_run_range(dto_ctx* ctx, dto_pair* P, uint32_t perm_first, int64_t n_perm
   // concurrently with the first permutations.
   std::vector<double> minp((size_t)n_perm);
   TaskResult unperm{};
-  for (long long b0 = 0; b0 < std::max<long long>(n_perm, 1); b0 += batch) {
+  // The first batch (the unpermuted task and up to first_batch permutations)
+  // goes through the exhaustive screen; its 90th-percentile bound then builds
+  // the table screen used by the remaining batches.
+  const long long first_batch = (long long)ctx->nsm * kGridWarps * 2;
+  const bool use_table = (mode == kModeScreen) && n_perm > 2 * first_batch;
+  bool table_ready = false;
+  long long step = use_table ? first_batch : batch;
+  for (long long b0 = 0; b0 < std::max<long long>(n_perm, 1); b0 += step, step = batch) {
     const int row0 = (b0 == 0) ? 1 : 0;
-    int cnt = (int)std::min(batch, n_perm - b0);
+    int cnt = (int)std::min(step, n_perm - b0);
     if (cnt < 0) cnt = 0;
     const int32_t* dI = nullptr;
     if (perm_idx && cnt > 0) {
@@ -685,7 +777,8 @@ int dto_run_range(dto_ctx* ctx, dto_pair* P, uint32_t perm_first, int64_t n_perm
     }
     if (row0) CK(cudaMemcpyAsync(ctx->dX, P->dYlab, (size_t)P->N1 * 2, cudaMemcpyDeviceToDevice, ctx->stream));
     const int ntask = cnt + row0;
-    rc = grid_tasks(ctx, P, (const int16_t*)ctx->dX, xs, ntask, mode, dRes, nullptr, nullptr, true);
+    if (table_ready) rc = table_tasks(ctx, P, xs, ntask, dRes);
+    else rc = grid_tasks(ctx, P, (const int16_t*)ctx->dX, xs, ntask, mode, dRes, nullptr, nullptr, true);
     if (rc) return rc;
     CK(cudaMemcpyAsync(hRes, dRes, (size_t)ntask * sizeof(TaskResult), cudaMemcpyDeviceToHost, ctx->stream));
     ctx->acc_d2h += (long long)ntask * (long long)sizeof(TaskResult);
@@ -701,6 +794,25 @@ int dto_run_range(dto_ctx* ctx, dto_pair* P, uint32_t perm_first, int64_t n_perm
       minp[(size_t)(b0 + q)] = r.p;
       if (out_minp) out_minp[b0 + q] = r.p;
       if (out_perm) fill_result(P, r, 1, &out_perm[b0 + q]);
+    }
+    if (use_table && !table_ready && cnt >= 256) {
+      std::vector<double> v(minp.begin() + b0, minp.begin() + b0 + cnt);
+      size_t q90 = (size_t)(0.9 * (double)(v.size() - 1));
+      std::nth_element(v.begin(), v.begin() + q90, v.end());
+      const double pq = v[q90];
+      const double pmax = *std::max_element(v.begin(), v.end());
+      const double sc = std::ldexp(1.0, P->fshift);
+      if (pq > 1e-300 && pmax < 1.0) {
+        const double t0 = std::floor(std::log(pq) * sc);
+        const double t1 = std::floor(std::min(std::log(pmax) + 1.0, 0.0) * sc);
+        if (t0 > -2.0e9 && t1 < 2.0e9) {
+          rc = ensure_table(ctx, P, 0, (int)t0);
+          if (rc) return rc;
+          rc = ensure_table(ctx, P, 1, (int)t1);
+          if (rc) return rc;
+          table_ready = true;
+        }
+      }
     }
   }
   fill_result(P, unperm, 0, out_unpermuted);

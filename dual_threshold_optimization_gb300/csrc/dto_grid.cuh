@@ -140,6 +140,51 @@ __device__ __forceinline__ Interval eval32(const uint32_t* F, int N, uint32_t FN
   return Interval{lo, min(hi, kScreenSlack)};
 }
 
+constexpr int kTableW = 48;  // pmf terms of the partial-sum lower bound
+
+// FP32 partial sum of w terms from k (ratios below 1 from the mode up); the
+// same error analysis as tail32 bounds |ln S32 - ln S| by d 1e-6 + 2e-5.
+__device__ __forceinline__ float partial32(int N, int a, int b, int k, float& err) {
+  float aj = (float)(a - k), bj = (float)(b - k), j1 = (float)(k + 1), cj = (float)(N - a - b + k + 1);
+  float t = 1.f, S = 1.f;
+  int d = 0;
+#pragma unroll 4
+  for (; d < kTableW - 1; ++d) {
+    if (aj <= 0.f) break;
+    float r = __fdividef(aj * bj, j1 * cj);
+    t *= r;
+    S += t;
+    aj -= 1.f;
+    bj -= 1.f;
+    j1 += 1.f;
+    cj += 1.f;
+  }
+  err = (float)d * 1e-6f + 2e-5f;
+  return __logf(S);
+}
+
+// Fixed-point lower bound of ln P(X >= k) used to build the table.
+__device__ __forceinline__ int lbt_fix(const uint32_t* __restrict__ F, int N, uint32_t FN, int K, int n,
+                                       int k, long long mode, double scale) {
+  const int a = min(K, n), b = max(K, n);
+  const int k0 = (long long)k <= mode ? (int)mode : k;
+  const int L = logpmf_fix(F, N, FN, K, n, k0);
+  float err;
+  float ls = partial32(N, a, b, k0, err);
+  return L - kScreenSlack + (int)floor((double)(ls - err) * scale) - 1;
+}
+
+// Stage 2 behind a cheaper filter: a cell whose partial-sum lower bound
+// already exceeds B + 1 can neither be the FP64 argmin (its ln p is above B)
+// nor lower B, so its tail is not summed.
+__device__ __forceinline__ Interval eval32_filtered(const uint32_t* F, int N, uint32_t FN, int K, int n, int k,
+                                                    double scale, int B) {
+  const int a = min(K, n), b = max(K, n);
+  const long long mode = ((long long)(a + 1) * (long long)(b + 1)) / (long long)(N + 2);
+  if (k > 0 && lbt_fix(F, N, FN, K, n, k, mode, scale) > B + 1) return Interval{0x7fffffff, 0x7fffffff};
+  return eval32(F, N, FN, K, n, k, scale);
+}
+
 // Device-side guess of the task's bound B from the tasks already finished in
 // this launch: a histogram of their final B in quarter-nat bins of -ln p.
 // A guess is used only as a starting point: the sweep it starts is accepted
@@ -270,11 +315,13 @@ __global__ void __launch_bounds__(kGridWarps * 32, 1) grid_kernel(const GridArgs
   const uint32_t FN = F[N];
   unsigned long long n32 = 0, n64 = 0, nfall = 0;  // stage-2, FP64 evaluations, fallbacks
 
+  const int ntask = A.ntask_dev ? *((volatile const int*)A.ntask_dev) : A.ntask;
   for (;;) {
     int b = 0;
     if (lane == 0) b = atomicAdd(A.work, 1);
     b = __shfl_sync(kFull, b, 0);
-    if (b >= A.ntask) break;
+    if (b >= ntask) break;
+    if (A.task_list) b = A.task_list[b];
     const int16_t* x = A.X + (long long)b * A.xstride;
 
     if (A.mode == kModeFull64 || A.mode == kModeDump) {
@@ -361,7 +408,7 @@ __global__ void __launch_bounds__(kGridWarps * 32, 1) grid_kernel(const GridArgs
         if (q < ncand) {
           c = cand[q];
           int ci = c.x >> 16, cj = c.x & 0xffff;
-          iv = eval32(F, N, FN, sRow[ci + 1], __ldg(A.P.ncnt + cj), c.y, scale);
+          iv = eval32_filtered(F, N, FN, sRow[ci + 1], __ldg(A.P.ncnt + cj), c.y, scale, B);
         }
         int h = iv.hi;
 #pragma unroll

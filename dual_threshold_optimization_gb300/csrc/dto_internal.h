@@ -62,6 +62,8 @@ struct GridArgs {
   int* work;             // task counter (zeroed before the launch)
   unsigned long long* n_refined;  // [3]: FP64 tails, FP32 tails, speculative sweeps rejected
   unsigned* guess_hist;  // nullable: [257] histogram of finished tasks' bounds (screen mode)
+  const int* task_list;  // nullable: task q is row/result task_list[q]
+  const int* ntask_dev;  // nullable: the task count, read on the device
   int* dump_k;           // kModeDump: [n1*n2] overlaps
   double* dump_p;        // kModeDump: [n1*n2] p-values
 };
@@ -90,7 +92,40 @@ struct ComposeArgs {
   long long xstride;
 };
 
+// Table screen (dto_table.cuh).
+constexpr int kTableWarps = 16;  // warps per CTA of the table-screen kernel (2 CTAs per SM)
+
+struct TableArgs {
+  int n1, n2, N, C;
+  const int* rowstart;   // K_i = rowstart[i+1]
+  const int* ncnt;
+  const uint32_t* F;
+  int fshift;
+  int tau;               // fixed-point ln p guess
+  uint16_t* kthr;        // [n1][32][table_cq(C)]
+};
+
+struct TableGridArgs {
+  PairDev P;
+  const int16_t* X;
+  long long xstride;
+  int ntask;
+  int tau;                // the guess the table was built for
+  const uint16_t* kthr;   // [n1][32][table_cq(C)]
+  TaskResult* out;
+  int* work;
+  unsigned long long* n_refined;  // [3]
+  int* fallback;          // [ntask] task ids whose minimum lies above the guess
+  int* nfallback;         // count (zeroed before the launch)
+  const int* task_list;   // nullable: task q is row/result task_list[q]
+  const int* ntask_dev;   // nullable: the task count, read on the device
+};
+
 size_t grid_smem_bytes(int C, int n1, long long Npop, int smemF);
+size_t table_smem_bytes(int C, int n1);
+size_t table_entries(int C, int n1);
+cudaError_t launch_table_build(const TableArgs& a, int nsm, cudaStream_t s);
+cudaError_t launch_table_grid(const TableGridArgs& a, int C, int ctas, cudaStream_t s);
 cudaError_t launch_grid(const GridArgs& a, int grid_ctas, cudaStream_t s);
 cudaError_t launch_perm(const PermArgs& a, int count, cudaStream_t s);
 cudaError_t launch_compose(const ComposeArgs& a, int count, cudaStream_t s);
@@ -102,5 +137,8 @@ cudaError_t launch_sf_batch(const double2* LF, const long long* q, double* out, 
 #define DTO_DECLARE_GRID(CC) cudaError_t launch_grid_c##CC(const GridArgs& a, int ctas, size_t smem, cudaStream_t s);
 DTO_FOR_EACH_C(DTO_DECLARE_GRID)
 #undef DTO_DECLARE_GRID
+#define DTO_DECLARE_TABLE(CC) cudaError_t launch_table_grid_c##CC(const TableGridArgs& a, int ctas, size_t smem, cudaStream_t s);
+DTO_FOR_EACH_C(DTO_DECLARE_TABLE)
+#undef DTO_DECLARE_TABLE
 
 }  // namespace dto

@@ -16,8 +16,11 @@
 //      0x20000000 | tag<<24 | b).
 // One level of Rao-Sandelius bucketing followed by uniform shuffles of the
 // buckets gives an exactly uniform permutation.
+#include <algorithm>
+
 #include "dto_grid.cuh"
 #include "dto_internal.h"
+#include "dto_table.cuh"
 #include "dto_math.cuh"
 
 namespace dto {
@@ -196,6 +199,33 @@ cudaError_t launch_grid(const GridArgs& a, int ctas, cudaStream_t s) {
 #define DTO_CASE(CC) \
   case CC:           \
     return launch_grid_c##CC(a, ctas, smem, s);
+    DTO_FOR_EACH_C(DTO_CASE)
+#undef DTO_CASE
+    default:
+      return cudaErrorInvalidValue;
+  }
+}
+
+size_t table_smem_bytes(int C, int n1) {
+  return (size_t)((n1 + 1 + 3) & ~3) * 4 + (size_t)kTableWarps * table_warp_ints(C) * 4;
+}
+
+size_t table_entries(int C, int n1) { return (size_t)n1 * 32 * table_cq(C); }
+
+cudaError_t launch_table_build(const TableArgs& a, int nsm, cudaStream_t s) {
+  long long cells = (long long)table_entries(a.C, a.n1);
+  int threads = 128;
+  long long blocks = std::min<long long>((cells + threads - 1) / threads, (long long)nsm * 64);
+  table_build_kernel<<<(unsigned)blocks, threads, 0, s>>>(a);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_table_grid(const TableGridArgs& a, int C, int ctas, cudaStream_t s) {
+  size_t smem = table_smem_bytes(C, a.P.n1);
+  switch (C) {
+#define DTO_CASE(CC) \
+  case CC:           \
+    return launch_table_grid_c##CC(a, ctas, smem, s);
     DTO_FOR_EACH_C(DTO_CASE)
 #undef DTO_CASE
     default:

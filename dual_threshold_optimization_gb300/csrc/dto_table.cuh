@@ -1,0 +1,382 @@
+// dto_table.cuh -- the table screen: the fast path of the threshold-pair search.
+//
+// For a pair and a bound guess tau (fixed-point ln p), kthr[i][j] is the
+// smallest overlap k of cell (i, j) whose lower bound LBT(k) of ln P(X >= k)
+// is <= tau + margin, where
+//   LBT(k) = ln P_w(max(k, mode)),  P_w(k) = sum_{j=k}^{k+w-1} pmf(j)  (w = 48),
+// evaluated in FP32 with its rounding error subtracted.  Above the mode P_w is
+// decreasing in k (the window loses pmf(k) and gains the smaller pmf(k+w)),
+// and P(X >= k) >= P_w(max(k, mode)) for every k, so every cell with
+// k < kthr has ln p > tau (the margin of 0.002 nats covers the FP32 error,
+// <= 1.1e-4 nats).  A task then needs, per cell, one shared-memory counter
+// load, two adds and one compare against the table row held in registers.
+//
+// A task is accepted when some cell's stage-2 upper bound reaches tau: the
+// FP64 argmin then lies among the hits (cells with k >= kthr).  Each hit is
+// rechecked with the fixed-point log-pmf bound against the task's running B
+// and goes through stage 2 (FP32 tail interval) and stage 3 (FP64) exactly as
+// in the exhaustive screen (dto_grid.cuh).  A task whose minimum lies above
+// tau is appended to a fallback list that the exhaustive screen processes.
+#pragma once
+#include "dto_grid.cuh"
+
+namespace dto {
+
+constexpr double kTableMargin = 0.002;  // nats added to tau when the table is built
+
+__host__ __device__ constexpr int table_cq(int C) { return (C + 7) & ~7; }
+
+// One thread per cell: binary search for the first overlap that passes.
+static __global__ void table_build_kernel(const TableArgs A) {
+  const int Cq = table_cq(A.C);
+  const long long cells = (long long)A.n1 * 32 * Cq;
+  const double scale = ldexp(1.0, A.fshift);
+  const int tauT = A.tau + (int)ceil(kTableMargin * scale);
+  const uint32_t FN = __ldg(A.F + A.N);
+  for (long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x; c < cells;
+       c += (long long)gridDim.x * blockDim.x) {
+    const int i = (int)(c / (32 * Cq));
+    const int rem = (int)(c % (32 * Cq));
+    const int lane = rem / Cq, t = rem % Cq;
+    const int j = lane * A.C + t;
+    uint16_t out = 0xFFFF;
+    if (t < A.C && j < A.n2) {
+      const int K = __ldg(A.rowstart + i + 1);
+      const int n = __ldg(A.ncnt + j);
+      const int a = min(K, n), b = max(K, n);
+      const long long mode = ((long long)(a + 1) * (long long)(b + 1)) / (long long)(A.N + 2);
+      if (lbt_fix(A.F, A.N, FN, K, n, (int)mode, mode, scale) <= tauT) {
+        out = 0;
+      } else {
+        // invariant: pred(lo) false, pred(hi) true or hi = a + 1
+        int lo = (int)mode, hi = a + 1;
+        while (hi - lo > 1) {
+          int mid = lo + (hi - lo) / 2;
+          if (lbt_fix(A.F, A.N, FN, K, n, mid, mode, scale) <= tauT) hi = mid;
+          else lo = mid;
+        }
+        out = (uint16_t)min(hi, 0xFFFF);
+      }
+    }
+    A.kthr[c] = out;
+  }
+}
+
+constexpr int kTableSurvCap = 64;
+
+// Per-warp state of the current task, in shared memory: the hot sweep never
+// touches it; only the (rare) hit path and the task end do.
+struct WarpTask {
+  int B;        // running bound (fixed-point ln p)
+  int B_valid;  // some cell's stage-2 upper bound reached B
+  int ncand, nsurv;
+  double bp;    // FP64 best so far
+  int bk, bi, bj;
+  int pad;
+  unsigned long long n32, n64;
+};
+
+__host__ __device__ constexpr int table_warp_ints(int C) {
+  return grid_cnt_ints(C) + 32 + 2 * kCandCap + 3 * kTableSurvCap + (int)(sizeof(WarpTask) / 4);
+}
+
+struct TableWarpMem {
+  int* cnt;
+  int* tot;
+  int2* cand;
+  int* survCell;
+  int* survK;
+  int* survLo;
+  WarpTask* st;
+};
+
+__device__ __forceinline__ TableWarpMem table_warp_mem(int* base, int C) {
+  TableWarpMem m;
+  m.cnt = base;
+  m.tot = base + grid_cnt_ints(C);
+  m.cand = reinterpret_cast<int2*>(m.tot + 32);
+  m.survCell = reinterpret_cast<int*>(m.cand + kCandCap);
+  m.survK = m.survCell + kTableSurvCap;
+  m.survLo = m.survK + kTableSurvCap;
+  m.st = reinterpret_cast<WarpTask*>(m.survLo + kTableSurvCap);
+  return m;
+}
+
+// Stage 3 on the survivors the current B admits.
+static __device__ __noinline__ void table_refine(const TableGridArgs& A, const int* sRow, const TableWarpMem& m,
+                                          int lane) {
+  __syncwarp();
+  WarpTask st = *m.st;
+  Best lb{st.bp, st.bk, st.bi, st.bj};
+  int done = 0;
+  for (int q = lane; q < st.nsurv; q += 32) {
+    if (m.survLo[q] <= st.B + 1) {
+      int ci = m.survCell[q] >> 16, cj = m.survCell[q] & 0xffff;
+      double p = sf64(A.P.LF, A.P.Npop, sRow[ci + 1], __ldg(A.P.ncnt + cj), m.survK[q]);
+      best_take(lb, p, m.survK[q], ci, cj);
+      ++done;
+    }
+  }
+#pragma unroll
+  for (int d = 16; d > 0; d >>= 1) done += __shfl_xor_sync(kFull, done, d);
+  warp_best(lb);
+  __syncwarp();
+  if (lane == 0) {
+    m.st->bp = lb.p;
+    m.st->bk = lb.k;
+    m.st->bi = lb.i;
+    m.st->bj = lb.j;
+    m.st->nsurv = 0;
+    m.st->n64 += (unsigned long long)done;
+  }
+  __syncwarp();
+}
+
+// Stage 2 on the candidate buffer.
+static __device__ __noinline__ void table_flush(const TableGridArgs& A, const int* sRow, const TableWarpMem& m,
+                                         int lane) {
+  __syncwarp();
+  const int N = (int)A.P.Npop;
+  const uint32_t* F = A.P.F;
+  const uint32_t FN = __ldg(F + N);
+  const double scale = ldexp(1.0, A.P.fshift);
+  const int Bfloor = (int)floor(-700.0 * scale);
+  const int ncand = m.st->ncand;
+  int B = m.st->B;
+  int B_valid = m.st->B_valid;
+  for (int q0 = 0; q0 < ncand; q0 += 32) {
+    int q = q0 + lane;
+    Interval iv{0x7fffffff, 0x7fffffff};
+    int2 c = make_int2(0, 0);
+    if (q < ncand) {
+      c = m.cand[q];
+      int ci = c.x >> 16, cj = c.x & 0xffff;
+      iv = eval32_filtered(F, N, FN, sRow[ci + 1], __ldg(A.P.ncnt + cj), c.y, scale, B);
+    }
+    int h = iv.hi;
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1) h = min(h, __shfl_xor_sync(kFull, h, d));
+    if (h <= B) {
+      B = max(h, Bfloor);
+      B_valid = 1;
+    }
+    bool keep = (q < ncand) && iv.lo <= B + 1;
+    unsigned msk = __ballot_sync(kFull, keep);
+    int nk = __popc(msk);
+    int nsurv = m.st->nsurv;
+    if (nsurv + nk > kTableSurvCap) {
+      __syncwarp();
+      if (lane == 0) m.st->B = B;
+      table_refine(A, sRow, m, lane);
+      nsurv = 0;
+    }
+    if (keep) {
+      int pos = nsurv + __popc(msk & ((1u << lane) - 1u));
+      m.survCell[pos] = c.x;
+      m.survK[pos] = c.y;
+      m.survLo[pos] = iv.lo;
+    }
+    __syncwarp();
+    if (lane == 0) m.st->nsurv = nsurv + nk;
+    __syncwarp();
+  }
+  __syncwarp();
+  if (lane == 0) {
+    m.st->B = B;
+    m.st->B_valid = B_valid;
+    m.st->ncand = 0;
+    m.st->n32 += (unsigned long long)ncand;
+  }
+  __syncwarp();
+}
+
+// The hits of row i: recheck against the running B with the fixed-point
+// log-pmf bound, then append to the candidate buffer (flushing when full).
+template <int C>
+__device__ __noinline__ void table_row_hits(const TableGridArgs& A, const int* sRow, const TableWarpMem& m,
+                                            int lane, int i, int k0, unsigned hit) {
+  constexpr int Cp = C | 1;
+  __syncwarp();
+  const int N = (int)A.P.Npop;
+  const uint32_t* F = A.P.F;
+  const uint32_t FN = __ldg(F + N);
+  const int K = sRow[i + 1];
+  const int NK = N - K;
+  const uint32_t Arow = __ldg(F + K) + __ldg(F + NK) - FN;
+  const float Kf = (float)K;
+  const float invN = 1.0f / (float)N;
+  const int tau = m.st->B + kScreenSlack + 1;
+  int kk = k0;
+  unsigned keep = 0;
+  int ks[C];
+#pragma unroll
+  for (int t = 0; t < C; ++t) {
+    kk += m.cnt[lane * Cp + t];
+    ks[t] = kk;
+  }
+#pragma unroll
+  for (int t = 0; t < C; ++t) {
+    if ((hit & (1u << t)) && lane * C + t < A.P.n2) {
+      const int n = __ldg(A.P.ncnt + lane * C + t);
+      const uint32_t Bcol = __ldg(F + n) + __ldg(F + N - n);
+      if (lb_fix(F, K, NK, Arow, Kf, n, Bcol, (float)n * invN, ks[t]) <= tau) keep |= 1u << t;
+    }
+  }
+  while (__any_sync(kFull, keep != 0)) {
+    int cntHit = __popc(keep);
+    int inc2 = cntHit;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+      int y = __shfl_up_sync(kFull, inc2, d);
+      if (lane >= d) inc2 += y;
+    }
+    int total = __shfl_sync(kFull, inc2, 31);
+    int ncand = m.st->ncand;
+    int room = kCandCap - ncand;
+    int pos = ncand + inc2 - cntHit;
+#pragma unroll
+    for (int t = 0; t < C; ++t) {
+      if (keep & (1u << t)) {
+        if (pos < kCandCap) {
+          m.cand[pos] = make_int2((i << 16) | (lane * C + t), ks[t]);
+          keep &= ~(1u << t);
+        }
+        ++pos;
+      }
+    }
+    __syncwarp();
+    if (lane == 0) m.st->ncand = ncand + min(total, room);
+    __syncwarp();
+    if (m.st->ncand >= kCandCap - 32 || __any_sync(kFull, keep != 0)) table_flush(A, sRow, m, lane);
+  }
+}
+
+template <int C>
+__global__ void __launch_bounds__(kTableWarps * 32, 2) table_grid_kernel(const TableGridArgs A) {
+  constexpr int Cp = C | 1;
+  constexpr int Cq = table_cq(C);
+  constexpr int NQ = Cq / 8;  // uint4 loads per lane per row
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int n1 = A.P.n1;
+
+  int* sRow = reinterpret_cast<int*>(smem_raw);
+  int* sWarp = sRow + ((n1 + 1 + 3) & ~3);
+  const TableWarpMem m = table_warp_mem(sWarp + warp * table_warp_ints(C), C);
+  for (int q = threadIdx.x; q <= n1; q += blockDim.x) sRow[q] = __ldg(A.P.rowstart + q);
+  if (lane == 0) {
+    m.st->n32 = 0;
+    m.st->n64 = 0;
+  }
+  __syncthreads();
+  const uint4* ktab = reinterpret_cast<const uint4*>(A.kthr);
+  unsigned long long nfall = 0;
+
+  const int ntask = A.ntask_dev ? *((volatile const int*)A.ntask_dev) : A.ntask;
+  for (;;) {
+    int b = 0;
+    if (lane == 0) b = atomicAdd(A.work, 1);
+    b = __shfl_sync(kFull, b, 0);
+    if (b >= ntask) break;
+    if (A.task_list) b = A.task_list[b];
+    const int16_t* x = A.X + (long long)b * A.xstride;
+    if (lane == 0) {
+      m.st->B = A.tau;
+      m.st->B_valid = 0;
+      m.st->ncand = 0;
+      m.st->nsurv = 0;
+      Best z = best_init();
+      m.st->bp = z.p;
+      m.st->bk = z.k;
+      m.st->bi = z.i;
+      m.st->bj = z.j;
+    }
+    for (int q = lane; q < 32 * Cp; q += 32) m.cnt[q] = 0;
+    m.tot[lane] = 0;
+    __syncwarp();
+    int s = sRow[0], e = sRow[1];
+    int pre = (s + lane < e) ? (int)__ldg(x + s + lane) : -1;
+    uint4 kt[NQ], ktn[NQ];
+#pragma unroll
+    for (int u = 0; u < NQ; ++u) kt[u] = __ldg(ktab + (size_t)lane * NQ + u);
+    for (int i = 0; i < n1; ++i) {
+      const int cur = pre;
+      const int sN = e;
+      const int eN = (i + 2 <= n1) ? sRow[i + 2] : e;
+      pre = (sN + lane < eN) ? (int)__ldg(x + sN + lane) : -1;
+      if (i + 1 < n1) {
+#pragma unroll
+        for (int u = 0; u < NQ; ++u) ktn[u] = __ldg(ktab + ((size_t)(i + 1) * 32 + lane) * NQ + u);
+      }
+      if (cur >= 0) {
+        atomicAdd(&m.cnt[cur], 1);
+        atomicAdd(&m.tot[cur / Cp], 1);
+      }
+      for (int p = s + 32 + lane; p < e; p += 32) {
+        int v = __ldg(x + p);
+        if (v >= 0) {
+          atomicAdd(&m.cnt[v], 1);
+          atomicAdd(&m.tot[v / Cp], 1);
+        }
+      }
+      __syncwarp();
+      const int mine = m.tot[lane];
+      int incl = mine;
+#pragma unroll
+      for (int d = 1; d < 32; d <<= 1) {
+        int y = __shfl_up_sync(kFull, incl, d);
+        if (lane >= d) incl += y;
+      }
+      const int k0 = incl - mine;  // overlap before this lane's first column
+      int k = k0;
+      unsigned hit = 0;
+#pragma unroll
+      for (int t = 0; t < C; ++t) {
+        k += m.cnt[lane * Cp + t];
+        const uint4 v = kt[t / 8];
+        const uint32_t w = ((t % 8) / 2 == 0) ? v.x : ((t % 8) / 2 == 1) ? v.y : ((t % 8) / 2 == 2) ? v.z : v.w;
+        const int thr = (t & 1) ? (int)(w >> 16) : (int)(w & 0xFFFFu);
+        hit |= (k >= thr) ? (1u << t) : 0u;
+      }
+      if (__any_sync(kFull, hit != 0)) table_row_hits<C>(A, sRow, m, lane, i, k0, hit);
+      __syncwarp();
+#pragma unroll
+      for (int u = 0; u < NQ; ++u) kt[u] = ktn[u];
+      s = sN;
+      e = eN;
+    }
+    if (m.st->ncand > 0) table_flush(A, sRow, m, lane);
+    if (m.st->B_valid) {
+      table_refine(A, sRow, m, lane);
+      if (lane == 0) A.out[b] = TaskResult{m.st->bp, m.st->bi, m.st->bj, m.st->bk, 0};
+    } else {
+      // every cell's ln p lies above the guess: hand the task to the
+      // exhaustive screen
+      if (lane == 0) A.fallback[atomicAdd(A.nfallback, 1)] = b;
+      ++nfall;
+    }
+    __syncwarp();
+  }
+  if (lane == 0 && A.n_refined) {
+    atomicAdd(A.n_refined, m.st->n64);
+    atomicAdd(A.n_refined + 1, m.st->n32);
+    atomicAdd(A.n_refined + 2, nfall);
+  }
+}
+
+template <int C>
+cudaError_t launch_table_grid_impl(const TableGridArgs& a, int ctas, size_t smem, cudaStream_t s) {
+  cudaError_t e = cudaFuncSetAttribute(table_grid_kernel<C>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  table_grid_kernel<C><<<ctas, kTableWarps * 32, smem, s>>>(a);
+  return cudaGetLastError();
+}
+
+}  // namespace dto
+
+#define DTO_DEFINE_TABLE_GRID(CC)                                                                     \
+  namespace dto {                                                                                     \
+  cudaError_t launch_table_grid_c##CC(const TableGridArgs& a, int ctas, size_t smem, cudaStream_t s) { \
+    return launch_table_grid_impl<CC>(a, ctas, smem, s);                                              \
+  }                                                                                                   \
+  }

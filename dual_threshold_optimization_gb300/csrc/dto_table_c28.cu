@@ -1,0 +1,3 @@
+// Table-screen kernel instantiation for 28 columns per lane.
+#include "dto_table.cuh"
+DTO_DEFINE_TABLE_GRID(28)

@@ -168,3 +168,16 @@ def test_grid_dump_matches_oracle_records(engine):
     for q, o in enumerate(allr):
         g = dict(zip(recs.dtype.names, recs[q].tolist()))
         assert_same(g, o, "cell %d" % q)
+
+
+def test_table_screen_equals_fp64_many_permutations(engine):
+    # enough permutations that the run switches to the table screen after its
+    # first batch; every permutation's optimum must equal the plain FP64 path's
+    p = synth.copula_pair(900, 0.2, seed=51, frac_tied2=0.05)
+    dp = engine.pair(p.ranks1, p.feat1, p.ranks2, p.feat2, p.n_features, p.population)
+    P = 7400
+    a = dp.run(P, seed=123, precision="screen", want_records=True)
+    b = dp.run(P, seed=123, precision="fp64", want_records=True)
+    assert a.unpermuted == b.unpermuted
+    assert np.array_equal(a.records, b.records)
+    assert a.summary["n_fallback"] > 0  # the 90th-percentile guess leaves ~10% to the exhaustive screen
