@@ -26,7 +26,7 @@ PRECISION_SCREEN = 1
 EXPORTS = (
     "dto_version", "dto_status_string", "dto_ctx_create", "dto_ctx_destroy", "dto_last_error",
     "dto_ctx_stream", "dto_generate_thresholds", "dto_pair_create", "dto_pair_destroy",
-    "dto_pair_info", "dto_pair_thresholds", "dto_pair_order", "dto_pair_upload_bytes", "dto_pair_set_stream", "dto_run", "dto_run_range",
+    "dto_pair_info", "dto_pair_thresholds", "dto_pair_order", "dto_pair_upload_bytes", "dto_pair_set_stream", "dto_run", "dto_run_range", "dto_run_range_noalloc",
     "dto_optimize",
     "dto_grid_dump", "dto_hypergeom_sf", "dto_export_permutations", "dto_fdr",
 )
@@ -103,6 +103,8 @@ def lib():
                           _P, C.POINTER(DtoSummary)]
     L.dto_run_range.argtypes = [_P, _P, C.c_uint32, C.c_int64, C.c_uint64, _P, C.c_int,
                                 C.POINTER(DtoResult), _P, _P, C.POINTER(DtoSummary)]
+    L.dto_run_range_noalloc.argtypes = [_P, _P, C.c_uint32, C.c_int64, C.c_uint64, _P]
+    L.dto_run_range_noalloc.restype = C.c_int
     L.dto_optimize.argtypes = [_P, _P, C.c_int, C.c_uint64, C.c_uint32, _P, _P, C.c_int,
                                C.POINTER(DtoResult)]
     L.dto_grid_dump.argtypes = [_P, _P, _P, _P, _P]

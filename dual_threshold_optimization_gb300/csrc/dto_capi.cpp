@@ -991,4 +991,89 @@ int dto_export_permutations(dto_ctx* ctx, dto_pair* P, uint64_t seed, uint32_t p
   return DTO_OK;
 }
 
+int dto_run_range_noalloc(dto_ctx* ctx, dto_pair* P, uint32_t perm_first, int64_t n_perm, uint64_t seed,
+                          double* d_minp) {
+  if (!ctx || !P || P->ctx != ctx || n_perm < 0 || (n_perm > 0 && !d_minp))
+    return set_err(ctx, DTO_ERR_INVALID, "dto_run_range_noalloc: null argument");
+  if ((long long)perm_first + n_perm > 0xffffffffLL)
+    return set_err(ctx, DTO_ERR_INVALID, "dto_run_range_noalloc: permutation ids out of range");
+  std::lock_guard<std::mutex> g(ctx->mu);
+  CK(cudaSetDevice(ctx->device));
+  void* base = nullptr;
+  size_t cap = 0;
+  CK(noalloc_scratch(ctx->device, &base, &cap));
+  if (n_perm == 0) return DTO_OK;
+  auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
+  const long long xs = xstride_of(P->N1);
+  const size_t per_perm = sizeof(TaskResult) + (size_t)xs * 2 + (P->same_set ? 0 : (size_t)(P->N1 + P->N2) * 4);
+  const size_t off_res = 256;
+  const size_t off_x = off_res + al((size_t)n_perm * sizeof(TaskResult));
+  const size_t off_sig = off_x + al((size_t)n_perm * xs * 2);
+  const size_t end = off_sig + (P->same_set ? 0 : al((size_t)n_perm * (P->N1 + P->N2) * 4));
+  if (end > cap) {
+    const long long most = (long long)((cap - 256 - 3 * 256) / per_perm);
+    char msg[256];
+    std::snprintf(msg, sizeof(msg),
+                  "dto_run_range_noalloc: n_perm %lld exceeds the %zu-byte device scratch; at most %lld "
+                  "permutations of this pair per call",
+                  (long long)n_perm, cap, most);
+    return set_err(ctx, DTO_ERR_INVALID, msg);
+  }
+  unsigned char* b8 = (unsigned char*)base;
+  int* work = (int*)b8;
+  TaskResult* res = (TaskResult*)(b8 + off_res);
+  int16_t* X = (int16_t*)(b8 + off_x);
+  int* sig = (int*)(b8 + off_sig);
+  const int cnt = (int)n_perm;
+  PermArgs a{};
+  a.seed = seed;
+  a.pair_id = P->pair_id;
+  a.perm_base = perm_first;
+  a.xstride = xs;
+  if (P->same_set) {
+    a.L = (int)P->N1;
+    a.list_tag = 1;
+    a.Ylab = P->dYlab;
+    a.X = X;
+    CK(launch_perm(a, cnt, ctx->stream));
+  } else {
+    const long long ss = P->N1 + P->N2;
+    a.L = (int)P->N1;
+    a.list_tag = 1;
+    a.sigma = sig;
+    a.sstride = ss;
+    CK(launch_perm(a, cnt, ctx->stream));
+    a.L = (int)P->N2;
+    a.list_tag = 2;
+    a.sigma = sig + P->N1;
+    CK(launch_perm(a, cnt, ctx->stream));
+    ComposeArgs c{};
+    c.N1 = (int)P->N1;
+    c.N2 = (int)P->N2;
+    c.idx1 = sig;
+    c.idx2 = sig + P->N1;
+    c.stride = ss;
+    c.map12 = P->dMap12;
+    c.lab2 = P->dLab2;
+    c.X = X;
+    c.xstride = xs;
+    CK(launch_compose(c, cnt, ctx->stream));
+  }
+  CK(cudaMemsetAsync(work, 0, 256, ctx->stream));  // the shared task counter starts at zero
+  GridArgs gk{};
+  gk.P = P->dev;
+  gk.P.LF = ctx->dLF;
+  gk.X = X;
+  gk.xstride = xs;
+  gk.ntask = cnt;
+  gk.mode = kModeScreen;
+  gk.smemF = grid_smem_bytes(P->C, P->dev.n1, P->npop, 1) <= ctx->smem_optin ? 1 : 0;
+  gk.out = res;
+  gk.work = work;
+  const int ctas = std::max(1, std::min(ctx->nsm, (cnt + kGridWarps - 1) / kGridWarps));
+  CK(launch_grid(gk, ctas, ctx->stream));
+  CK(launch_noalloc_copy_p(res, d_minp, cnt, ctx->stream));
+  return DTO_OK;
+}
+
 }  // extern "C"

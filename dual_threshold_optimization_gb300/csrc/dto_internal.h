@@ -129,6 +129,8 @@ cudaError_t launch_table_grid(const TableGridArgs& a, int C, int ctas, cudaStrea
 cudaError_t launch_grid(const GridArgs& a, int grid_ctas, cudaStream_t s);
 cudaError_t launch_perm(const PermArgs& a, int count, cudaStream_t s);
 cudaError_t launch_compose(const ComposeArgs& a, int count, cudaStream_t s);
+cudaError_t noalloc_scratch(int device, void** ptr, size_t* bytes);
+cudaError_t launch_noalloc_copy_p(const TaskResult* r, double* out, int n, cudaStream_t s);
 cudaError_t launch_sf_batch(const double2* LF, const long long* q, double* out, long long count,
                             cudaStream_t s);
 

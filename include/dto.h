@@ -151,6 +151,24 @@ DTO_API int dto_run_range(dto_ctx* ctx, dto_pair* pair, uint32_t perm_first, int
                           dto_result* out_unpermuted, double* out_minp, dto_result* out_perm,
                           dto_summary* out_summary);
 
+/* No counterpart in the reference.  dto_run_range for callers that cannot
+ * allocate device memory when they run it -- code recording a CUDA graph, or a
+ * process whose memory manager owns every device allocation.  It calls no
+ * allocating routine: permutation labels, the task counter and the per-task
+ * optima live in a fixed 32 MiB device array inside libdto.so (held on every
+ * GPU that loads the library until the process exits).  The caller passes the
+ * pair (created beforehand with dto_pair_create) and d_minp, device memory of
+ * n_perm doubles that receives each permutation's minimum p-value (the same
+ * values as dto_run_range, exhaustive screen).  At most
+ * 32 MiB / (24 + 2 * round8(n1) [+ 4 (n1 + n2) when the lists' feature sets
+ * differ]) permutations per call (about 830 at n1 = n2 = 20,000); larger
+ * n_perm -> DTO_ERR_INVALID.  The work is enqueued on the context's stream and
+ * the call returns without waiting.  The first call on a device resolves the
+ * array's device address and should come before any stream capture.  Calls
+ * share the array: calls whose GPU work overlaps race. */
+DTO_API int dto_run_range_noalloc(dto_ctx* ctx, dto_pair* pair, uint32_t perm_first, int64_t n_perm,
+                                  uint64_t seed, double* d_minp);
+
 /* One task: optimize(list1, list2, permute, population, debug=false)
  * (src/dto/optimize_main.rs:53-118).  permute != 0 uses permutation perm_id of
  * seed, or idx1/idx2 when both are non-NULL. */
