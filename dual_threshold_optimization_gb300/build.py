@@ -58,8 +58,9 @@ def build(force=False, verbose=False, jobs=None):
     flags = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
                     "-Xcompiler", "-ffp-contract=off", "-Xcompiler", "-fvisibility=hidden",
                     "-I", INCLUDE, "-I", CSRC]
-    if os.environ.get("DTO_GRID_WARPS"):
-        flags += ["-DDTO_GRID_WARPS=%d" % int(os.environ["DTO_GRID_WARPS"])]
+    for knob in ("DTO_GRID_WARPS", "DTO_PERM_THREADS", "DTO_BUCKET_BITS"):
+        if os.environ.get(knob):
+            flags += ["-D%s=%d" % (knob, int(os.environ[knob]))]
     if verbose:
         flags += ["-Xptxas", "-v"]
     srcs = _sources()

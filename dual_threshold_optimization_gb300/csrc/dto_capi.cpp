@@ -26,6 +26,8 @@ struct dto_ctx {
   int nsm = 0;
   size_t smem_optin = 0;
   cudaStream_t stream = nullptr;
+  cudaStream_t side = nullptr;  // the unpermuted task runs here next to the first batch
+  cudaEvent_t evSide = nullptr;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   cudaEvent_t evk[4] = {nullptr, nullptr, nullptr, nullptr};  // perm start/end, grid start/end
   // per-call accounting (reset by dto_run)
@@ -51,6 +53,8 @@ struct dto_ctx {
   unsigned* dGuess = nullptr;  // bound histogram shared by the batches of one run
   void* dFall = nullptr;       // fallback task lists of the two table levels
   size_t fallBytes = 0;
+  void* dHits = nullptr;       // per-warp hit buffers of the table screen
+  size_t hitBytes = 0;
   int* dNFall = nullptr;
 };
 
@@ -72,9 +76,9 @@ struct dto_pair {
   int16_t* dYlab = nullptr;
   int16_t* dLab2 = nullptr;
   int* dMap12 = nullptr;
-  uint16_t* dKthr[2] = {nullptr, nullptr};  // table screens, built for bounds kthr_tau
-  int kthr_tau[2] = {0, 0};
-  bool kthr_ok[2] = {false, false};
+  uint16_t* dKthr[3] = {nullptr, nullptr, nullptr};  // table screens, built for bounds kthr_tau
+  int kthr_tau[3] = {0, 0, 0};
+  bool kthr_ok[3] = {false, false, false};
   PairDev dev{};
 };
 
@@ -299,24 +303,27 @@ int ensure_table(dto_ctx* ctx, dto_pair* P, int level, int tau) {
   return DTO_OK;
 }
 
-// Tasks [0, ntask) of ctx->dX through the table ladder: level 0 (bound at the
-// first batch's 90th percentile), then its fallbacks through level 1 (bound
-// one nat above the first batch's largest minimum), then the rest through the
-// exhaustive screen.  Counts of each list stay on the device.
-int table_tasks(dto_ctx* ctx, dto_pair* P, long long xstride, int ntask, TaskResult* dOut) {
-  int rc = grow(ctx, &ctx->dFall, &ctx->fallBytes, (size_t)std::max(ntask, 1) * 8);
+// Tasks [0, ntask) of X through the table ladder: level l takes the tasks
+// that level l-1 could not settle (their minimum lies above its bound), and
+// the exhaustive screen takes what the last level leaves.  The lists and
+// their counts stay on the device.
+int table_tasks(dto_ctx* ctx, dto_pair* P, const int16_t* X, long long xstride, int ntask, TaskResult* dOut,
+                int nlev) {
+  const int cap = std::max(ntask, 1);
+  int rc = grow(ctx, &ctx->dFall, &ctx->fallBytes, (size_t)nlev * cap * 4);
   if (rc) return rc;
-  int* fall0 = (int*)ctx->dFall;
-  int* fall1 = fall0 + std::max(ntask, 1);
-  CK(cudaMemsetAsync(ctx->dWork, 0, 4 * sizeof(int), ctx->stream));
-  CK(cudaMemsetAsync(ctx->dNFall, 0, 2 * sizeof(int), ctx->stream));
+  const int hitcap = 8192;
+  rc = grow(ctx, &ctx->dHits, &ctx->hitBytes, (size_t)2 * ctx->nsm * kTableWarps * hitcap * 8);
+  if (rc) return rc;
+  int* fall = (int*)ctx->dFall;
+  CK(cudaMemsetAsync(ctx->dWork, 0, 8 * sizeof(int), ctx->stream));
+  CK(cudaMemsetAsync(ctx->dNFall, 0, 4 * sizeof(int), ctx->stream));
   CK(cudaEventRecord(ctx->evk[2], ctx->stream));
-  const int per_cta = kTableWarps;
-  for (int level = 0; level < 2; ++level) {
+  for (int level = 0; level < nlev; ++level) {
     TableGridArgs a{};
     a.P = P->dev;
     a.P.LF = ctx->dLF;
-    a.X = (const int16_t*)ctx->dX;
+    a.X = X;
     a.xstride = xstride;
     a.ntask = ntask;
     a.tau = P->kthr_tau[level];
@@ -324,31 +331,38 @@ int table_tasks(dto_ctx* ctx, dto_pair* P, long long xstride, int ntask, TaskRes
     a.out = dOut;
     a.work = ctx->dWork + level;
     a.n_refined = ctx->dRefined;
-    a.fallback = level == 0 ? fall0 : fall1;
+    a.fallback = fall + (size_t)level * cap;
     a.nfallback = ctx->dNFall + level;
-    a.task_list = level == 0 ? nullptr : fall0;
-    a.ntask_dev = level == 0 ? nullptr : ctx->dNFall;
-    int ctas = level == 0 ? std::max(1, std::min(2 * ctx->nsm, (ntask + per_cta - 1) / per_cta))
+    a.task_list = level == 0 ? nullptr : fall + (size_t)(level - 1) * cap;
+    a.ntask_dev = level == 0 ? nullptr : ctx->dNFall + level - 1;
+    a.hitbuf = (int2*)ctx->dHits;
+    a.hitcap = hitcap;
+    int ctas = level == 0 ? std::max(1, std::min(2 * ctx->nsm, (ntask + kTableWarps - 1) / kTableWarps))
                           : 2 * ctx->nsm;
     CK(launch_table_grid(a, P->C, ctas, ctx->stream));
   }
   GridArgs g{};
   g.P = P->dev;
   g.P.LF = ctx->dLF;
-  g.X = (const int16_t*)ctx->dX;
+  g.X = X;
   g.xstride = xstride;
   g.ntask = ntask;
   g.mode = kModeScreen;
   g.smemF = grid_smem_bytes(P->C, P->dev.n1, P->npop, 1) <= ctx->smem_optin ? 1 : 0;
   g.out = dOut;
-  g.work = ctx->dWork + 2;
+  g.work = ctx->dWork + nlev;
   g.n_refined = ctx->dRefined;
-  g.task_list = fall1;
-  g.ntask_dev = ctx->dNFall + 1;
+  g.task_list = fall + (size_t)(nlev - 1) * cap;
+  g.ntask_dev = ctx->dNFall + nlev - 1;
   CK(launch_grid(g, ctx->nsm, ctx->stream));
   CK(cudaEventRecord(ctx->evk[3], ctx->stream));
-  ctx->acc_launches += 3;
+  ctx->acc_launches += nlev + 1;
   return DTO_OK;
+}
+
+int fixed_log(double p, int fshift) {
+  double t = std::floor(std::log(p) * std::ldexp(1.0, fshift));
+  return (int)std::max(-2.0e9, std::min(0.0, t));
 }
 
 // Labels of n_perm permutations starting at perm id `first` into ctx->dX.
@@ -464,6 +478,8 @@ int dto_ctx_create(int device, dto_ctx** out) {
   ctx->nsm = prop.multiProcessorCount;
   ctx->smem_optin = prop.sharedMemPerBlockOptin;
   if ((e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking)) != cudaSuccess) return fail(e);
+  if ((e = cudaStreamCreateWithFlags(&ctx->side, cudaStreamNonBlocking)) != cudaSuccess) return fail(e);
+  if ((e = cudaEventCreateWithFlags(&ctx->evSide, cudaEventDisableTiming)) != cudaSuccess) return fail(e);
   if ((e = cudaEventCreate(&ctx->ev0)) != cudaSuccess) return fail(e);
   if ((e = cudaEventCreate(&ctx->ev1)) != cudaSuccess) return fail(e);
   for (int q = 0; q < 4; ++q)
@@ -489,11 +505,14 @@ int dto_ctx_destroy(dto_ctx* ctx) {
   cudaFree(ctx->dRefined);
   cudaFree(ctx->dGuess);
   cudaFree(ctx->dFall);
+  cudaFree(ctx->dHits);
   cudaFree(ctx->dNFall);
   if (ctx->ev0) cudaEventDestroy(ctx->ev0);
   if (ctx->ev1) cudaEventDestroy(ctx->ev1);
   for (int q = 0; q < 4; ++q)
     if (ctx->evk[q]) cudaEventDestroy(ctx->evk[q]);
+  if (ctx->evSide) cudaEventDestroy(ctx->evSide);
+  if (ctx->side) cudaStreamDestroy(ctx->side);
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
   delete ctx;
   return DTO_OK;
@@ -525,7 +544,7 @@ int dto_pair_create(dto_ctx* ctx, const uint32_t* ranks1, const int32_t* feat1, 
   if (n1 <= 0 || n2 <= 0 || !ranks1 || !ranks2 || !feat1 || !feat2)
     return set_err(ctx, DTO_ERR_INVALID, "empty ranked feature list");
   if (n1 > kMaxListLen || n2 > kMaxListLen)
-    return set_err(ctx, DTO_ERR_INVALID, "ranked feature lists are limited to 65536 features");
+    return set_err(ctx, DTO_ERR_INVALID, "ranked feature lists are limited to 65534 features");
   if (population <= 0 || population > 4000000)
     return set_err(ctx, DTO_ERR_INVALID, "population size must lie in [1, 4000000]");
   if (n_features <= 0) return set_err(ctx, DTO_ERR_INVALID, "n_features must be positive");
@@ -663,8 +682,7 @@ int dto_pair_destroy(dto_pair* P) {
   cudaFree(P->dYlab);
   cudaFree(P->dLab2);
   cudaFree(P->dMap12);
-  cudaFree(P->dKthr[0]);
-  cudaFree(P->dKthr[1]);
+  for (int l = 0; l < 3; ++l) cudaFree(P->dKthr[l]);
   delete P;
   return DTO_OK;
 }
@@ -748,12 +766,15 @@ int dto_run_range(dto_ctx* ctx, dto_pair* P, uint32_t perm_first, int64_t n_perm
   // concurrently with the first permutations.
   std::vector<double> minp((size_t)n_perm);
   TaskResult unperm{};
-  // The first batch (the unpermuted task and up to first_batch permutations)
-  // goes through the exhaustive screen; its 90th-percentile bound then builds
-  // the table screen used by the remaining batches.
-  const long long first_batch = (long long)ctx->nsm * kGridWarps * 2;
+  // Without the table screen, the unpermuted task (task 0) rides in row 0 of
+  // the first batch of the exhaustive screen.  With it, the first batch of
+  // first_batch permutations goes through tables built for fixed bounds
+  // (ln 0.05, ln 0.5) while task 0 runs through the exhaustive screen on the
+  // side stream; the first batch's 90th and 99th percentiles and maximum then
+  // set the three-level table ladder for the remaining batches.
+  const long long first_batch = 1024;
   const bool use_table = (mode == kModeScreen) && n_perm > 2 * first_batch;
-  bool table_ready = false;
+  int nlev = 0;
   long long step = use_table ? first_batch : batch;
   for (long long b0 = 0; b0 < std::max<long long>(n_perm, 1); b0 += step, step = batch) {
     const int row0 = (b0 == 0) ? 1 : 0;
@@ -777,9 +798,41 @@ int dto_run_range(dto_ctx* ctx, dto_pair* P, uint32_t perm_first, int64_t n_perm
     }
     if (row0) CK(cudaMemcpyAsync(ctx->dX, P->dYlab, (size_t)P->N1 * 2, cudaMemcpyDeviceToDevice, ctx->stream));
     const int ntask = cnt + row0;
-    if (table_ready) rc = table_tasks(ctx, P, xs, ntask, dRes);
-    else rc = grid_tasks(ctx, P, (const int16_t*)ctx->dX, xs, ntask, mode, dRes, nullptr, nullptr, true);
-    if (rc) return rc;
+    const int16_t* X = (const int16_t*)ctx->dX;
+    if (use_table) {
+      if (row0) {
+        // task 0 on the side stream, after its labels are in place
+        CK(cudaEventRecord(ctx->evSide, ctx->stream));
+        CK(cudaStreamWaitEvent(ctx->side, ctx->evSide, 0));
+        GridArgs g{};
+        g.P = P->dev;
+        g.P.LF = ctx->dLF;
+        g.X = X;
+        g.xstride = xs;
+        g.ntask = 1;
+        g.mode = kModeScreen;
+        g.smemF = grid_smem_bytes(P->C, P->dev.n1, P->npop, 1) <= ctx->smem_optin ? 1 : 0;
+        g.out = dRes;
+        g.work = ctx->dWork + 16;
+        g.n_refined = ctx->dRefined;
+        CK(cudaMemsetAsync(ctx->dWork + 16, 0, sizeof(int), ctx->side));
+        CK(launch_grid(g, 1, ctx->side));
+        ctx->acc_launches += 1;
+        CK(cudaEventRecord(ctx->evSide, ctx->side));
+        const int sc = P->fshift;
+        rc = ensure_table(ctx, P, 0, fixed_log(0.05, sc));
+        if (rc) return rc;
+        rc = ensure_table(ctx, P, 1, fixed_log(0.5, sc));
+        if (rc) return rc;
+        nlev = 2;
+      }
+      rc = table_tasks(ctx, P, X + (size_t)row0 * xs, xs, cnt, dRes + row0, nlev);
+      if (rc) return rc;
+      if (row0) CK(cudaStreamWaitEvent(ctx->stream, ctx->evSide, 0));
+    } else {
+      rc = grid_tasks(ctx, P, X, xs, ntask, mode, dRes, nullptr, nullptr, true);
+      if (rc) return rc;
+    }
     CK(cudaMemcpyAsync(hRes, dRes, (size_t)ntask * sizeof(TaskResult), cudaMemcpyDeviceToHost, ctx->stream));
     ctx->acc_d2h += (long long)ntask * (long long)sizeof(TaskResult);
     CK(cudaStreamSynchronize(ctx->stream));
@@ -795,23 +848,24 @@ int dto_run_range(dto_ctx* ctx, dto_pair* P, uint32_t perm_first, int64_t n_perm
       if (out_minp) out_minp[b0 + q] = r.p;
       if (out_perm) fill_result(P, r, 1, &out_perm[b0 + q]);
     }
-    if (use_table && !table_ready && cnt >= 256) {
+    if (use_table && row0 && cnt >= 256) {
       std::vector<double> v(minp.begin() + b0, minp.begin() + b0 + cnt);
-      size_t q90 = (size_t)(0.9 * (double)(v.size() - 1));
-      std::nth_element(v.begin(), v.begin() + q90, v.end());
-      const double pq = v[q90];
-      const double pmax = *std::max_element(v.begin(), v.end());
-      const double sc = std::ldexp(1.0, P->fshift);
-      if (pq > 1e-300 && pmax < 1.0) {
-        const double t0 = std::floor(std::log(pq) * sc);
-        const double t1 = std::floor(std::min(std::log(pmax) + 1.0, 0.0) * sc);
-        if (t0 > -2.0e9 && t1 < 2.0e9) {
-          rc = ensure_table(ctx, P, 0, (int)t0);
-          if (rc) return rc;
-          rc = ensure_table(ctx, P, 1, (int)t1);
-          if (rc) return rc;
-          table_ready = true;
-        }
+      std::sort(v.begin(), v.end());
+      const double p90 = v[(size_t)(0.90 * (double)(v.size() - 1))];
+      const double p99 = v[(size_t)(0.99 * (double)(v.size() - 1))];
+      const double pmax = v.back();
+      if (p90 > 1e-300) {
+        const int sc = P->fshift;
+        const int t0 = fixed_log(p90, sc);
+        const int t1 = std::max(fixed_log(p99, sc), t0 + 1);
+        const int t2 = std::max((int)std::min(0.0, std::floor((std::log(pmax) + 1.0) * std::ldexp(1.0, sc))), t1 + 1);
+        rc = ensure_table(ctx, P, 0, t0);
+        if (rc) return rc;
+        rc = ensure_table(ctx, P, 1, t1);
+        if (rc) return rc;
+        rc = ensure_table(ctx, P, 2, t2);
+        if (rc) return rc;
+        nlev = 3;
       }
     }
   }

@@ -10,9 +10,18 @@ namespace dto {
 #endif
 constexpr int kGridWarps = DTO_GRID_WARPS;  // warps per CTA of the grid kernel (one task per warp)
 constexpr int kCandCap = 64;         // per-warp candidate buffer of the screen
-constexpr int kPermThreads = 1024;   // threads per CTA of the permutation kernel
-constexpr int kBuckets = 1024;       // Rao-Sandelius buckets (one per thread)
-constexpr int kMaxListLen = 65536;   // positions are stored as uint16 in shared memory
+#ifndef DTO_PERM_THREADS
+#define DTO_PERM_THREADS 1024
+#endif
+#ifndef DTO_BUCKET_BITS
+#define DTO_BUCKET_BITS 12
+#endif
+constexpr int kPermThreads = DTO_PERM_THREADS;  // threads per CTA of the permutation kernel
+constexpr int kBucketBits = DTO_BUCKET_BITS;
+constexpr int kBuckets = 1 << kBucketBits;  // Rao-Sandelius buckets
+static_assert(kBuckets % kPermThreads == 0 && kPermThreads % 32 == 0 && kPermThreads <= 1024,
+              "perm_kernel: buckets must split evenly over its warps");
+constexpr int kMaxListLen = 65534;   // positions are uint16; overlaps stay below the 0xFFFF "never" mark
 constexpr int kScreenSlack = 5;      // fixed-point units added to the screen threshold
 constexpr int kSurvCap = 256;        // per-warp survivors of the FP32 stage
 
@@ -119,6 +128,8 @@ struct TableGridArgs {
   int* nfallback;         // count (zeroed before the launch)
   const int* task_list;   // nullable: task q is row/result task_list[q]
   const int* ntask_dev;   // nullable: the task count, read on the device
+  int2* hitbuf;           // [gridDim.x * kTableWarps][hitcap] hits (packed cell, overlap)
+  int hitcap;
 };
 
 size_t grid_smem_bytes(int C, int n1, long long Npop, int smemF);

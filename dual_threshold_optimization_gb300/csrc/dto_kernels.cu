@@ -5,7 +5,7 @@
 // (src/collections/permuted.rs:56-60: a uniform shuffle of 0..len with
 // rand's thread_rng).  Here a permutation is a deterministic function of
 // (seed, pair id, permutation id, list tag):
-//   1. every element e draws a bucket in [0, 1024) from the top 10 bits of one
+//   1. every element e draws a bucket in [0, 4096) from the top 12 bits of one
 //      Philox4x32-10 word (counter (e/4, perm, pair, 0x10000000 | tag<<24),
 //      word e%4, key = the two halves of the seed);
 //   2. elements are grouped by bucket, in increasing element order inside a
@@ -58,22 +58,27 @@ struct PhiloxStream {
 
 __device__ __forceinline__ uint32_t bucket_of(uint4 w, int q) {
   uint32_t v = (q == 0) ? w.x : (q == 1) ? w.y : (q == 2) ? w.z : w.w;
-  return v >> 22;
+  return v >> (32 - kBucketBits);
 }
 
+// One CTA per permutation.  Shared memory: the bucket counters (int32,
+// kBuckets; after the scatter they hold each bucket's end) and the shuffled
+// element indices (uint16, L).  kBuckets = 4096 keeps buckets at a few
+// elements for the list lengths of interest, so the per-bucket canonical sort
+// and Fisher-Yates are a few operations per element.
 __global__ void __launch_bounds__(kPermThreads) perm_kernel(const PermArgs A) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  uint16_t* sA = reinterpret_cast<uint16_t*>(smem_raw);
-  __shared__ int cnt[kBuckets];
-  __shared__ int start[kBuckets + 1];
-  __shared__ int warpSum[kPermThreads / 32];
+  int* cnt = reinterpret_cast<int*>(smem_raw);
+  uint16_t* sA = reinterpret_cast<uint16_t*>(cnt + kBuckets);
+  __shared__ int warpTot[kPermThreads / 32];
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int L = A.L;
   const uint32_t perm = A.perm_base + blockIdx.x;
   const uint32_t k0 = (uint32_t)A.seed, k1 = (uint32_t)(A.seed >> 32);
   const uint32_t tagB = 0x10000000u | (A.list_tag << 24);
+  constexpr int kPerWarp = kBuckets / (kPermThreads / 32);
 
-  cnt[tid] = 0;
+  for (int b = tid; b < kBuckets; b += kPermThreads) cnt[b] = 0;
   __syncthreads();
   const int groups = (L + 3) >> 2;
   for (int g = tid; g < groups; g += kPermThreads) {
@@ -83,31 +88,40 @@ __global__ void __launch_bounds__(kPermThreads) perm_kernel(const PermArgs A) {
       if (4 * g + q < L) atomicAdd(&cnt[bucket_of(w, q)], 1);
   }
   __syncthreads();
-  // exclusive scan of the 1024 bucket counts
-  int v = cnt[tid];
-  int incl = v;
+  // exclusive scan of the counters: warp w scans buckets [w*kPerWarp, (w+1)*kPerWarp)
+  {
+    int carry = 0;
+    for (int r = 0; r < kPerWarp; r += 32) {
+      const int idx = warp * kPerWarp + r + lane;
+      const int v = cnt[idx];
+      int incl = v;
 #pragma unroll
-  for (int d = 1; d < 32; d <<= 1) {
-    int y = __shfl_up_sync(0xffffffffu, incl, d);
-    if (lane >= d) incl += y;
+      for (int d = 1; d < 32; d <<= 1) {
+        int y = __shfl_up_sync(0xffffffffu, incl, d);
+        if (lane >= d) incl += y;
+      }
+      cnt[idx] = carry + incl - v;
+      carry += __shfl_sync(0xffffffffu, incl, 31);
+    }
+    if (lane == 0) warpTot[warp] = carry;
   }
-  if (lane == 31) warpSum[warp] = incl;
   __syncthreads();
   if (warp == 0) {
-    int ws = warpSum[lane];
-    int wi = ws;
+    constexpr int kWarps = kPermThreads / 32;
+    const int v = lane < kWarps ? warpTot[lane] : 0;
+    int incl = v;
 #pragma unroll
     for (int d = 1; d < 32; d <<= 1) {
-      int y = __shfl_up_sync(0xffffffffu, wi, d);
-      if (lane >= d) wi += y;
+      int y = __shfl_up_sync(0xffffffffu, incl, d);
+      if (lane >= d) incl += y;
     }
-    warpSum[lane] = wi - ws;
+    if (lane < kWarps) warpTot[lane] = incl - v;
   }
   __syncthreads();
-  int excl = incl - v + warpSum[warp];
-  start[tid] = excl;
-  if (tid == kPermThreads - 1) start[kBuckets] = excl + v;
-  cnt[tid] = excl;  // reused as the fill cursor
+  {
+    const int off = warpTot[warp];
+    for (int r = 0; r < kPerWarp; r += 32) cnt[warp * kPerWarp + r + lane] += off;
+  }
   __syncthreads();
   for (int g = tid; g < groups; g += kPermThreads) {
     uint4 w = philox4x32_10(make_uint4((uint32_t)g, perm, A.pair_id, tagB), k0, k1);
@@ -121,8 +135,11 @@ __global__ void __launch_bounds__(kPermThreads) perm_kernel(const PermArgs A) {
     }
   }
   __syncthreads();
-  {
-    const int s0 = start[tid], sz = start[tid + 1] - s0;
+  // cnt[b] now holds the end of bucket b
+  for (int b = tid; b < kBuckets; b += kPermThreads) {
+    const int s0 = b == 0 ? 0 : cnt[b - 1];
+    const int sz = cnt[b] - s0;
+    if (sz < 2) continue;
     uint16_t* a = sA + s0;
     // canonical (increasing) order inside the bucket
     for (int i = 1; i < sz; ++i) {
@@ -135,7 +152,7 @@ __global__ void __launch_bounds__(kPermThreads) perm_kernel(const PermArgs A) {
       a[j + 1] = key;
     }
     PhiloxStream st;
-    st.ctr = make_uint4(0u, perm, A.pair_id, 0x20000000u | (A.list_tag << 24) | (uint32_t)tid);
+    st.ctr = make_uint4(0u, perm, A.pair_id, 0x20000000u | (A.list_tag << 24) | (uint32_t)b);
     st.k0 = k0;
     st.k1 = k1;
     st.used = 4;
@@ -235,7 +252,7 @@ cudaError_t launch_table_grid(const TableGridArgs& a, int C, int ctas, cudaStrea
 
 cudaError_t launch_perm(const PermArgs& a, int count, cudaStream_t s) {
   if (count <= 0) return cudaSuccess;
-  size_t smem = ((size_t)a.L * 2 + 15) & ~(size_t)15;
+  size_t smem = (size_t)kBuckets * 4 + (((size_t)a.L * 2 + 15) & ~(size_t)15);
   cudaError_t e = cudaFuncSetAttribute(perm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   perm_kernel<<<count, kPermThreads, smem, s>>>(a);

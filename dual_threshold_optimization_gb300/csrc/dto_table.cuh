@@ -63,6 +63,7 @@ static __global__ void table_build_kernel(const TableArgs A) {
 }
 
 constexpr int kTableSurvCap = 64;
+constexpr int kPend = 64;  // deferred FP64 evaluations per warp (several tasks)
 
 // Per-warp state of the current task, in shared memory: the hot sweep never
 // touches it; only the (rare) hit path and the task end do.
@@ -72,12 +73,15 @@ struct WarpTask {
   int ncand, nsurv;
   double bp;    // FP64 best so far
   int bk, bi, bj;
-  int pad;
+  int nhits;    // hits appended by the sweep
   unsigned long long n32, n64;
+  int npend;    // entries in the deferred FP64 queue
+  int pad2;
 };
 
 __host__ __device__ constexpr int table_warp_ints(int C) {
-  return grid_cnt_ints(C) + 32 + 2 * kCandCap + 3 * kTableSurvCap + (int)(sizeof(WarpTask) / 4);
+  return grid_cnt_ints(C) + 32 + 2 * kCandCap + 3 * kTableSurvCap + (int)(sizeof(WarpTask) / 4) +
+         5 * kPend;
 }
 
 struct TableWarpMem {
@@ -88,6 +92,10 @@ struct TableWarpMem {
   int* survK;
   int* survLo;
   WarpTask* st;
+  double* pendP;  // deferred FP64 queue: p, task, packed cell, overlap
+  int* pendTask;
+  int* pendCell;
+  int* pendK;
 };
 
 __device__ __forceinline__ TableWarpMem table_warp_mem(int* base, int C) {
@@ -99,6 +107,10 @@ __device__ __forceinline__ TableWarpMem table_warp_mem(int* base, int C) {
   m.survK = m.survCell + kTableSurvCap;
   m.survLo = m.survK + kTableSurvCap;
   m.st = reinterpret_cast<WarpTask*>(m.survLo + kTableSurvCap);
+  m.pendP = reinterpret_cast<double*>(m.st + 1);
+  m.pendTask = reinterpret_cast<int*>(m.pendP + kPend);
+  m.pendCell = m.pendTask + kPend;
+  m.pendK = m.pendCell + kPend;
   return m;
 }
 
@@ -128,6 +140,74 @@ static __device__ __noinline__ void table_refine(const TableGridArgs& A, const i
     m.st->bj = lb.j;
     m.st->nsurv = 0;
     m.st->n64 += (unsigned long long)done;
+  }
+  __syncwarp();
+}
+
+// The deferred FP64 queue: one tail per lane, then the first entry of each
+// task's run (a task's entries are contiguous) takes the task's argmin with
+// the reference's tie-break and writes its result.  Tasks share the FP64
+// instructions this way: on GB300 an FP64 warp instruction costs the same
+// whether one lane or all 32 are active.
+static __device__ __noinline__ void table_pending_flush(const TableGridArgs& A, const int* sRow,
+                                                        const TableWarpMem& m, int lane) {
+  __syncwarp();
+  const int np = m.st->npend;
+  for (int q = lane; q < np; q += 32) {
+    const int ci = m.pendCell[q] >> 16, cj = m.pendCell[q] & 0xffff;
+    m.pendP[q] = sf64(A.P.LF, A.P.Npop, sRow[ci + 1], __ldg(A.P.ncnt + cj), m.pendK[q]);
+  }
+  __syncwarp();
+  for (int q = lane; q < np; q += 32) {
+    const int task = m.pendTask[q];
+    if (q == 0 || m.pendTask[q - 1] != task) {
+      Best b = best_init();
+      for (int r = q; r < np && m.pendTask[r] == task; ++r)
+        best_take(b, m.pendP[r], m.pendK[r], m.pendCell[r] >> 16, m.pendCell[r] & 0xffff);
+      A.out[task] = TaskResult{b.p, b.i, b.j, b.k, 0};
+    }
+  }
+  __syncwarp();
+  if (lane == 0) {
+    m.st->n64 += (unsigned long long)np;
+    m.st->npend = 0;
+  }
+  __syncwarp();
+}
+
+// Queue the task's survivors that the final B admits, without duplicates
+// (a cell can reach stage 2 twice: as a seed and as a hit).
+static __device__ __noinline__ void table_defer(const TableGridArgs& A, const int* sRow, const TableWarpMem& m,
+                                                int lane, int task) {
+  __syncwarp();
+  const int B = m.st->B;
+  const int ns = m.st->nsurv;
+  if (m.st->npend + ns > kPend) table_pending_flush(A, sRow, m, lane);
+  int npend = m.st->npend;
+  for (int q0 = 0; q0 < ns; q0 += 32) {
+    const int q = q0 + lane;
+    bool keep = q < ns && m.survLo[q] <= B + 1;
+    if (keep) {
+      const int cell = m.survCell[q];
+      for (int r = 0; r < q; ++r)
+        if (m.survCell[r] == cell && m.survLo[r] <= B + 1) {
+          keep = false;
+          break;
+        }
+    }
+    const unsigned msk = __ballot_sync(kFull, keep);
+    if (keep) {
+      const int pos = npend + __popc(msk & ((1u << lane) - 1u));
+      m.pendTask[pos] = task;
+      m.pendCell[pos] = m.survCell[q];
+      m.pendK[pos] = m.survK[q];
+    }
+    npend += __popc(msk);
+  }
+  __syncwarp();
+  if (lane == 0) {
+    m.st->npend = npend;
+    m.st->nsurv = 0;
   }
   __syncwarp();
 }
@@ -190,65 +270,67 @@ static __device__ __noinline__ void table_flush(const TableGridArgs& A, const in
   __syncwarp();
 }
 
-// The hits of row i: recheck against the running B with the fixed-point
-// log-pmf bound, then append to the candidate buffer (flushing when full).
-template <int C>
-__device__ __noinline__ void table_row_hits(const TableGridArgs& A, const int* sRow, const TableWarpMem& m,
-                                            int lane, int i, int k0, unsigned hit) {
-  constexpr int Cp = C | 1;
-  __syncwarp();
+// Fixed-point lower bound of ln p for one cell from its counts alone.
+__device__ __forceinline__ int cell_lb(const uint32_t* F, int N, uint32_t FN, int K, int n, int k) {
+  const uint32_t Arow = __ldg(F + K) + __ldg(F + N - K) - FN;
+  const uint32_t Bcol = __ldg(F + n) + __ldg(F + N - n);
+  return lb_fix(F, K, N - K, Arow, (float)K, n, Bcol, (float)n * (1.0f / (float)N), k);
+}
+
+// Resolve a task from its hits (cells with k >= kthr), held in global memory.
+// The lowest stage-1 bound of each lane's hits seeds B through stage 2; then
+// every hit whose stage-1 bound is within B goes through stage 2 (behind the
+// partial-sum filter) in batches, B tightening as it goes.  The claim of
+// dto_grid.cuh applies unchanged: the FP64 argmin is among the hits and is
+// never filtered out.
+static __device__ __noinline__ void table_resolve(const TableGridArgs& A, const int* sRow,
+                                                  const TableWarpMem& m, int lane, const int2* hb, int nh) {
   const int N = (int)A.P.Npop;
   const uint32_t* F = A.P.F;
   const uint32_t FN = __ldg(F + N);
-  const int K = sRow[i + 1];
-  const int NK = N - K;
-  const uint32_t Arow = __ldg(F + K) + __ldg(F + NK) - FN;
-  const float Kf = (float)K;
-  const float invN = 1.0f / (float)N;
-  const int tau = m.st->B + kScreenSlack + 1;
-  int kk = k0;
-  unsigned keep = 0;
-  int ks[C];
-#pragma unroll
-  for (int t = 0; t < C; ++t) {
-    kk += m.cnt[lane * Cp + t];
-    ks[t] = kk;
-  }
-#pragma unroll
-  for (int t = 0; t < C; ++t) {
-    if ((hit & (1u << t)) && lane * C + t < A.P.n2) {
-      const int n = __ldg(A.P.ncnt + lane * C + t);
-      const uint32_t Bcol = __ldg(F + n) + __ldg(F + N - n);
-      if (lb_fix(F, K, NK, Arow, Kf, n, Bcol, (float)n * invN, ks[t]) <= tau) keep |= 1u << t;
+  // seed: each lane's lowest-bound hit
+  int bestLB = 0x7fffffff;
+  int2 best = make_int2(0, 0);
+  for (int q = lane; q < nh; q += 32) {
+    const int2 h = hb[q];
+    const int lb = cell_lb(F, N, FN, sRow[(h.x >> 16) + 1], __ldg(A.P.ncnt + (h.x & 0xffff)), h.y);
+    if (lb < bestLB) {
+      bestLB = lb;
+      best = h;
     }
   }
-  while (__any_sync(kFull, keep != 0)) {
-    int cntHit = __popc(keep);
-    int inc2 = cntHit;
-#pragma unroll
-    for (int d = 1; d < 32; d <<= 1) {
-      int y = __shfl_up_sync(kFull, inc2, d);
-      if (lane >= d) inc2 += y;
-    }
-    int total = __shfl_sync(kFull, inc2, 31);
-    int ncand = m.st->ncand;
-    int room = kCandCap - ncand;
-    int pos = ncand + inc2 - cntHit;
-#pragma unroll
-    for (int t = 0; t < C; ++t) {
-      if (keep & (1u << t)) {
-        if (pos < kCandCap) {
-          m.cand[pos] = make_int2((i << 16) | (lane * C + t), ks[t]);
-          keep &= ~(1u << t);
-        }
-        ++pos;
-      }
-    }
+  {
+    const bool have = bestLB != 0x7fffffff;
+    const unsigned msk = __ballot_sync(kFull, have);
     __syncwarp();
-    if (lane == 0) m.st->ncand = ncand + min(total, room);
+    if (have) m.cand[__popc(msk & ((1u << lane) - 1u))] = best;
     __syncwarp();
-    if (m.st->ncand >= kCandCap - 32 || __any_sync(kFull, keep != 0)) table_flush(A, sRow, m, lane);
+    if (lane == 0) m.st->ncand = __popc(msk);
+    __syncwarp();
+    table_flush(A, sRow, m, lane);
   }
+  // every hit within the bound
+  for (int q0 = 0; q0 < nh; q0 += 32) {
+    const int q = q0 + lane;
+    int2 h = make_int2(0, 0);
+    bool keep = false;
+    if (q < nh) {
+      h = hb[q];
+      keep = cell_lb(F, N, FN, sRow[(h.x >> 16) + 1], __ldg(A.P.ncnt + (h.x & 0xffff)), h.y) <=
+             m.st->B + kScreenSlack + 1;
+    }
+    const unsigned msk = __ballot_sync(kFull, keep);
+    if (msk) {
+      const int base = m.st->ncand;
+      __syncwarp();
+      if (keep) m.cand[base + __popc(msk & ((1u << lane) - 1u))] = h;
+      __syncwarp();
+      if (lane == 0) m.st->ncand = base + __popc(msk);
+      __syncwarp();
+      if (m.st->ncand > kCandCap - 32) table_flush(A, sRow, m, lane);
+    }
+  }
+  if (m.st->ncand > 0) table_flush(A, sRow, m, lane);
 }
 
 template <int C>
@@ -267,9 +349,11 @@ __global__ void __launch_bounds__(kTableWarps * 32, 2) table_grid_kernel(const T
   if (lane == 0) {
     m.st->n32 = 0;
     m.st->n64 = 0;
+    m.st->npend = 0;
   }
   __syncthreads();
   const uint4* ktab = reinterpret_cast<const uint4*>(A.kthr);
+  int2* hb = A.hitbuf + (size_t)(blockIdx.x * kTableWarps + warp) * A.hitcap;
   unsigned long long nfall = 0;
 
   const int ntask = A.ntask_dev ? *((volatile const int*)A.ntask_dev) : A.ntask;
@@ -285,6 +369,7 @@ __global__ void __launch_bounds__(kTableWarps * 32, 2) table_grid_kernel(const T
       m.st->B_valid = 0;
       m.st->ncand = 0;
       m.st->nsurv = 0;
+      m.st->nhits = 0;
       Best z = best_init();
       m.st->bp = z.p;
       m.st->bk = z.k;
@@ -296,6 +381,7 @@ __global__ void __launch_bounds__(kTableWarps * 32, 2) table_grid_kernel(const T
     __syncwarp();
     int s = sRow[0], e = sRow[1];
     int pre = (s + lane < e) ? (int)__ldg(x + s + lane) : -1;
+    bool anyhits = false;
     uint4 kt[NQ], ktn[NQ];
 #pragma unroll
     for (int u = 0; u < NQ; ++u) kt[u] = __ldg(ktab + (size_t)lane * NQ + u);
@@ -327,36 +413,52 @@ __global__ void __launch_bounds__(kTableWarps * 32, 2) table_grid_kernel(const T
         int y = __shfl_up_sync(kFull, incl, d);
         if (lane >= d) incl += y;
       }
-      const int k0 = incl - mine;  // overlap before this lane's first column
-      int k = k0;
-      unsigned hit = 0;
+      int k = incl - mine;  // overlap before this lane's first column
 #pragma unroll
       for (int t = 0; t < C; ++t) {
         k += m.cnt[lane * Cp + t];
         const uint4 v = kt[t / 8];
         const uint32_t w = ((t % 8) / 2 == 0) ? v.x : ((t % 8) / 2 == 1) ? v.y : ((t % 8) / 2 == 2) ? v.z : v.w;
         const int thr = (t & 1) ? (int)(w >> 16) : (int)(w & 0xFFFFu);
-        hit |= (k >= thr) ? (1u << t) : 0u;
+        if (k >= thr && lane * C + t < A.P.n2) {
+          const int pos = atomicAdd(&m.st->nhits, 1);
+          if (pos < A.hitcap) hb[pos] = make_int2((i << 16) | (lane * C + t), k);
+        }
       }
-      if (__any_sync(kFull, hit != 0)) table_row_hits<C>(A, sRow, m, lane, i, k0, hit);
       __syncwarp();
+      if (m.st->nhits > A.hitcap - 32 * C) {
+        // the buffer could overflow on the next row: resolve what it holds
+        table_resolve(A, sRow, m, lane, hb, m.st->nhits);
+        anyhits = true;
+        __syncwarp();
+        if (lane == 0) m.st->nhits = 0;
+        __syncwarp();
+      }
 #pragma unroll
       for (int u = 0; u < NQ; ++u) kt[u] = ktn[u];
       s = sN;
       e = eN;
     }
-    if (m.st->ncand > 0) table_flush(A, sRow, m, lane);
-    if (m.st->B_valid) {
-      table_refine(A, sRow, m, lane);
-      if (lane == 0) A.out[b] = TaskResult{m.st->bp, m.st->bi, m.st->bj, m.st->bk, 0};
+    __syncwarp();
+    const int nh = m.st->nhits;
+    if (nh > 0) table_resolve(A, sRow, m, lane, hb, nh);
+    if ((nh > 0 || anyhits) && m.st->B_valid) {
+      if (isinf(m.st->bp)) {
+        // no FP64 tail evaluated yet for this task: queue its survivors
+        table_defer(A, sRow, m, lane, b);
+      } else {
+        table_refine(A, sRow, m, lane);
+        if (lane == 0) A.out[b] = TaskResult{m.st->bp, m.st->bi, m.st->bj, m.st->bk, 0};
+      }
     } else {
-      // every cell's ln p lies above the guess: hand the task to the
-      // exhaustive screen
+      // no cell reaches the guess: the next level (or the exhaustive
+      // screen) takes the task
       if (lane == 0) A.fallback[atomicAdd(A.nfallback, 1)] = b;
       ++nfall;
     }
     __syncwarp();
   }
+  if (m.st->npend > 0) table_pending_flush(A, sRow, m, lane);
   if (lane == 0 && A.n_refined) {
     atomicAdd(A.n_refined, m.st->n64);
     atomicAdd(A.n_refined + 1, m.st->n32);

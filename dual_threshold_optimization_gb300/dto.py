@@ -14,7 +14,7 @@ import threading
 
 import numpy as np
 
-from .collections import PermutedRankedFeatureList, RankedFeatureList, dense_ids
+from .feature_lists import PermutedRankedFeatureList, RankedFeatureList, dense_ids
 from .engine import Engine
 
 _state = threading.local()

@@ -3,7 +3,7 @@
 read_ranked_feature_list_from_csv  src/read/read_ranked_feature_list_from_csv.rs:50-70
 read_feature_list_from_file        src/read/read_feature_list_from_file.rs:45-53
 """
-from .collections import Feature, FeatureList, RankedFeatureList
+from .feature_lists import Feature, FeatureList, RankedFeatureList
 
 
 class ReadError(ValueError):

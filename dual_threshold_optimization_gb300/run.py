@@ -16,7 +16,7 @@ import os
 
 import numpy as np
 
-from .collections import dense_ids
+from .feature_lists import dense_ids
 from .dto import OptimizationResult, OptimizationResultRecord, default_engine
 
 

@@ -413,7 +413,7 @@ OR_EXPORT double or_empirical(double p_obs, const double* p_perm, int64_t n_perm
 /* ------------------------------------------------------------------------- */
 /* Philox4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11) and the permutation       */
 /* specification used by the GPU's on-device permutations:                     */
-/*   one level of Rao-Sandelius bucketing (1024 buckets, bucket = top 10 bits  */
+/*   one level of Rao-Sandelius bucketing (4096 buckets, bucket = top 12 bits  */
 /*   of one Philox word per element), elements in each bucket kept in index    */
 /*   order, then a Fisher-Yates shuffle of each bucket with Lemire's unbiased  */
 /*   bounded integers.  The result is an exactly uniform permutation.          */
@@ -434,7 +434,7 @@ OR_EXPORT void or_philox4x32_10(const uint32_t* ctr_in, const uint32_t* key_in, 
     out[0] = c0; out[1] = c1; out[2] = c2; out[3] = c3;
 }
 
-#define OR_NBUCKET 1024
+#define OR_NBUCKET 4096
 
 typedef struct {
     uint32_t key[2];
@@ -471,17 +471,16 @@ static uint32_t bounded(or_stream_t* s, uint32_t range) {
 OR_EXPORT void or_shuffle(uint64_t seed, uint32_t pair_id, uint32_t perm_id, uint32_t list_tag, int32_t L, int32_t* sigma) {
     uint32_t key[2] = {(uint32_t)seed, (uint32_t)(seed >> 32)};
     int32_t* bucket = (int32_t*)malloc((size_t)(L > 0 ? L : 1) * 4);
-    int64_t cnt[OR_NBUCKET + 1];
-    memset(cnt, 0, sizeof(cnt));
+    int64_t* cnt = (int64_t*)calloc(OR_NBUCKET + 1, sizeof(int64_t));
+    int64_t* fill = (int64_t*)malloc(OR_NBUCKET * sizeof(int64_t));
     for (int32_t e = 0; e < L; ++e) {
         uint32_t ctr[4] = {(uint32_t)e >> 2, perm_id, pair_id, 0x10000000u | (list_tag << 24)};
         uint32_t w[4];
         or_philox4x32_10(ctr, key, w);
-        bucket[e] = (int32_t)(w[e & 3] >> 22);
+        bucket[e] = (int32_t)(w[e & 3] >> 20);
         cnt[bucket[e] + 1] += 1;
     }
     for (int b = 0; b < OR_NBUCKET; ++b) cnt[b + 1] += cnt[b];
-    int64_t fill[OR_NBUCKET];
     for (int b = 0; b < OR_NBUCKET; ++b) fill[b] = cnt[b];
     for (int32_t e = 0; e < L; ++e) sigma[fill[bucket[e]]++] = e;
     for (int b = 0; b < OR_NBUCKET; ++b) {
@@ -499,6 +498,8 @@ OR_EXPORT void or_shuffle(uint64_t seed, uint32_t pair_id, uint32_t perm_id, uin
         }
     }
     free(bucket);
+    free(cnt);
+    free(fill);
 }
 
 /* ------------------------------------------------------------------------- */

@@ -6,7 +6,7 @@ import os
 import numpy as np
 import pytest
 
-from dual_threshold_optimization_gb300 import collections as col
+from dual_threshold_optimization_gb300 import feature_lists as col
 from dual_threshold_optimization_gb300 import dto, run, stat_operations
 
 pytestmark = pytest.mark.gpu

@@ -5,7 +5,7 @@ import os
 import numpy as np
 import pytest
 
-from dual_threshold_optimization_gb300 import collections as col
+from dual_threshold_optimization_gb300 import feature_lists as col
 from dual_threshold_optimization_gb300 import dto, read, run, stat_operations
 
 GOLDEN = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "reference_golden.json")))

@@ -50,7 +50,7 @@ def _worker(rank, world, port, n_perm, seed, q, fail_rank):
     from datetime import timedelta
     dist.init_process_group("gloo", rank=rank, world_size=world, timeout=timedelta(seconds=20))
     try:
-        from dual_threshold_optimization_gb300 import collections as col, run, stat_operations
+        from dual_threshold_optimization_gb300 import feature_lists as col, run, stat_operations
         p = _pair()
         names = p.feature_names()
         l1 = col.RankedFeatureList.from_(col.FeatureList([names[f] for f in p.feat1]), p.ranks1)
