@@ -322,7 +322,7 @@ def run_gpu(args):
     roofline = {"bound": "fp32", "achieved": achieved_tflops, "peak": fp32_peak, "unit": "TFLOP/s",
                 "frac": (achieved_tflops / fp32_peak) if fp32_peak else None,
                 "traffic": args.traffic,
-                "kernel": "grid_kernel<20> (threshold-pair search)",
+                "kernel": "threshold-pair search: table_grid_kernel<20> ladder + exhaustive grid_kernel<20> fallback",
                 "work_per_task": "8 ops x %d cells" % cells,
                 "peak_source": "measured: cuBLAS SGEMM 8192^3 without TF32 on this GPU (FP32 pipe)",
                 "grid_ms_per_step": statistics.mean(grid_ms),

@@ -61,6 +61,8 @@ def build(force=False, verbose=False, jobs=None):
     for knob in ("DTO_GRID_WARPS", "DTO_PERM_THREADS", "DTO_BUCKET_BITS"):
         if os.environ.get(knob):
             flags += ["-D%s=%d" % (knob, int(os.environ[knob]))]
+    if os.environ.get("DTO_L0_QUANTILE"):
+        flags += ["-DDTO_L0_QUANTILE=%.4f" % float(os.environ["DTO_L0_QUANTILE"])]
     if verbose:
         flags += ["-Xptxas", "-v"]
     srcs = _sources()

@@ -221,6 +221,12 @@ std::vector<uint32_t> thresholds_of(uint32_t max_rank) {
 
 constexpr int kCs[] = {4, 8, 12, 16, 20, 24, 28, 32};
 
+// Quantile of the first batch's minimum p-values that sets the level-0 table.
+#ifndef DTO_L0_QUANTILE
+#define DTO_L0_QUANTILE 0.90
+#endif
+constexpr double kLevel0Quantile = DTO_L0_QUANTILE;
+
 int pick_C(int n2) {
   for (int c : kCs)
     if (32 * c >= n2) return c;
@@ -851,7 +857,7 @@ int dto_run_range(dto_ctx* ctx, dto_pair* P, uint32_t perm_first, int64_t n_perm
     if (use_table && row0 && cnt >= 256) {
       std::vector<double> v(minp.begin() + b0, minp.begin() + b0 + cnt);
       std::sort(v.begin(), v.end());
-      const double p90 = v[(size_t)(0.90 * (double)(v.size() - 1))];
+      const double p90 = v[(size_t)(kLevel0Quantile * (double)(v.size() - 1))];
       const double p99 = v[(size_t)(0.99 * (double)(v.size() - 1))];
       const double pmax = v.back();
       if (p90 > 1e-300) {

@@ -379,31 +379,51 @@ __global__ void __launch_bounds__(kTableWarps * 32, 2) table_grid_kernel(const T
     for (int q = lane; q < 32 * Cp; q += 32) m.cnt[q] = 0;
     m.tot[lane] = 0;
     __syncwarp();
+    // Labels are read as 32-bit words (two labels each); a row's words are
+    // prefetched one row ahead, 64 words (128 labels) per warp.  X rows start
+    // 16-byte aligned and are padded to a multiple of 8 labels.
+    const int* x32 = reinterpret_cast<const int*>(x);
     int s = sRow[0], e = sRow[1];
-    int pre = (s + lane < e) ? (int)__ldg(x + s + lane) : -1;
+    int w0, w1;
+    {
+      const int q0 = (s >> 1) + lane;
+      w0 = (2 * q0 < e) ? __ldg(x32 + q0) : -1;
+      w1 = (2 * (q0 + 32) < e) ? __ldg(x32 + q0 + 32) : -1;
+    }
     bool anyhits = false;
     uint4 kt[NQ], ktn[NQ];
 #pragma unroll
     for (int u = 0; u < NQ; ++u) kt[u] = __ldg(ktab + (size_t)lane * NQ + u);
+    auto add_word = [&](int w, int q, int rs, int re) {
+      const int p = 2 * q;
+      const int lab0 = (int)(short)(w & 0xffff), lab1 = w >> 16;  // sign-extended labels
+      if (p >= rs && p < re && lab0 >= 0) {
+        atomicAdd(&m.cnt[lab0], 1);
+        atomicAdd(&m.tot[lab0 / Cp], 1);
+      }
+      if (p + 1 >= rs && p + 1 < re && lab1 >= 0) {
+        atomicAdd(&m.cnt[lab1], 1);
+        atomicAdd(&m.tot[lab1 / Cp], 1);
+      }
+    };
     for (int i = 0; i < n1; ++i) {
-      const int cur = pre;
+      const int c0 = w0, c1 = w1;
       const int sN = e;
       const int eN = (i + 2 <= n1) ? sRow[i + 2] : e;
-      pre = (sN + lane < eN) ? (int)__ldg(x + sN + lane) : -1;
+      {
+        const int q0 = (sN >> 1) + lane;
+        w0 = (2 * q0 < eN) ? __ldg(x32 + q0) : -1;
+        w1 = (2 * (q0 + 32) < eN) ? __ldg(x32 + q0 + 32) : -1;
+      }
       if (i + 1 < n1) {
 #pragma unroll
         for (int u = 0; u < NQ; ++u) ktn[u] = __ldg(ktab + ((size_t)(i + 1) * 32 + lane) * NQ + u);
       }
-      if (cur >= 0) {
-        atomicAdd(&m.cnt[cur], 1);
-        atomicAdd(&m.tot[cur / Cp], 1);
-      }
-      for (int p = s + 32 + lane; p < e; p += 32) {
-        int v = __ldg(x + p);
-        if (v >= 0) {
-          atomicAdd(&m.cnt[v], 1);
-          atomicAdd(&m.tot[v / Cp], 1);
-        }
+      {
+        const int q0 = (s >> 1) + lane;
+        add_word(c0, q0, s, e);
+        add_word(c1, q0 + 32, s, e);
+        for (int q = q0 + 64; 2 * q < e; q += 32) add_word(__ldg(x32 + q), q, s, e);
       }
       __syncwarp();
       const int mine = m.tot[lane];
@@ -420,7 +440,7 @@ __global__ void __launch_bounds__(kTableWarps * 32, 2) table_grid_kernel(const T
         const uint4 v = kt[t / 8];
         const uint32_t w = ((t % 8) / 2 == 0) ? v.x : ((t % 8) / 2 == 1) ? v.y : ((t % 8) / 2 == 2) ? v.z : v.w;
         const int thr = (t & 1) ? (int)(w >> 16) : (int)(w & 0xFFFFu);
-        if (k >= thr && lane * C + t < A.P.n2) {
+        if (k >= thr) {  // columns past n2 hold 0xFFFF, above any overlap
           const int pos = atomicAdd(&m.st->nhits, 1);
           if (pos < A.hitcap) hb[pos] = make_int2((i << 16) | (lane * C + t), k);
         }
