@@ -21,6 +21,25 @@
 
 using namespace dto;
 
+// Buffers of one in-flight batch of the table-screen pipeline.
+struct BatchSlot {
+  void* dX = nullptr;
+  size_t xBytes = 0;
+  void* dRes = nullptr;
+  size_t resBytes = 0;
+  void* hRes = nullptr;  // pinned
+  size_t hResBytes = 0;
+  void* dFall = nullptr;
+  size_t fallBytes = 0;
+  void* dIdx = nullptr;
+  size_t idxBytes = 0;
+  int* dCnt = nullptr;  // [0, 8): task counters, [8, 12): fallback counts
+  cudaEvent_t ev[8] = {};  // perm start/end, tables start, -, exhaustive start/end, tables done, batch done
+  bool busy = false;
+  long long b0 = 0;
+  int cnt = 0;
+};
+
 struct dto_ctx {
   int device = 0;
   int nsm = 0;
@@ -55,6 +74,7 @@ struct dto_ctx {
   size_t fallBytes = 0;
   void* dHits = nullptr;       // per-warp hit buffers of the table screen
   size_t hitBytes = 0;
+  BatchSlot slot[2];           // double-buffered batches of the table-screen pipeline
   int* dNFall = nullptr;
 };
 
@@ -312,19 +332,17 @@ int ensure_table(dto_ctx* ctx, dto_pair* P, int level, int tau) {
 // Tasks [0, ntask) of X through the table ladder: level l takes the tasks
 // that level l-1 could not settle (their minimum lies above its bound), and
 // the exhaustive screen takes what the last level leaves.  The lists and
-// their counts stay on the device.
-int table_tasks(dto_ctx* ctx, dto_pair* P, const int16_t* X, long long xstride, int ntask, TaskResult* dOut,
-                int nlev) {
+// their counts stay on the device.  `fall` holds nlev lists of cap entries,
+// `cnts` 8 task counters then 4 list counts.  The levels run on the context's
+// stream; the exhaustive screen runs on `xstream` after `evTab` (which may be
+// the same stream).
+int table_levels(dto_ctx* ctx, dto_pair* P, const int16_t* X, long long xstride, int ntask, TaskResult* dOut,
+                 int nlev, int* fall, int* cnts) {
   const int cap = std::max(ntask, 1);
-  int rc = grow(ctx, &ctx->dFall, &ctx->fallBytes, (size_t)nlev * cap * 4);
-  if (rc) return rc;
   const int hitcap = 8192;
-  rc = grow(ctx, &ctx->dHits, &ctx->hitBytes, (size_t)2 * ctx->nsm * kTableWarps * hitcap * 8);
+  int rc = grow(ctx, &ctx->dHits, &ctx->hitBytes, (size_t)2 * ctx->nsm * kTableWarps * hitcap * 8);
   if (rc) return rc;
-  int* fall = (int*)ctx->dFall;
-  CK(cudaMemsetAsync(ctx->dWork, 0, 8 * sizeof(int), ctx->stream));
-  CK(cudaMemsetAsync(ctx->dNFall, 0, 4 * sizeof(int), ctx->stream));
-  CK(cudaEventRecord(ctx->evk[2], ctx->stream));
+  CK(cudaMemsetAsync(cnts, 0, 12 * sizeof(int), ctx->stream));
   for (int level = 0; level < nlev; ++level) {
     TableGridArgs a{};
     a.P = P->dev;
@@ -335,18 +353,26 @@ int table_tasks(dto_ctx* ctx, dto_pair* P, const int16_t* X, long long xstride, 
     a.tau = P->kthr_tau[level];
     a.kthr = P->dKthr[level];
     a.out = dOut;
-    a.work = ctx->dWork + level;
+    a.work = cnts + level;
     a.n_refined = ctx->dRefined;
     a.fallback = fall + (size_t)level * cap;
-    a.nfallback = ctx->dNFall + level;
+    a.nfallback = cnts + 8 + level;
     a.task_list = level == 0 ? nullptr : fall + (size_t)(level - 1) * cap;
-    a.ntask_dev = level == 0 ? nullptr : ctx->dNFall + level - 1;
+    a.ntask_dev = level == 0 ? nullptr : cnts + 8 + level - 1;
     a.hitbuf = (int2*)ctx->dHits;
     a.hitcap = hitcap;
     int ctas = level == 0 ? std::max(1, std::min(2 * ctx->nsm, (ntask + kTableWarps - 1) / kTableWarps))
                           : 2 * ctx->nsm;
     CK(launch_table_grid(a, P->C, ctas, ctx->stream));
   }
+  ctx->acc_launches += nlev;
+  return DTO_OK;
+}
+
+// The exhaustive screen of what the last table level left, on `stream`.
+int table_exhaustive(dto_ctx* ctx, dto_pair* P, const int16_t* X, long long xstride, int ntask, TaskResult* dOut,
+                     int nlev, const int* fall, int* cnts, cudaStream_t stream) {
+  const int cap = std::max(ntask, 1);
   GridArgs g{};
   g.P = P->dev;
   g.P.LF = ctx->dLF;
@@ -356,13 +382,27 @@ int table_tasks(dto_ctx* ctx, dto_pair* P, const int16_t* X, long long xstride, 
   g.mode = kModeScreen;
   g.smemF = grid_smem_bytes(P->C, P->dev.n1, P->npop, 1) <= ctx->smem_optin ? 1 : 0;
   g.out = dOut;
-  g.work = ctx->dWork + nlev;
+  g.work = cnts + nlev;
   g.n_refined = ctx->dRefined;
   g.task_list = fall + (size_t)(nlev - 1) * cap;
-  g.ntask_dev = ctx->dNFall + nlev - 1;
-  CK(launch_grid(g, ctx->nsm, ctx->stream));
+  g.ntask_dev = cnts + 8 + nlev - 1;
+  CK(launch_grid(g, ctx->nsm, stream));
+  ctx->acc_launches += 1;
+  return DTO_OK;
+}
+
+// The first batch's form: everything on the context's stream, with the
+// context's shared buffers.
+int table_tasks(dto_ctx* ctx, dto_pair* P, const int16_t* X, long long xstride, int ntask, TaskResult* dOut,
+                int nlev) {
+  int rc = grow(ctx, &ctx->dFall, &ctx->fallBytes, (size_t)nlev * std::max(ntask, 1) * 4);
+  if (rc) return rc;
+  CK(cudaEventRecord(ctx->evk[2], ctx->stream));
+  rc = table_levels(ctx, P, X, xstride, ntask, dOut, nlev, (int*)ctx->dFall, ctx->dWork + 32);
+  if (rc) return rc;
+  rc = table_exhaustive(ctx, P, X, xstride, ntask, dOut, nlev, (const int*)ctx->dFall, ctx->dWork + 32, ctx->stream);
+  if (rc) return rc;
   CK(cudaEventRecord(ctx->evk[3], ctx->stream));
-  ctx->acc_launches += nlev + 1;
   return DTO_OK;
 }
 
@@ -502,6 +542,7 @@ int dto_ctx_destroy(dto_ctx* ctx) {
   if (!ctx) return DTO_ERR_INVALID;
   cudaSetDevice(ctx->device);
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+  if (ctx->side) cudaStreamSynchronize(ctx->side);
   cudaFree(ctx->dLF);
   cudaFree(ctx->dX);
   cudaFree(ctx->dSig);
@@ -512,6 +553,16 @@ int dto_ctx_destroy(dto_ctx* ctx) {
   cudaFree(ctx->dGuess);
   cudaFree(ctx->dFall);
   cudaFree(ctx->dHits);
+  for (BatchSlot& sl : ctx->slot) {
+    cudaFree(sl.dX);
+    cudaFree(sl.dRes);
+    cudaFreeHost(sl.hRes);
+    cudaFree(sl.dFall);
+    cudaFree(sl.dIdx);
+    cudaFree(sl.dCnt);
+    for (cudaEvent_t e : sl.ev)
+      if (e) cudaEventDestroy(e);
+  }
   cudaFree(ctx->dNFall);
   if (ctx->ev0) cudaEventDestroy(ctx->ev0);
   if (ctx->ev1) cudaEventDestroy(ctx->ev1);
@@ -781,6 +832,7 @@ int dto_run_range(dto_ctx* ctx, dto_pair* P, uint32_t perm_first, int64_t n_perm
   const long long first_batch = 1024;
   const bool use_table = (mode == kModeScreen) && n_perm > 2 * first_batch;
   int nlev = 0;
+  long long pipe_from = -1;
   long long step = use_table ? first_batch : batch;
   for (long long b0 = 0; b0 < std::max<long long>(n_perm, 1); b0 += step, step = batch) {
     const int row0 = (b0 == 0) ? 1 : 0;
@@ -872,8 +924,91 @@ int dto_run_range(dto_ctx* ctx, dto_pair* P, uint32_t perm_first, int64_t n_perm
         rc = ensure_table(ctx, P, 2, t2);
         if (rc) return rc;
         nlev = 3;
+        pipe_from = b0 + cnt;
+        break;
       }
     }
+  }
+  if (pipe_from >= 0 && pipe_from < n_perm) {
+    // Remaining batches, two in flight: while batch b's exhaustive fallback
+    // and result copy run on the side stream, batch b+1's permutations and
+    // table levels run on the main stream.
+    auto harvest = [&](BatchSlot& sl) -> int {
+      CK(cudaEventSynchronize(sl.ev[7]));
+      float ms = 0.f;
+      if (cudaEventElapsedTime(&ms, sl.ev[0], sl.ev[1]) == cudaSuccess) ctx->acc_perm_ms += ms;
+      if (cudaEventElapsedTime(&ms, sl.ev[2], sl.ev[6]) == cudaSuccess) ctx->acc_grid_ms += ms;
+      if (cudaEventElapsedTime(&ms, sl.ev[4], sl.ev[5]) == cudaSuccess) ctx->acc_grid_ms += ms;
+      const TaskResult* hr = (const TaskResult*)sl.hRes;
+      for (int q = 0; q < sl.cnt; ++q) {
+        const TaskResult& r = hr[q];
+        minp[(size_t)(sl.b0 + q)] = r.p;
+        if (out_minp) out_minp[sl.b0 + q] = r.p;
+        if (out_perm) fill_result(P, r, 1, &out_perm[sl.b0 + q]);
+      }
+      ctx->acc_d2h += (long long)sl.cnt * (long long)sizeof(TaskResult);
+      sl.busy = false;
+      return DTO_OK;
+    };
+    // slots left busy by a call that returned early hold nothing of this call
+    CK(cudaStreamSynchronize(ctx->side));
+    for (BatchSlot& sl : ctx->slot) sl.busy = false;
+    long long it = 0;
+    for (long long b0 = pipe_from; b0 < n_perm; b0 += batch, ++it) {
+      BatchSlot& sl = ctx->slot[it & 1];
+      if (sl.busy) {
+        rc = harvest(sl);
+        if (rc) return rc;
+      }
+      const int cnt = (int)std::min(batch, n_perm - b0);
+      if (!sl.ev[0])
+        for (cudaEvent_t& e : sl.ev) CK(cudaEventCreate(&e));
+      if (!sl.dCnt) CK(cudaMalloc(&sl.dCnt, 256));
+      rc = grow(ctx, &sl.dX, &sl.xBytes, (size_t)cnt * xs * 2);
+      if (!rc) rc = grow(ctx, &sl.dRes, &sl.resBytes, (size_t)cnt * sizeof(TaskResult));
+      if (!rc) rc = grow_host(ctx, &sl.hRes, &sl.hResBytes, (size_t)cnt * sizeof(TaskResult));
+      if (!rc) rc = grow(ctx, &sl.dFall, &sl.fallBytes, (size_t)nlev * cnt * 4);
+      if (rc) return rc;
+      const int32_t* dI = nullptr;
+      if (perm_idx) {
+        const size_t bytes = (size_t)cnt * L12 * 4;
+        rc = grow(ctx, &sl.dIdx, &sl.idxBytes, bytes);
+        if (rc) return rc;
+        CK(cudaMemcpyAsync(sl.dIdx, perm_idx + b0 * L12, bytes, cudaMemcpyHostToDevice, ctx->stream));
+        ctx->acc_h2d += (long long)bytes;
+        dI = (const int32_t*)sl.dIdx;
+      }
+      int16_t* X = (int16_t*)sl.dX;
+      TaskResult* dR = (TaskResult*)sl.dRes;
+      CK(cudaEventRecord(sl.ev[0], ctx->stream));
+      rc = make_labels_launch(ctx, P, seed, (uint32_t)(perm_first + b0), cnt, dI, X, xs);
+      if (rc) return rc;
+      CK(cudaEventRecord(sl.ev[1], ctx->stream));
+      CK(cudaEventRecord(sl.ev[2], ctx->stream));
+      rc = table_levels(ctx, P, X, xs, cnt, dR, nlev, (int*)sl.dFall, sl.dCnt);
+      if (rc) return rc;
+      CK(cudaEventRecord(sl.ev[6], ctx->stream));
+      CK(cudaStreamWaitEvent(ctx->side, sl.ev[6], 0));
+      CK(cudaEventRecord(sl.ev[4], ctx->side));
+      rc = table_exhaustive(ctx, P, X, xs, cnt, dR, nlev, (const int*)sl.dFall, sl.dCnt, ctx->side);
+      if (rc) return rc;
+      CK(cudaEventRecord(sl.ev[5], ctx->side));
+      CK(cudaMemcpyAsync(sl.hRes, dR, (size_t)cnt * sizeof(TaskResult), cudaMemcpyDeviceToHost, ctx->side));
+      CK(cudaEventRecord(sl.ev[7], ctx->side));
+      sl.busy = true;
+      sl.b0 = b0;
+      sl.cnt = cnt;
+    }
+    for (long long k = it; k < it + 2; ++k) {
+      BatchSlot& sl = ctx->slot[k & 1];
+      if (sl.busy) {
+        rc = harvest(sl);
+        if (rc) return rc;
+      }
+    }
+    // the main stream's timing event follows the side stream's last work
+    CK(cudaEventRecord(ctx->evSide, ctx->side));
+    CK(cudaStreamWaitEvent(ctx->stream, ctx->evSide, 0));
   }
   fill_result(P, unperm, 0, out_unpermuted);
   const double p_obs = unperm.p;

@@ -181,3 +181,27 @@ def test_table_screen_equals_fp64_many_permutations(engine):
     assert a.unpermuted == b.unpermuted
     assert np.array_equal(a.records, b.records)
     assert a.summary["n_fallback"] > 0  # the 90th-percentile guess leaves ~10% to the exhaustive screen
+
+
+@pytest.mark.parametrize("kind", ["same_set", "general"])
+def test_pipelined_batches_equal_short_runs(engine, kind):
+    # a run long enough for three label batches after the first one (two
+    # batches in flight, one slot reused) must give every permutation the
+    # optimum that short runs of the same permutation ids give
+    if kind == "same_set":
+        p = synth.copula_pair(20000, 0.2, seed=57)
+        P = 60000  # 1,024 + 26,843 + 26,843 + 5,290 at 40,000 label bytes a permutation
+    else:
+        p = synth.small_pair(20000, 0.2, seed=58, subset1=19000, subset2=19500)
+        P = 15000  # 1,024 + 6,972 + 6,972 + 32 at 1 GiB of two-list index scratch
+    dp = engine.pair(p.ranks1, p.feat1, p.ranks2, p.feat2, p.n_features, p.population)
+    long_run = dp.run(P, seed=99, precision="screen", want_records=True)
+    step = 2000  # at most 2,048: the exhaustive screen alone
+    for first in range(1, P + 1, step):
+        n = min(step, P + 1 - first)
+        short = dp.run(n, seed=99, first=first, precision="screen", want_records=True)
+        assert short.unpermuted == long_run.unpermuted
+        assert np.array_equal(short.records, long_run.records[first - 1:first - 1 + n]), first
+    s = long_run.summary
+    assert s["empirical_pvalue"] == np.mean(long_run.minp <= long_run.unpermuted["pvalue"])
+    dp.close()
