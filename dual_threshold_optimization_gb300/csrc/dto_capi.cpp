@@ -70,10 +70,8 @@ struct dto_ctx {
   int* dWork = nullptr;
   unsigned long long* dRefined = nullptr;
   unsigned* dGuess = nullptr;  // bound histogram shared by the batches of one run
-  void* dFall = nullptr;       // fallback task lists of the two table levels
-  size_t fallBytes = 0;
-  void* dHits = nullptr;       // per-warp hit buffers of the table screen
-  size_t hitBytes = 0;
+  void* dHits[2] = {nullptr, nullptr};  // per-warp hit buffers of the table screen, one per stream
+  size_t hitBytes[2] = {0, 0};
   BatchSlot slot[2];           // double-buffered batches of the table-screen pipeline
   int* dNFall = nullptr;
 };
@@ -321,6 +319,7 @@ int ensure_table(dto_ctx* ctx, dto_pair* P, int level, int tau) {
   t.F = P->dF;
   t.fshift = P->fshift;
   t.tau = tau;
+  t.packed = P->ncommon <= kPackedMaxCommon ? 1 : 0;
   t.kthr = P->dKthr[level];
   CK(launch_table_build(t, ctx->nsm, ctx->stream));
   ctx->acc_launches += 1;
@@ -337,13 +336,13 @@ int ensure_table(dto_ctx* ctx, dto_pair* P, int level, int tau) {
 // stream; the exhaustive screen runs on `xstream` after `evTab` (which may be
 // the same stream).
 int table_levels(dto_ctx* ctx, dto_pair* P, const int16_t* X, long long xstride, int ntask, TaskResult* dOut,
-                 int nlev, int* fall, int* cnts) {
+                 int lev_begin, int lev_end, int* fall, int* cnts, cudaStream_t stream, int hb) {
   const int cap = std::max(ntask, 1);
   const int hitcap = 8192;
-  int rc = grow(ctx, &ctx->dHits, &ctx->hitBytes, (size_t)2 * ctx->nsm * kTableWarps * hitcap * 8);
+  int rc = grow(ctx, &ctx->dHits[hb], &ctx->hitBytes[hb], (size_t)kTableCtasPerSm * ctx->nsm * kTableWarps * hitcap * 8);
   if (rc) return rc;
-  CK(cudaMemsetAsync(cnts, 0, 12 * sizeof(int), ctx->stream));
-  for (int level = 0; level < nlev; ++level) {
+  if (lev_begin == 0) CK(cudaMemsetAsync(cnts, 0, 12 * sizeof(int), stream));
+  for (int level = lev_begin; level < lev_end; ++level) {
     TableGridArgs a{};
     a.P = P->dev;
     a.P.LF = ctx->dLF;
@@ -352,6 +351,7 @@ int table_levels(dto_ctx* ctx, dto_pair* P, const int16_t* X, long long xstride,
     a.ntask = ntask;
     a.tau = P->kthr_tau[level];
     a.kthr = P->dKthr[level];
+    a.packed = P->ncommon <= kPackedMaxCommon ? 1 : 0;
     a.out = dOut;
     a.work = cnts + level;
     a.n_refined = ctx->dRefined;
@@ -359,13 +359,16 @@ int table_levels(dto_ctx* ctx, dto_pair* P, const int16_t* X, long long xstride,
     a.nfallback = cnts + 8 + level;
     a.task_list = level == 0 ? nullptr : fall + (size_t)(level - 1) * cap;
     a.ntask_dev = level == 0 ? nullptr : cnts + 8 + level - 1;
-    a.hitbuf = (int2*)ctx->dHits;
+    a.hitbuf = (int2*)ctx->dHits[hb];
     a.hitcap = hitcap;
-    int ctas = level == 0 ? std::max(1, std::min(2 * ctx->nsm, (ntask + kTableWarps - 1) / kTableWarps))
-                          : 2 * ctx->nsm;
-    CK(launch_table_grid(a, P->C, ctas, ctx->stream));
+    // a later level sees the tasks the earlier ones left (about 10 % and 1 %
+    // of the batch); one warp per expected task keeps its latency to one sweep
+    const double expect = level == 0 ? 1.0 : level == 1 ? 0.15 : 0.03;
+    const int want = (int)(expect * (double)ntask / kTableWarps) + 1;
+    const int ctas = std::max(1, std::min(kTableCtasPerSm * ctx->nsm, want));
+    CK(launch_table_grid(a, P->C, ctas, stream));
   }
-  ctx->acc_launches += nlev;
+  ctx->acc_launches += lev_end - lev_begin;
   return DTO_OK;
 }
 
@@ -388,21 +391,6 @@ int table_exhaustive(dto_ctx* ctx, dto_pair* P, const int16_t* X, long long xstr
   g.ntask_dev = cnts + 8 + nlev - 1;
   CK(launch_grid(g, ctx->nsm, stream));
   ctx->acc_launches += 1;
-  return DTO_OK;
-}
-
-// The first batch's form: everything on the context's stream, with the
-// context's shared buffers.
-int table_tasks(dto_ctx* ctx, dto_pair* P, const int16_t* X, long long xstride, int ntask, TaskResult* dOut,
-                int nlev) {
-  int rc = grow(ctx, &ctx->dFall, &ctx->fallBytes, (size_t)nlev * std::max(ntask, 1) * 4);
-  if (rc) return rc;
-  CK(cudaEventRecord(ctx->evk[2], ctx->stream));
-  rc = table_levels(ctx, P, X, xstride, ntask, dOut, nlev, (int*)ctx->dFall, ctx->dWork + 32);
-  if (rc) return rc;
-  rc = table_exhaustive(ctx, P, X, xstride, ntask, dOut, nlev, (const int*)ctx->dFall, ctx->dWork + 32, ctx->stream);
-  if (rc) return rc;
-  CK(cudaEventRecord(ctx->evk[3], ctx->stream));
   return DTO_OK;
 }
 
@@ -551,8 +539,8 @@ int dto_ctx_destroy(dto_ctx* ctx) {
   cudaFree(ctx->dWork);
   cudaFree(ctx->dRefined);
   cudaFree(ctx->dGuess);
-  cudaFree(ctx->dFall);
-  cudaFree(ctx->dHits);
+  cudaFree(ctx->dHits[0]);
+  cudaFree(ctx->dHits[1]);
   for (BatchSlot& sl : ctx->slot) {
     cudaFree(sl.dX);
     cudaFree(sl.dRes);
@@ -823,12 +811,10 @@ int dto_run_range(dto_ctx* ctx, dto_pair* P, uint32_t perm_first, int64_t n_perm
   // concurrently with the first permutations.
   std::vector<double> minp((size_t)n_perm);
   TaskResult unperm{};
-  // Without the table screen, the unpermuted task (task 0) rides in row 0 of
-  // the first batch of the exhaustive screen.  With it, the first batch of
-  // first_batch permutations goes through tables built for fixed bounds
-  // (ln 0.05, ln 0.5) while task 0 runs through the exhaustive screen on the
-  // side stream; the first batch's 90th and 99th percentiles and maximum then
-  // set the three-level table ladder for the remaining batches.
+  // The unpermuted task (task 0) rides in row 0 of the first batch, through
+  // the exhaustive screen.  With the table screen, the first batch holds
+  // first_batch permutations; its 90th and 99th percentiles and maximum of
+  // the minimum p set the three-level table ladder of the remaining batches.
   const long long first_batch = 1024;
   const bool use_table = (mode == kModeScreen) && n_perm > 2 * first_batch;
   int nlev = 0;
@@ -857,40 +843,8 @@ int dto_run_range(dto_ctx* ctx, dto_pair* P, uint32_t perm_first, int64_t n_perm
     if (row0) CK(cudaMemcpyAsync(ctx->dX, P->dYlab, (size_t)P->N1 * 2, cudaMemcpyDeviceToDevice, ctx->stream));
     const int ntask = cnt + row0;
     const int16_t* X = (const int16_t*)ctx->dX;
-    if (use_table) {
-      if (row0) {
-        // task 0 on the side stream, after its labels are in place
-        CK(cudaEventRecord(ctx->evSide, ctx->stream));
-        CK(cudaStreamWaitEvent(ctx->side, ctx->evSide, 0));
-        GridArgs g{};
-        g.P = P->dev;
-        g.P.LF = ctx->dLF;
-        g.X = X;
-        g.xstride = xs;
-        g.ntask = 1;
-        g.mode = kModeScreen;
-        g.smemF = grid_smem_bytes(P->C, P->dev.n1, P->npop, 1) <= ctx->smem_optin ? 1 : 0;
-        g.out = dRes;
-        g.work = ctx->dWork + 16;
-        g.n_refined = ctx->dRefined;
-        CK(cudaMemsetAsync(ctx->dWork + 16, 0, sizeof(int), ctx->side));
-        CK(launch_grid(g, 1, ctx->side));
-        ctx->acc_launches += 1;
-        CK(cudaEventRecord(ctx->evSide, ctx->side));
-        const int sc = P->fshift;
-        rc = ensure_table(ctx, P, 0, fixed_log(0.05, sc));
-        if (rc) return rc;
-        rc = ensure_table(ctx, P, 1, fixed_log(0.5, sc));
-        if (rc) return rc;
-        nlev = 2;
-      }
-      rc = table_tasks(ctx, P, X + (size_t)row0 * xs, xs, cnt, dRes + row0, nlev);
-      if (rc) return rc;
-      if (row0) CK(cudaStreamWaitEvent(ctx->stream, ctx->evSide, 0));
-    } else {
-      rc = grid_tasks(ctx, P, X, xs, ntask, mode, dRes, nullptr, nullptr, true);
-      if (rc) return rc;
-    }
+    rc = grid_tasks(ctx, P, X, xs, ntask, mode, dRes, nullptr, nullptr, true);
+    if (rc) return rc;
     CK(cudaMemcpyAsync(hRes, dRes, (size_t)ntask * sizeof(TaskResult), cudaMemcpyDeviceToHost, ctx->stream));
     ctx->acc_d2h += (long long)ntask * (long long)sizeof(TaskResult);
     CK(cudaStreamSynchronize(ctx->stream));
@@ -930,9 +884,9 @@ int dto_run_range(dto_ctx* ctx, dto_pair* P, uint32_t perm_first, int64_t n_perm
     }
   }
   if (pipe_from >= 0 && pipe_from < n_perm) {
-    // Remaining batches, two in flight: while batch b's exhaustive fallback
-    // and result copy run on the side stream, batch b+1's permutations and
-    // table levels run on the main stream.
+    // Remaining batches, two in flight: while batch b's later table levels,
+    // exhaustive fallback and result copy run on the side stream, batch
+    // b+1's permutations and level-0 table sweep run on the main stream.
     auto harvest = [&](BatchSlot& sl) -> int {
       CK(cudaEventSynchronize(sl.ev[7]));
       float ms = 0.f;
@@ -985,11 +939,13 @@ int dto_run_range(dto_ctx* ctx, dto_pair* P, uint32_t perm_first, int64_t n_perm
       if (rc) return rc;
       CK(cudaEventRecord(sl.ev[1], ctx->stream));
       CK(cudaEventRecord(sl.ev[2], ctx->stream));
-      rc = table_levels(ctx, P, X, xs, cnt, dR, nlev, (int*)sl.dFall, sl.dCnt);
+      rc = table_levels(ctx, P, X, xs, cnt, dR, 0, 1, (int*)sl.dFall, sl.dCnt, ctx->stream, 0);
       if (rc) return rc;
       CK(cudaEventRecord(sl.ev[6], ctx->stream));
       CK(cudaStreamWaitEvent(ctx->side, sl.ev[6], 0));
       CK(cudaEventRecord(sl.ev[4], ctx->side));
+      rc = table_levels(ctx, P, X, xs, cnt, dR, 1, nlev, (int*)sl.dFall, sl.dCnt, ctx->side, 1);
+      if (rc) return rc;
       rc = table_exhaustive(ctx, P, X, xs, cnt, dR, nlev, (const int*)sl.dFall, sl.dCnt, ctx->side);
       if (rc) return rc;
       CK(cudaEventRecord(sl.ev[5], ctx->side));

@@ -102,7 +102,27 @@ struct ComposeArgs {
 };
 
 // Table screen (dto_table.cuh).
-constexpr int kTableWarps = 16;  // warps per CTA of the table-screen kernel (2 CTAs per SM)
+// Warps per CTA of the table-screen kernel and the CTAs per SM its register
+// budget is compiled for.  One CTA of 16 warps per SM gives each thread 128
+// registers, which keeps the row sweep free of register spills; at 2 CTAs
+// (64 registers) spilled state reloads from L2 inside the sweep and the
+// kernel runs about 25 % slower.
+#ifndef DTO_TABLE_WARPS
+#define DTO_TABLE_WARPS 16
+#endif
+#ifndef DTO_TABLE_MINB
+#define DTO_TABLE_MINB 1
+#endif
+constexpr int kTableWarps = DTO_TABLE_WARPS;
+constexpr int kTableCtasPerSm = DTO_TABLE_MINB;
+
+// The packed table sweep holds overlaps in 16-bit halves and tests
+// k >= kthr as the sign bit of k + (0x8000 - kthr): it needs every overlap,
+// hence the number of features the two lists share, to be <= 0x7FFF.
+#ifndef DTO_TABLE_PACKED
+#define DTO_TABLE_PACKED 1
+#endif
+constexpr long long kPackedMaxCommon = DTO_TABLE_PACKED ? 0x7FFF : -1;
 
 struct TableArgs {
   int n1, n2, N, C;
@@ -111,7 +131,8 @@ struct TableArgs {
   const uint32_t* F;
   int fshift;
   int tau;               // fixed-point ln p guess
-  uint16_t* kthr;        // [n1][32][table_cq(C)]
+  int packed;            // entry form of the packed (16-bit overlap) sweep
+  uint16_t* kthr;        // [n1][table_cq(C) / 8][32][8]
 };
 
 struct TableGridArgs {
@@ -120,7 +141,8 @@ struct TableGridArgs {
   long long xstride;
   int ntask;
   int tau;                // the guess the table was built for
-  const uint16_t* kthr;   // [n1][32][table_cq(C)]
+  const uint16_t* kthr;   // [n1][table_cq(C) / 8][32][8]
+  int packed;             // 16-bit overlap sweep (every overlap <= 0x7FFF)
   TaskResult* out;
   int* work;
   unsigned long long* n_refined;  // [3]

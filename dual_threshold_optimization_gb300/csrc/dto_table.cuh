@@ -26,7 +26,16 @@ constexpr double kTableMargin = 0.002;  // nats added to tau when the table is b
 
 __host__ __device__ constexpr int table_cq(int C) { return (C + 7) & ~7; }
 
-// One thread per cell: binary search for the first overlap that passes.
+// Lane stride, in 32-bit words, of the packed counters: C/2 words of two
+// 16-bit column counts each, padded to whole 16-byte chunks, an odd number of
+// chunks so that a quarter-warp's 128-bit loads hit distinct banks.
+__host__ __device__ constexpr int table_wp(int C) { return 4 * ((table_cq(C) / 8) | 1); }
+
+// One thread per entry: binary search for the first overlap that passes.
+// Layout [i][q][lane][8]: entry t of a lane's row is in its q = t / 8-th
+// 16-byte chunk, so a warp's load of chunk q reads 512 contiguous bytes.
+// Plain entries hold kthr (0xFFFF: never); packed entries hold
+// 0x8000 - min(kthr, 0x8000) (0: never).
 static __global__ void table_build_kernel(const TableArgs A) {
   const int Cq = table_cq(A.C);
   const long long cells = (long long)A.n1 * 32 * Cq;
@@ -37,16 +46,17 @@ static __global__ void table_build_kernel(const TableArgs A) {
        c += (long long)gridDim.x * blockDim.x) {
     const int i = (int)(c / (32 * Cq));
     const int rem = (int)(c % (32 * Cq));
-    const int lane = rem / Cq, t = rem % Cq;
+    const int q = rem / 256, lane = (rem / 8) % 32;
+    const int t = 8 * q + rem % 8;
     const int j = lane * A.C + t;
-    uint16_t out = 0xFFFF;
+    int thr = 0x10000;  // never
     if (t < A.C && j < A.n2) {
       const int K = __ldg(A.rowstart + i + 1);
       const int n = __ldg(A.ncnt + j);
       const int a = min(K, n), b = max(K, n);
       const long long mode = ((long long)(a + 1) * (long long)(b + 1)) / (long long)(A.N + 2);
       if (lbt_fix(A.F, A.N, FN, K, n, (int)mode, mode, scale) <= tauT) {
-        out = 0;
+        thr = 0;
       } else {
         // invariant: pred(lo) false, pred(hi) true or hi = a + 1
         int lo = (int)mode, hi = a + 1;
@@ -55,10 +65,10 @@ static __global__ void table_build_kernel(const TableArgs A) {
           if (lbt_fix(A.F, A.N, FN, K, n, mid, mode, scale) <= tauT) hi = mid;
           else lo = mid;
         }
-        out = (uint16_t)min(hi, 0xFFFF);
+        thr = hi;
       }
     }
-    A.kthr[c] = out;
+    A.kthr[c] = A.packed ? (uint16_t)(0x8000 - min(thr, 0x8000)) : (uint16_t)min(thr, 0xFFFF);
   }
 }
 
@@ -333,11 +343,15 @@ static __device__ __noinline__ void table_resolve(const TableGridArgs& A, const 
   if (m.st->ncand > 0) table_flush(A, sRow, m, lane);
 }
 
-template <int C>
-__global__ void __launch_bounds__(kTableWarps * 32, 2) table_grid_kernel(const TableGridArgs A) {
+template <int C, bool Packed>
+__global__ void __launch_bounds__(kTableWarps * 32, kTableCtasPerSm) table_grid_kernel(const TableGridArgs A) {
   constexpr int Cp = C | 1;
   constexpr int Cq = table_cq(C);
-  constexpr int NQ = Cq / 8;  // uint4 loads per lane per row
+  constexpr int NQ = Cq / 8;  // 16-byte table chunks per lane per row
+  constexpr int NW = C / 2;   // packed counter words per lane
+  constexpr int Wp = table_wp(C);
+  static_assert(C % 2 == 0, "packed columns come in pairs");
+  static_assert(32 * Wp <= grid_cnt_ints(C), "packed counters fit the counter area");
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int n1 = A.P.n1;
@@ -345,6 +359,7 @@ __global__ void __launch_bounds__(kTableWarps * 32, 2) table_grid_kernel(const T
   int* sRow = reinterpret_cast<int*>(smem_raw);
   int* sWarp = sRow + ((n1 + 1 + 3) & ~3);
   const TableWarpMem m = table_warp_mem(sWarp + warp * table_warp_ints(C), C);
+  uint32_t* cw = reinterpret_cast<uint32_t*>(m.cnt);  // packed counters (16-byte aligned)
   for (int q = threadIdx.x; q <= n1; q += blockDim.x) sRow[q] = __ldg(A.P.rowstart + q);
   if (lane == 0) {
     m.st->n32 = 0;
@@ -393,18 +408,27 @@ __global__ void __launch_bounds__(kTableWarps * 32, 2) table_grid_kernel(const T
     bool anyhits = false;
     uint4 kt[NQ], ktn[NQ];
 #pragma unroll
-    for (int u = 0; u < NQ; ++u) kt[u] = __ldg(ktab + (size_t)lane * NQ + u);
+    for (int u = 0; u < NQ; ++u) kt[u] = __ldg(ktab + (size_t)u * 32 + lane);
+    // a label is the counter slot lane * Cp + t of its column lane * C + t
+    auto add_lab = [&](int lab) {
+      const int l = lab / Cp;
+      if (Packed) {
+        const int t = lab - l * Cp;
+        atomicAdd(&cw[l * Wp + (t >> 1)], 1u << ((t & 1) << 4));
+      } else {
+        atomicAdd(&m.cnt[lab], 1);
+      }
+      atomicAdd(&m.tot[l], 1);
+    };
     auto add_word = [&](int w, int q, int rs, int re) {
       const int p = 2 * q;
       const int lab0 = (int)(short)(w & 0xffff), lab1 = w >> 16;  // sign-extended labels
-      if (p >= rs && p < re && lab0 >= 0) {
-        atomicAdd(&m.cnt[lab0], 1);
-        atomicAdd(&m.tot[lab0 / Cp], 1);
-      }
-      if (p + 1 >= rs && p + 1 < re && lab1 >= 0) {
-        atomicAdd(&m.cnt[lab1], 1);
-        atomicAdd(&m.tot[lab1 / Cp], 1);
-      }
+      if (p >= rs && p < re && lab0 >= 0) add_lab(lab0);
+      if (p + 1 >= rs && p + 1 < re && lab1 >= 0) add_lab(lab1);
+    };
+    auto push_hit = [&](int i, int t, int k) {
+      const int pos = atomicAdd(&m.st->nhits, 1);
+      if (pos < A.hitcap) hb[pos] = make_int2((i << 16) | (lane * C + t), k);
     };
     for (int i = 0; i < n1; ++i) {
       const int c0 = w0, c1 = w1;
@@ -417,7 +441,7 @@ __global__ void __launch_bounds__(kTableWarps * 32, 2) table_grid_kernel(const T
       }
       if (i + 1 < n1) {
 #pragma unroll
-        for (int u = 0; u < NQ; ++u) ktn[u] = __ldg(ktab + ((size_t)(i + 1) * 32 + lane) * NQ + u);
+        for (int u = 0; u < NQ; ++u) ktn[u] = __ldg(ktab + ((size_t)(i + 1) * NQ + u) * 32 + lane);
       }
       {
         const int q0 = (s >> 1) + lane;
@@ -433,16 +457,51 @@ __global__ void __launch_bounds__(kTableWarps * 32, 2) table_grid_kernel(const T
         int y = __shfl_up_sync(kFull, incl, d);
         if (lane >= d) incl += y;
       }
-      int k = incl - mine;  // overlap before this lane's first column
+      if (Packed) {
+        // y[w] = (overlap of column 2w+1) << 16 | (overlap of column 2w);
+        // R carries the running overlap in both halves
+        uint32_t R = (uint32_t)(incl - mine) * 0x10001u;
+        uint32_t y[NW];
+        uint32_t acc = 0;
 #pragma unroll
-      for (int t = 0; t < C; ++t) {
-        k += m.cnt[lane * Cp + t];
-        const uint4 v = kt[t / 8];
-        const uint32_t w = ((t % 8) / 2 == 0) ? v.x : ((t % 8) / 2 == 1) ? v.y : ((t % 8) / 2 == 2) ? v.z : v.w;
-        const int thr = (t & 1) ? (int)(w >> 16) : (int)(w & 0xFFFFu);
-        if (k >= thr) {  // columns past n2 hold 0xFFFF, above any overlap
-          const int pos = atomicAdd(&m.st->nhits, 1);
-          if (pos < A.hitcap) hb[pos] = make_int2((i << 16) | (lane * C + t), k);
+        for (int u = 0; u < NQ; ++u) {
+          const uint4 c4 = *reinterpret_cast<const uint4*>(cw + lane * Wp + 4 * u);
+          const uint32_t cv[4] = {c4.x, c4.y, c4.z, c4.w};
+          const uint32_t tv[4] = {kt[u].x, kt[u].y, kt[u].z, kt[u].w};
+#pragma unroll
+          for (int c = 0; c < 4; ++c) {
+            if (4 * u + c < NW) {
+              const uint32_t v = cv[c] * 0x10001u + R;
+              y[4 * u + c] = v;
+              R = __byte_perm(v, 0, 0x3232);
+              acc |= v + tv[c];
+            }
+          }
+        }
+        if (acc & 0x80008000u) {
+#pragma unroll
+          for (int u = 0; u < NQ; ++u) {
+            const uint32_t tv[4] = {kt[u].x, kt[u].y, kt[u].z, kt[u].w};
+#pragma unroll
+            for (int c = 0; c < 4; ++c) {
+              if (4 * u + c < NW) {
+                const int w = 4 * u + c;
+                const uint32_t d = y[w] + tv[c];
+                if (d & 0x8000u) push_hit(i, 2 * w, (int)(y[w] & 0xFFFFu));
+                if (d & 0x80000000u) push_hit(i, 2 * w + 1, (int)(y[w] >> 16));
+              }
+            }
+          }
+        }
+      } else {
+        int k = incl - mine;  // overlap before this lane's first column
+#pragma unroll
+        for (int t = 0; t < C; ++t) {
+          k += m.cnt[lane * Cp + t];
+          const uint4 v = kt[t / 8];
+          const uint32_t w = ((t % 8) / 2 == 0) ? v.x : ((t % 8) / 2 == 1) ? v.y : ((t % 8) / 2 == 2) ? v.z : v.w;
+          const int thr = (t & 1) ? (int)(w >> 16) : (int)(w & 0xFFFFu);
+          if (k >= thr) push_hit(i, t, k);  // columns past n2 hold 0xFFFF, above any overlap
         }
       }
       __syncwarp();
@@ -486,12 +545,19 @@ __global__ void __launch_bounds__(kTableWarps * 32, 2) table_grid_kernel(const T
   }
 }
 
+template <int C, bool Packed>
+cudaError_t launch_table_grid_kernel(const TableGridArgs& a, int ctas, size_t smem, cudaStream_t s) {
+  cudaError_t e =
+      cudaFuncSetAttribute(table_grid_kernel<C, Packed>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  table_grid_kernel<C, Packed><<<ctas, kTableWarps * 32, smem, s>>>(a);
+  return cudaGetLastError();
+}
+
 template <int C>
 cudaError_t launch_table_grid_impl(const TableGridArgs& a, int ctas, size_t smem, cudaStream_t s) {
-  cudaError_t e = cudaFuncSetAttribute(table_grid_kernel<C>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  if (e != cudaSuccess) return e;
-  table_grid_kernel<C><<<ctas, kTableWarps * 32, smem, s>>>(a);
-  return cudaGetLastError();
+  return a.packed ? launch_table_grid_kernel<C, true>(a, ctas, smem, s)
+                  : launch_table_grid_kernel<C, false>(a, ctas, smem, s);
 }
 
 }  // namespace dto

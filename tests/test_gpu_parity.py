@@ -205,3 +205,19 @@ def test_pipelined_batches_equal_short_runs(engine, kind):
     s = long_run.summary
     assert s["empirical_pvalue"] == np.mean(long_run.minp <= long_run.unpermuted["pvalue"])
     dp.close()
+
+
+def test_table_sweep_beyond_16_bit_overlaps(engine):
+    # 40,000 shared features: overlaps exceed 0x7FFF, so the table screen takes
+    # its 32-bit sweep; its optima must equal the exhaustive screen's (runs of
+    # at most 2,048 permutations take the exhaustive screen alone)
+    p = synth.copula_pair(40000, 0.1, seed=59)
+    dp = engine.pair(p.ranks1, p.feat1, p.ranks2, p.feat2, p.n_features, p.population)
+    P = 3000
+    long_run = dp.run(P, seed=7, precision="screen", want_records=True)
+    assert long_run.summary["n_launches"] > 0
+    for first, n in ((1, 1500), (1501, 1500)):
+        short = dp.run(n, seed=7, first=first, precision="screen", want_records=True)
+        assert short.unpermuted == long_run.unpermuted
+        assert np.array_equal(short.records, long_run.records[first - 1:first - 1 + n])
+    dp.close()
