@@ -21,6 +21,9 @@ constexpr int kBucketBits = DTO_BUCKET_BITS;
 constexpr int kBuckets = 1 << kBucketBits;  // Rao-Sandelius buckets
 static_assert(kBuckets % kPermThreads == 0 && kPermThreads % 32 == 0 && kPermThreads <= 1024,
               "perm_kernel: buckets must split evenly over its warps");
+// Longest list whose Philox words the permutation kernel keeps in shared
+// memory (4 + 2 bytes an element + the counters: 208 KB at 32,768).
+constexpr int kPermWordsMaxL = 32768;
 constexpr int kMaxListLen = 65534;   // positions are uint16; overlaps stay below the 0xFFFF "never" mark
 constexpr int kScreenSlack = 5;      // fixed-point units added to the screen threshold
 constexpr int kSurvCap = 256;        // per-warp survivors of the FP32 stage

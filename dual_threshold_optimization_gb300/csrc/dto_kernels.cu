@@ -5,15 +5,19 @@
 // (src/collections/permuted.rs:56-60: a uniform shuffle of 0..len with
 // rand's thread_rng).  Here a permutation is a deterministic function of
 // (seed, pair id, permutation id, list tag):
-//   1. every element e draws a bucket in [0, 4096) from the top 12 bits of one
-//      Philox4x32-10 word (counter (e/4, perm, pair, 0x10000000 | tag<<24),
-//      word e%4, key = the two halves of the seed);
+//   1. every element e draws one Philox4x32-10 word W[e] (counter
+//      (e/4, perm, pair, 0x10000000 | tag<<24), word e%4, key = the two
+//      halves of the seed); its top 12 bits pick a bucket in [0, 4096);
 //   2. elements are grouped by bucket, in increasing element order inside a
 //      bucket;
-//   3. each bucket b is shuffled by Fisher-Yates, drawing j uniform in [0, i]
-//      with Lemire's multiply-shift method and rejection (exactly unbiased)
-//      from the Philox stream counter (call, perm, pair,
-//      0x20000000 | tag<<24 | b).
+//   3. each bucket is shuffled by the forward Fisher-Yates pass (i = 1..sz-1:
+//      swap positions i and j, j uniform in [0, i]).  Draw i uses the low 20
+//      bits r of W of the element at position i (untouched before step i, so
+//      r is independent of everything drawn before): j = (r (i+1)) >> 20,
+//      unless the low 20 bits of r (i+1) fall below 2^20 mod (i+1), in which
+//      case j comes from the bucket's own Philox stream (counter (call, perm,
+//      pair, 0x20000000 | tag<<24 | bucket)) by Lemire's multiply-shift with
+//      rejection.  Both are exactly uniform.
 // One level of Rao-Sandelius bucketing followed by uniform shuffles of the
 // buckets gives an exactly uniform permutation.
 #include <algorithm>
@@ -62,14 +66,15 @@ __device__ __forceinline__ uint32_t bucket_of(uint4 w, int q) {
 }
 
 // One CTA per permutation.  Shared memory: the bucket counters (int32,
-// kBuckets; after the scatter they hold each bucket's end) and the shuffled
-// element indices (uint16, L).  kBuckets = 4096 keeps buckets at a few
-// elements for the list lengths of interest, so the per-bucket canonical sort
-// and Fisher-Yates are a few operations per element.
-__global__ void __launch_bounds__(kPermThreads) perm_kernel(const PermArgs A) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  int* cnt = reinterpret_cast<int*>(smem_raw);
-  uint16_t* sA = reinterpret_cast<uint16_t*>(cnt + kBuckets);
+// kBuckets; after the scatter they hold each bucket's end), the shuffled
+// element indices (uint16, L) and, for L <= kPermWordsMaxL, every element's
+// Philox word (uint32, L), so that the scatter and the shuffle draws reuse
+// the words of the counting pass; longer lists recompute a word where it is
+// needed.  kBuckets = 4096 keeps buckets at a few elements for the list
+// lengths of interest, so the per-bucket canonical sort and Fisher-Yates are
+// a few operations per element.
+template <bool kWords>
+__device__ __forceinline__ void perm_body(const PermArgs& A, int* cnt, uint16_t* sA, uint32_t* sW) {
   __shared__ int warpTot[kPermThreads / 32];
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int L = A.L;
@@ -77,15 +82,28 @@ __global__ void __launch_bounds__(kPermThreads) perm_kernel(const PermArgs A) {
   const uint32_t k0 = (uint32_t)A.seed, k1 = (uint32_t)(A.seed >> 32);
   const uint32_t tagB = 0x10000000u | (A.list_tag << 24);
   constexpr int kPerWarp = kBuckets / (kPermThreads / 32);
+  constexpr int kLowBits = 32 - kBucketBits;
+  constexpr uint32_t kLowMask = (1u << kLowBits) - 1u;
+  auto word_of = [&](int e) -> uint32_t {
+    if (kWords) return sW[e];
+    const uint4 w = philox4x32_10(make_uint4((uint32_t)(e >> 2), perm, A.pair_id, tagB), k0, k1);
+    const int q = e & 3;
+    return (q == 0) ? w.x : (q == 1) ? w.y : (q == 2) ? w.z : w.w;
+  };
 
   for (int b = tid; b < kBuckets; b += kPermThreads) cnt[b] = 0;
   __syncthreads();
   const int groups = (L + 3) >> 2;
   for (int g = tid; g < groups; g += kPermThreads) {
     uint4 w = philox4x32_10(make_uint4((uint32_t)g, perm, A.pair_id, tagB), k0, k1);
+    const uint32_t wv[4] = {w.x, w.y, w.z, w.w};
 #pragma unroll
-    for (int q = 0; q < 4; ++q)
-      if (4 * g + q < L) atomicAdd(&cnt[bucket_of(w, q)], 1);
+    for (int q = 0; q < 4; ++q) {
+      if (4 * g + q < L) {
+        if (kWords) sW[4 * g + q] = wv[q];
+        atomicAdd(&cnt[wv[q] >> kLowBits], 1);
+      }
+    }
   }
   __syncthreads();
   // exclusive scan of the counters: warp w scans buckets [w*kPerWarp, (w+1)*kPerWarp)
@@ -123,14 +141,22 @@ __global__ void __launch_bounds__(kPermThreads) perm_kernel(const PermArgs A) {
     for (int r = 0; r < kPerWarp; r += 32) cnt[warp * kPerWarp + r + lane] += off;
   }
   __syncthreads();
-  for (int g = tid; g < groups; g += kPermThreads) {
-    uint4 w = philox4x32_10(make_uint4((uint32_t)g, perm, A.pair_id, tagB), k0, k1);
+  if (kWords) {
+    for (int e = tid; e < L; e += kPermThreads) {
+      const int pos = atomicAdd(&cnt[sW[e] >> kLowBits], 1);
+      sA[pos] = (uint16_t)e;
+    }
+  } else {
+    for (int g = tid; g < groups; g += kPermThreads) {
+      uint4 w = philox4x32_10(make_uint4((uint32_t)g, perm, A.pair_id, tagB), k0, k1);
+      const uint32_t wv[4] = {w.x, w.y, w.z, w.w};
 #pragma unroll
-    for (int q = 0; q < 4; ++q) {
-      int e = 4 * g + q;
-      if (e < L) {
-        int pos = atomicAdd(&cnt[bucket_of(w, q)], 1);
-        sA[pos] = (uint16_t)e;
+      for (int q = 0; q < 4; ++q) {
+        const int e = 4 * g + q;
+        if (e < L) {
+          const int pos = atomicAdd(&cnt[wv[q] >> kLowBits], 1);
+          sA[pos] = (uint16_t)e;
+        }
       }
     }
   }
@@ -156,9 +182,13 @@ __global__ void __launch_bounds__(kPermThreads) perm_kernel(const PermArgs A) {
     st.k0 = k0;
     st.k1 = k1;
     st.used = 4;
-    for (int i = sz - 1; i >= 1; --i) {
-      uint32_t j = st.bounded((uint32_t)(i + 1));
-      uint16_t tmp = a[i];
+    for (int i = 1; i < sz; ++i) {
+      const uint32_t n = (uint32_t)(i + 1);
+      const unsigned long long m = (unsigned long long)(word_of(a[i]) & kLowMask) * n;
+      uint32_t j = (uint32_t)(m >> kLowBits);
+      const uint32_t l = (uint32_t)m & kLowMask;
+      if (l < n && l < (kLowMask + 1u) % n) j = st.bounded(n);
+      const uint16_t tmp = a[i];
       a[i] = a[j];
       a[j] = tmp;
     }
@@ -171,6 +201,17 @@ __global__ void __launch_bounds__(kPermThreads) perm_kernel(const PermArgs A) {
   if (A.sigma) {
     int* so = A.sigma + (long long)blockIdx.x * A.sstride;
     for (int p = tid; p < L; p += kPermThreads) so[p] = sA[p];
+  }
+}
+
+__global__ void __launch_bounds__(kPermThreads) perm_kernel(const PermArgs A) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  int* cnt = reinterpret_cast<int*>(smem_raw);
+  if (A.L <= kPermWordsMaxL) {
+    uint32_t* sW = reinterpret_cast<uint32_t*>(cnt + kBuckets);
+    perm_body<true>(A, cnt, reinterpret_cast<uint16_t*>(sW + A.L), sW);
+  } else {
+    perm_body<false>(A, cnt, reinterpret_cast<uint16_t*>(cnt + kBuckets), nullptr);
   }
 }
 
@@ -252,7 +293,8 @@ cudaError_t launch_table_grid(const TableGridArgs& a, int C, int ctas, cudaStrea
 
 cudaError_t launch_perm(const PermArgs& a, int count, cudaStream_t s) {
   if (count <= 0) return cudaSuccess;
-  size_t smem = (size_t)kBuckets * 4 + (((size_t)a.L * 2 + 15) & ~(size_t)15);
+  size_t smem = (size_t)kBuckets * 4 + (a.L <= kPermWordsMaxL ? (size_t)a.L * 4 : 0) +
+                (((size_t)a.L * 2 + 15) & ~(size_t)15);
   cudaError_t e = cudaFuncSetAttribute(perm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   perm_kernel<<<count, kPermThreads, smem, s>>>(a);

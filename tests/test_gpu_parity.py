@@ -221,3 +221,16 @@ def test_table_sweep_beyond_16_bit_overlaps(engine):
         assert short.unpermuted == long_run.unpermuted
         assert np.array_equal(short.records, long_run.records[first - 1:first - 1 + n])
     dp.close()
+
+
+@pytest.mark.parametrize("N", [30000, 40000])
+def test_philox_permutations_long_lists_match_spec(engine, N):
+    # 30,000 elements: the kernel keeps every Philox word in shared memory;
+    # 40,000: it recomputes a word where the shuffle needs it.  Same spec.
+    p = synth.copula_pair(N, 0.1, seed=60)
+    dp = engine.pair(p.ranks1, p.feat1, p.ranks2, p.feat2, p.n_features, p.population)
+    seed = 0xFEEDFACE
+    i1, _ = dp.export_permutations(seed, 11, 3)
+    for b in range(3):
+        assert np.array_equal(O.shuffle(seed, 0, 11 + b, 1, N), i1[b])
+    dp.close()

@@ -209,3 +209,37 @@ def test_shuffle_position_marginals():
     chi2 = ((pos - exp) ** 2 / exp).sum()
     dof = (L - 1) ** 2
     assert abs(chi2 - dof) < 6 * math.sqrt(2 * dof), chi2
+
+
+def test_shuffle_within_bucket_orders_are_uniform():
+    # Lists long enough that buckets hold several elements: recompute each
+    # element's Philox word and bucket, and check that every bucket of size 3
+    # comes out in each of its 6 orders equally often (the forward
+    # Fisher-Yates pass on the words' low 20 bits) and every bucket of size 2
+    # swapped half the time.
+    L, n = 12288, 40
+    seed, pair, tag = 77, 0, 1
+    words = np.zeros(L, np.uint32)
+    c3 = {}
+    swaps2 = tot2 = 0
+    for t in range(1, n + 1):
+        for g in range((L + 3) // 4):
+            w = O.philox4x32_10([g, t, pair, 0x10000000 | (tag << 24)], [seed & 0xFFFFFFFF, seed >> 32])
+            words[4 * g:4 * g + 4] = w[:min(4, L - 4 * g)]
+        bucket = words >> 20
+        s = O.shuffle(seed, pair, t, tag, L)
+        starts = np.searchsorted(np.sort(bucket), np.arange(4097))
+        for b in range(4096):
+            seg = s[starts[b]:starts[b + 1]]
+            assert np.all(bucket[seg] == b)
+            if len(seg) == 2:
+                tot2 += 1
+                swaps2 += int(seg[0] > seg[1])
+            elif len(seg) == 3:
+                key = tuple(np.argsort(np.argsort(seg)).tolist())
+                c3[key] = c3.get(key, 0) + 1
+    assert abs(swaps2 - tot2 / 2) < 5 * math.sqrt(tot2 / 4), (swaps2, tot2)
+    m3 = sum(c3.values())
+    exp = m3 / 6.0
+    chi2 = sum((c - exp) ** 2 / exp for c in c3.values())
+    assert len(c3) == 6 and chi2 < 25.0, (chi2, c3)
