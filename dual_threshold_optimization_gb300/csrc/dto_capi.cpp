@@ -279,7 +279,9 @@ void fill_result(const dto_pair* P, const TaskResult& r, int permuted, dto_resul
 }
 
 int grid_tasks(dto_ctx* ctx, dto_pair* P, const int16_t* dX, long long xstride, int ntask, int mode,
-               TaskResult* dOut, int* dumpK = nullptr, double* dumpP = nullptr, bool guess = false) {
+               TaskResult* dOut, int* dumpK = nullptr, double* dumpP = nullptr, bool guess = false,
+               cudaStream_t stream = nullptr) {
+  if (!stream) stream = ctx->stream;
   GridArgs a{};
   a.P = P->dev;
   a.P.LF = ctx->dLF;  // the context's table may have grown since the pair was created
@@ -295,12 +297,12 @@ int grid_tasks(dto_ctx* ctx, dto_pair* P, const int16_t* dX, long long xstride, 
   a.guess_hist = (guess && mode == kModeScreen) ? ctx->dGuess : nullptr;
   a.dump_k = dumpK;
   a.dump_p = dumpP;
-  CK(cudaMemsetAsync(ctx->dWork, 0, sizeof(int), ctx->stream));
+  CK(cudaMemsetAsync(ctx->dWork, 0, sizeof(int), stream));
   int ctas = std::min(ctx->nsm, (ntask + kGridWarps - 1) / kGridWarps);
   ctas = std::max(ctas, 1);
-  CK(cudaEventRecord(ctx->evk[2], ctx->stream));
-  CK(launch_grid(a, ctas, ctx->stream));
-  CK(cudaEventRecord(ctx->evk[3], ctx->stream));
+  CK(cudaEventRecord(ctx->evk[2], stream));
+  CK(launch_grid(a, ctas, stream));
+  CK(cudaEventRecord(ctx->evk[3], stream));
   ctx->acc_launches += 1;
   return DTO_OK;
 }
@@ -807,137 +809,168 @@ int dto_run_range(dto_ctx* ctx, dto_pair* P, uint32_t perm_first, int64_t n_perm
   CK(cudaMemsetAsync(ctx->dRefined, 0, 3 * sizeof(unsigned long long), ctx->stream));
   CK(cudaMemsetAsync(ctx->dGuess, 0, 2048, ctx->stream));
   CK(cudaEventRecord(ctx->ev0, ctx->stream));
-  // Task 0 (unpermuted) rides in row 0 of the first batch, so it runs
-  // concurrently with the first permutations.
   std::vector<double> minp((size_t)n_perm);
   TaskResult unperm{};
   // The unpermuted task (task 0) rides in row 0 of the first batch, through
-  // the exhaustive screen.  With the table screen, the first batch holds
-  // first_batch permutations; its 90th and 99th percentiles and maximum of
-  // the minimum p set the three-level table ladder of the remaining batches.
+  // the exhaustive screen.  With the table screen (long runs), the first
+  // batch holds first_batch permutations; its 90th and 99th percentiles and
+  // maximum of the minimum p set the three-level table ladder of the
+  // remaining batches.
   const long long first_batch = 1024;
   const bool use_table = (mode == kModeScreen) && n_perm > 2 * first_batch;
-  int nlev = 0;
-  long long pipe_from = -1;
-  long long step = use_table ? first_batch : batch;
-  for (long long b0 = 0; b0 < std::max<long long>(n_perm, 1); b0 += step, step = batch) {
-    const int row0 = (b0 == 0) ? 1 : 0;
-    int cnt = (int)std::min(step, n_perm - b0);
-    if (cnt < 0) cnt = 0;
-    const int32_t* dI = nullptr;
-    if (perm_idx && cnt > 0) {
-      size_t bytes = (size_t)cnt * L12 * 4;
-      rc = grow(ctx, &dIdx, &idxBytes, bytes);
-      if (rc) return rc;
-      CK(cudaMemcpyAsync(dIdx, perm_idx + b0 * L12, bytes, cudaMemcpyHostToDevice, ctx->stream));
-      ctx->acc_h2d += (long long)bytes;
-      dI = (const int32_t*)dIdx;
-    }
-    if (cnt > 0) {
-      rc = make_labels(ctx, P, seed, (uint32_t)(perm_first + b0), cnt, dI, row0);
-      if (rc) return rc;
-    } else {
-      rc = grow(ctx, &ctx->dX, &ctx->xBytes, (size_t)xs * 2);
-      if (rc) return rc;
-    }
-    if (row0) CK(cudaMemcpyAsync(ctx->dX, P->dYlab, (size_t)P->N1 * 2, cudaMemcpyDeviceToDevice, ctx->stream));
-    const int ntask = cnt + row0;
-    const int16_t* X = (const int16_t*)ctx->dX;
-    rc = grid_tasks(ctx, P, X, xs, ntask, mode, dRes, nullptr, nullptr, true);
-    if (rc) return rc;
-    CK(cudaMemcpyAsync(hRes, dRes, (size_t)ntask * sizeof(TaskResult), cudaMemcpyDeviceToHost, ctx->stream));
-    ctx->acc_d2h += (long long)ntask * (long long)sizeof(TaskResult);
-    CK(cudaStreamSynchronize(ctx->stream));
-    {
-      float ms = 0.f;
-      if (cnt > 0 && cudaEventElapsedTime(&ms, ctx->evk[0], ctx->evk[1]) == cudaSuccess) ctx->acc_perm_ms += ms;
-      if (cudaEventElapsedTime(&ms, ctx->evk[2], ctx->evk[3]) == cudaSuccess) ctx->acc_grid_ms += ms;
-    }
-    if (row0) unperm = hRes[0];
+  auto take = [&](const TaskResult* hr, long long b0, int cnt) {
     for (int q = 0; q < cnt; ++q) {
-      const TaskResult& r = hRes[q + row0];
+      const TaskResult& r = hr[q];
       minp[(size_t)(b0 + q)] = r.p;
       if (out_minp) out_minp[b0 + q] = r.p;
       if (out_perm) fill_result(P, r, 1, &out_perm[b0 + q]);
     }
-    if (use_table && row0 && cnt >= 256) {
-      std::vector<double> v(minp.begin() + b0, minp.begin() + b0 + cnt);
-      std::sort(v.begin(), v.end());
-      const double p90 = v[(size_t)(kLevel0Quantile * (double)(v.size() - 1))];
-      const double p99 = v[(size_t)(0.99 * (double)(v.size() - 1))];
-      const double pmax = v.back();
-      if (p90 > 1e-300) {
-        const int sc = P->fshift;
-        const int t0 = fixed_log(p90, sc);
-        const int t1 = std::max(fixed_log(p99, sc), t0 + 1);
-        const int t2 = std::max((int)std::min(0.0, std::floor((std::log(pmax) + 1.0) * std::ldexp(1.0, sc))), t1 + 1);
-        rc = ensure_table(ctx, P, 0, t0);
+  };
+  auto upload_idx = [&](void** buf, size_t* cap, long long b0, int cnt, const int32_t** dI) -> int {
+    *dI = nullptr;
+    if (!perm_idx || cnt <= 0) return DTO_OK;
+    const size_t bytes = (size_t)cnt * L12 * 4;
+    int r = grow(ctx, buf, cap, bytes);
+    if (r) return r;
+    CK(cudaMemcpyAsync(*buf, perm_idx + b0 * L12, bytes, cudaMemcpyHostToDevice, ctx->stream));
+    ctx->acc_h2d += (long long)bytes;
+    *dI = (const int32_t*)*buf;
+    return DTO_OK;
+  };
+  if (!use_table) {
+    for (long long b0 = 0; b0 < std::max<long long>(n_perm, 1); b0 += batch) {
+      const int row0 = (b0 == 0) ? 1 : 0;
+      const int cnt = (int)std::max(0LL, std::min(batch, n_perm - b0));
+      const int32_t* dI = nullptr;
+      rc = upload_idx(&dIdx, &idxBytes, b0, cnt, &dI);
+      if (rc) return rc;
+      if (cnt > 0) {
+        rc = make_labels(ctx, P, seed, (uint32_t)(perm_first + b0), cnt, dI, row0);
         if (rc) return rc;
-        rc = ensure_table(ctx, P, 1, t1);
+      } else {
+        rc = grow(ctx, &ctx->dX, &ctx->xBytes, (size_t)xs * 2);
         if (rc) return rc;
-        rc = ensure_table(ctx, P, 2, t2);
-        if (rc) return rc;
-        nlev = 3;
-        pipe_from = b0 + cnt;
-        break;
       }
+      if (row0) CK(cudaMemcpyAsync(ctx->dX, P->dYlab, (size_t)P->N1 * 2, cudaMemcpyDeviceToDevice, ctx->stream));
+      const int ntask = cnt + row0;
+      rc = grid_tasks(ctx, P, (const int16_t*)ctx->dX, xs, ntask, mode, dRes, nullptr, nullptr, true);
+      if (rc) return rc;
+      CK(cudaMemcpyAsync(hRes, dRes, (size_t)ntask * sizeof(TaskResult), cudaMemcpyDeviceToHost, ctx->stream));
+      ctx->acc_d2h += (long long)ntask * (long long)sizeof(TaskResult);
+      CK(cudaStreamSynchronize(ctx->stream));
+      float ms = 0.f;
+      if (cnt > 0 && cudaEventElapsedTime(&ms, ctx->evk[0], ctx->evk[1]) == cudaSuccess) ctx->acc_perm_ms += ms;
+      if (cudaEventElapsedTime(&ms, ctx->evk[2], ctx->evk[3]) == cudaSuccess) ctx->acc_grid_ms += ms;
+      if (row0) unperm = hRes[0];
+      take(hRes + row0, b0, cnt);
     }
-  }
-  if (pipe_from >= 0 && pipe_from < n_perm) {
-    // Remaining batches, two in flight: while batch b's later table levels,
-    // exhaustive fallback and result copy run on the side stream, batch
-    // b+1's permutations and level-0 table sweep run on the main stream.
+  } else {
+    // Slots left busy by a call that returned early hold nothing of this call.
+    CK(cudaStreamSynchronize(ctx->side));
+    for (BatchSlot& sl : ctx->slot) sl.busy = false;
+    // Batch 0 (task 0 + first_batch permutations) runs through the exhaustive
+    // screen on the side stream.  Its slowest tasks (the permutations with
+    // the largest minimum p) take several times a typical task; meanwhile the
+    // main stream draws the labels of the first two pipelined batches.
+    const int cnt0 = (int)first_batch;
+    const int32_t* dI0 = nullptr;
+    rc = upload_idx(&dIdx, &idxBytes, 0, cnt0, &dI0);
+    if (rc) return rc;
+    rc = make_labels(ctx, P, seed, perm_first, cnt0, dI0, 1);
+    if (rc) return rc;
+    CK(cudaMemcpyAsync(ctx->dX, P->dYlab, (size_t)P->N1 * 2, cudaMemcpyDeviceToDevice, ctx->stream));
+    CK(cudaEventRecord(ctx->evSide, ctx->stream));
+    CK(cudaStreamWaitEvent(ctx->side, ctx->evSide, 0));
+    rc = grid_tasks(ctx, P, (const int16_t*)ctx->dX, xs, cnt0 + 1, mode, dRes, nullptr, nullptr, true, ctx->side);
+    if (rc) return rc;
+    CK(cudaMemcpyAsync(hRes, dRes, (size_t)(cnt0 + 1) * sizeof(TaskResult), cudaMemcpyDeviceToHost, ctx->side));
+    ctx->acc_d2h += (long long)(cnt0 + 1) * (long long)sizeof(TaskResult);
+    CK(cudaEventRecord(ctx->evSide, ctx->side));
+    // Labels of the pipelined batches b = 0, 1, ... (permutations
+    // first_batch + b * batch on), slot b & 1; the first two are drawn now.
+    const long long pipe_from = first_batch;
+    const long long npipe = (n_perm - pipe_from + batch - 1) / batch;
+    bool drawn[2] = {false, false};
+    auto draw = [&](long long it) -> int {
+      BatchSlot& sl = ctx->slot[it & 1];
+      const long long b0 = pipe_from + it * batch;
+      const int cnt = (int)std::min(batch, n_perm - b0);
+      if (!sl.ev[0])
+        for (cudaEvent_t& e : sl.ev) CK(cudaEventCreate(&e));
+      if (!sl.dCnt) CK(cudaMalloc(&sl.dCnt, 256));
+      int r = grow(ctx, &sl.dX, &sl.xBytes, (size_t)cnt * xs * 2);
+      if (!r) r = grow(ctx, &sl.dRes, &sl.resBytes, (size_t)cnt * sizeof(TaskResult));
+      if (!r) r = grow_host(ctx, &sl.hRes, &sl.hResBytes, (size_t)cnt * sizeof(TaskResult));
+      if (!r) r = grow(ctx, &sl.dFall, &sl.fallBytes, (size_t)3 * cnt * 4);
+      if (r) return r;
+      const int32_t* dI = nullptr;
+      r = upload_idx(&sl.dIdx, &sl.idxBytes, b0, cnt, &dI);
+      if (r) return r;
+      CK(cudaEventRecord(sl.ev[0], ctx->stream));
+      r = make_labels_launch(ctx, P, seed, (uint32_t)(perm_first + b0), cnt, dI, (int16_t*)sl.dX, xs);
+      if (r) return r;
+      CK(cudaEventRecord(sl.ev[1], ctx->stream));
+      sl.b0 = b0;
+      sl.cnt = cnt;
+      return DTO_OK;
+    };
+    for (long long it = 0; it < std::min<long long>(npipe, 2); ++it) {
+      rc = draw(it);
+      if (rc) return rc;
+      drawn[it] = true;
+    }
+    // the first batch's results set the ladder
+    CK(cudaEventSynchronize(ctx->evSide));
+    {
+      float ms = 0.f;
+      if (cudaEventElapsedTime(&ms, ctx->evk[0], ctx->evk[1]) == cudaSuccess) ctx->acc_perm_ms += ms;
+      if (cudaEventElapsedTime(&ms, ctx->evk[2], ctx->evk[3]) == cudaSuccess) ctx->acc_grid_ms += ms;
+    }
+    unperm = hRes[0];
+    take(hRes + 1, 0, cnt0);
+    std::vector<double> v(minp.begin(), minp.begin() + cnt0);
+    std::sort(v.begin(), v.end());
+    const double p90 = std::max(v[(size_t)(kLevel0Quantile * (double)(v.size() - 1))], 1e-300);
+    const double p99 = std::max(v[(size_t)(0.99 * (double)(v.size() - 1))], 1e-300);
+    const double pmax = std::max(v.back(), 1e-300);
+    const int sc = P->fshift;
+    const int t0 = fixed_log(p90, sc);
+    const int t1 = std::max(fixed_log(p99, sc), t0 + 1);
+    const int t2 = std::max((int)std::min(0.0, std::floor((std::log(pmax) + 1.0) * std::ldexp(1.0, sc))), t1 + 1);
+    rc = ensure_table(ctx, P, 0, t0);
+    if (rc) return rc;
+    rc = ensure_table(ctx, P, 1, t1);
+    if (rc) return rc;
+    rc = ensure_table(ctx, P, 2, t2);
+    if (rc) return rc;
+    const int nlev = 3;
+    // Two batches in flight: while batch b's later table levels, exhaustive
+    // fallback and result copy run on the side stream, batch b+1's labels and
+    // level-0 table sweep run on the main stream.
     auto harvest = [&](BatchSlot& sl) -> int {
       CK(cudaEventSynchronize(sl.ev[7]));
       float ms = 0.f;
       if (cudaEventElapsedTime(&ms, sl.ev[0], sl.ev[1]) == cudaSuccess) ctx->acc_perm_ms += ms;
       if (cudaEventElapsedTime(&ms, sl.ev[2], sl.ev[6]) == cudaSuccess) ctx->acc_grid_ms += ms;
       if (cudaEventElapsedTime(&ms, sl.ev[4], sl.ev[5]) == cudaSuccess) ctx->acc_grid_ms += ms;
-      const TaskResult* hr = (const TaskResult*)sl.hRes;
-      for (int q = 0; q < sl.cnt; ++q) {
-        const TaskResult& r = hr[q];
-        minp[(size_t)(sl.b0 + q)] = r.p;
-        if (out_minp) out_minp[sl.b0 + q] = r.p;
-        if (out_perm) fill_result(P, r, 1, &out_perm[sl.b0 + q]);
-      }
+      take((const TaskResult*)sl.hRes, sl.b0, sl.cnt);
       ctx->acc_d2h += (long long)sl.cnt * (long long)sizeof(TaskResult);
       sl.busy = false;
       return DTO_OK;
     };
-    // slots left busy by a call that returned early hold nothing of this call
-    CK(cudaStreamSynchronize(ctx->side));
-    for (BatchSlot& sl : ctx->slot) sl.busy = false;
-    long long it = 0;
-    for (long long b0 = pipe_from; b0 < n_perm; b0 += batch, ++it) {
+    for (long long it = 0; it < npipe; ++it) {
       BatchSlot& sl = ctx->slot[it & 1];
       if (sl.busy) {
         rc = harvest(sl);
         if (rc) return rc;
       }
-      const int cnt = (int)std::min(batch, n_perm - b0);
-      if (!sl.ev[0])
-        for (cudaEvent_t& e : sl.ev) CK(cudaEventCreate(&e));
-      if (!sl.dCnt) CK(cudaMalloc(&sl.dCnt, 256));
-      rc = grow(ctx, &sl.dX, &sl.xBytes, (size_t)cnt * xs * 2);
-      if (!rc) rc = grow(ctx, &sl.dRes, &sl.resBytes, (size_t)cnt * sizeof(TaskResult));
-      if (!rc) rc = grow_host(ctx, &sl.hRes, &sl.hResBytes, (size_t)cnt * sizeof(TaskResult));
-      if (!rc) rc = grow(ctx, &sl.dFall, &sl.fallBytes, (size_t)nlev * cnt * 4);
-      if (rc) return rc;
-      const int32_t* dI = nullptr;
-      if (perm_idx) {
-        const size_t bytes = (size_t)cnt * L12 * 4;
-        rc = grow(ctx, &sl.dIdx, &sl.idxBytes, bytes);
+      if (!(it < 2 && drawn[it])) {
+        rc = draw(it);
         if (rc) return rc;
-        CK(cudaMemcpyAsync(sl.dIdx, perm_idx + b0 * L12, bytes, cudaMemcpyHostToDevice, ctx->stream));
-        ctx->acc_h2d += (long long)bytes;
-        dI = (const int32_t*)sl.dIdx;
       }
+      const int cnt = sl.cnt;
       int16_t* X = (int16_t*)sl.dX;
       TaskResult* dR = (TaskResult*)sl.dRes;
-      CK(cudaEventRecord(sl.ev[0], ctx->stream));
-      rc = make_labels_launch(ctx, P, seed, (uint32_t)(perm_first + b0), cnt, dI, X, xs);
-      if (rc) return rc;
-      CK(cudaEventRecord(sl.ev[1], ctx->stream));
       CK(cudaEventRecord(sl.ev[2], ctx->stream));
       rc = table_levels(ctx, P, X, xs, cnt, dR, 0, 1, (int*)sl.dFall, sl.dCnt, ctx->stream, 0);
       if (rc) return rc;
@@ -952,11 +985,8 @@ int dto_run_range(dto_ctx* ctx, dto_pair* P, uint32_t perm_first, int64_t n_perm
       CK(cudaMemcpyAsync(sl.hRes, dR, (size_t)cnt * sizeof(TaskResult), cudaMemcpyDeviceToHost, ctx->side));
       CK(cudaEventRecord(sl.ev[7], ctx->side));
       sl.busy = true;
-      sl.b0 = b0;
-      sl.cnt = cnt;
     }
-    for (long long k = it; k < it + 2; ++k) {
-      BatchSlot& sl = ctx->slot[k & 1];
+    for (BatchSlot& sl : ctx->slot) {
       if (sl.busy) {
         rc = harvest(sl);
         if (rc) return rc;

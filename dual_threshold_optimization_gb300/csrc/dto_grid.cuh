@@ -174,14 +174,52 @@ __device__ __forceinline__ int lbt_fix(const uint32_t* __restrict__ F, int N, ui
   return L - kScreenSlack + (int)floor((double)(ls - err) * scale) - 1;
 }
 
-// Stage 2 behind a cheaper filter: a cell whose partial-sum lower bound
-// already exceeds B + 1 can neither be the FP64 argmin (its ln p is above B)
-// nor lower B, so its tail is not summed.
+// Closed-form lower bound of ln P(X >= k), fixed point, for the stage-2 gate.
+// With k0 = max(k, mode) and the pmf ratios r_x = pmf(x+1)/pmf(x)
+// non-increasing (the hypergeometric pmf is log-concave),
+//   P(X >= k) >= P(X >= k0) >= pmf(k0) sum_{j<w} rho^j = pmf(k0) (1 - rho^w) / (1 - rho)
+// for any w <= a - k0 + 1, rho = r_{k0+w-2} (every ratio of the first w - 1
+// terms is >= rho).  1 - rho = D / ((x+1)(N-a-b+x+1)) with the exact integer
+// D = (N+2)(x+1) - (a+1)(b+1), x = k0 + w - 2, so there is no cancellation;
+// the sum is -expm1(w log1p(-u)) / u, u = 1 - rho, each step a few ulps in
+// FP32, far inside the 1e-4 nats subtracted.  The best of w = 4, 32, 256 is
+// taken: a few transcendental operations instead of the 48 pmf terms of
+// lbt_fix, and close to ln p for cells with a wide distribution, whose tails
+// run to hundreds of terms.
+__device__ __forceinline__ int lbg_fix(const uint32_t* F, int N, uint32_t FN, int K, int n, int k,
+                                       long long mode, double scale) {
+  const int a = min(K, n), b = max(K, n);
+  const int k0 = (long long)k <= mode ? (int)mode : k;
+  const int L = logpmf_fix(F, N, FN, K, n, k0);
+  const long long ab1 = (long long)(a + 1) * (long long)(b + 1);
+  float g = 0.f;
+#pragma unroll
+  for (int q = 0; q < 3; ++q) {
+    const int w = min(q == 0 ? 4 : q == 1 ? 32 : 256, a - k0 + 1);
+    if (w < 2) break;
+    const int x = k0 + w - 2;
+    const long long D = (long long)(N + 2) * (long long)(x + 1) - ab1;
+    float G = (float)w;
+    if (D > 0) {
+      const float u = __fdiv_rn((float)D, (float)(x + 1) * (float)(N - a - b + x + 1));
+      G = -expm1f((float)w * log1pf(-fminf(u, 1.f))) / u;
+    }
+    g = fmaxf(g, logf(G));
+  }
+  return L - kScreenSlack + (int)floor((double)(g - 1e-4f) * scale) - 1;
+}
+
+// Stage 2 behind cheaper filters: a cell whose closed-form or partial-sum
+// lower bound already exceeds B + 1 can neither be the FP64 argmin (its ln p
+// is above B) nor lower B, so its tail is not summed.
 __device__ __forceinline__ Interval eval32_filtered(const uint32_t* F, int N, uint32_t FN, int K, int n, int k,
                                                     double scale, int B) {
   const int a = min(K, n), b = max(K, n);
   const long long mode = ((long long)(a + 1) * (long long)(b + 1)) / (long long)(N + 2);
-  if (k > 0 && lbt_fix(F, N, FN, K, n, k, mode, scale) > B + 1) return Interval{0x7fffffff, 0x7fffffff};
+  if (k > 0) {
+    if (lbg_fix(F, N, FN, K, n, k, mode, scale) > B + 1) return Interval{0x7fffffff, 0x7fffffff};
+    if (lbt_fix(F, N, FN, K, n, k, mode, scale) > B + 1) return Interval{0x7fffffff, 0x7fffffff};
+  }
   return eval32(F, N, FN, K, n, k, scale);
 }
 
