@@ -5,6 +5,6 @@ The permutation null of the threshold-pair search (the reference crate's
 hand-written CUDA for sm_103a behind the C ABI of ``include/dto.h``
 (``libdto.so``).  The Python modules mirror the reference's library surface.
 """
-from .engine import DevicePair, Engine  # noqa: F401
+from .engine import DevicePair, Engine, Job, Server  # noqa: F401
 
 __version__ = "0.1.0"

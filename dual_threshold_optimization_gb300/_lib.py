@@ -29,6 +29,8 @@ EXPORTS = (
     "dto_pair_info", "dto_pair_thresholds", "dto_pair_order", "dto_pair_upload_bytes", "dto_pair_set_stream", "dto_run", "dto_run_range", "dto_run_range_noalloc",
     "dto_optimize",
     "dto_grid_dump", "dto_hypergeom_sf", "dto_export_permutations", "dto_fdr",
+    "dto_serve_create", "dto_serve_destroy", "dto_serve_submit", "dto_serve_poll", "dto_serve_wait",
+    "dto_serve_last_error", "dto_serve_stats", "dto_run_device_bytes", "dto_batch_run",
 )
 
 
@@ -112,6 +114,18 @@ def lib():
     L.dto_export_permutations.argtypes = [_P, _P, C.c_uint64, C.c_uint32, C.c_int64, _P, _P]
     L.dto_fdr.argtypes = [C.c_int64, C.c_int64, C.c_int64, C.c_int64, C.c_double]
     L.dto_fdr.restype = C.c_double
+    L.dto_serve_create.argtypes = [_P, C.c_int, C.c_int64, C.POINTER(_P)]
+    L.dto_serve_destroy.argtypes = [_P]
+    L.dto_serve_submit.argtypes = [_P, _P, C.c_uint32, C.c_int64, C.c_uint64, C.c_int,
+                                   C.POINTER(DtoResult), _P, C.POINTER(DtoSummary), C.POINTER(C.c_int64)]
+    L.dto_serve_poll.argtypes = [_P, C.c_int64, C.POINTER(C.c_int)]
+    L.dto_serve_wait.argtypes = [_P, C.c_int64, C.POINTER(C.c_double), C.POINTER(C.c_double)]
+    L.dto_serve_last_error.argtypes = [_P]
+    L.dto_serve_last_error.restype = C.c_char_p
+    L.dto_serve_stats.argtypes = [_P, _P, _P, _P, _P]
+    L.dto_run_device_bytes.argtypes = [_P, C.c_int64]
+    L.dto_run_device_bytes.restype = C.c_int64
+    L.dto_batch_run.argtypes = [_P, C.c_int, _P, _P, _P, C.c_int, C.c_int, _P, _P, _P]
     for name in EXPORTS:
         getattr(L, name)
     for name in EXPORTS:
@@ -120,7 +134,9 @@ def lib():
                                              "dto_pair_destroy", "dto_pair_info",
                                              "dto_pair_thresholds", "dto_pair_order", "dto_run",
                                              "dto_run_range", "dto_optimize", "dto_grid_dump", "dto_hypergeom_sf",
-                                             "dto_export_permutations"):
+                                             "dto_export_permutations", "dto_serve_create",
+                                             "dto_serve_destroy", "dto_serve_submit", "dto_serve_poll",
+                                             "dto_serve_wait", "dto_serve_stats", "dto_batch_run"):
             fn.restype = C.c_int
     return L
 

@@ -1,6 +1,6 @@
-// dto_capi.cpp -- host side of libdto.so: contexts, list pairs, batch
-// orchestration of the permutation null, and the C ABI declared in
-// include/dto.h.
+// dto_capi.cpp -- host side of libdto.so: contexts, list pairs and the C ABI
+// declared in include/dto.h (the permutation-null driver is dto_lane.cpp,
+// the request executor dto_serve.cpp).
 //
 // Host arithmetic that feeds the kernels (thresholds, the log-factorial
 // tables) is written so that it gives the same bits on x86-64 and aarch64:
@@ -16,89 +16,9 @@
 #include <string>
 #include <vector>
 
-#include "../../include/dto.h"
-#include "dto_internal.h"
+#include "dto_host.h"
 
 using namespace dto;
-
-// Buffers of one in-flight batch of the table-screen pipeline.
-struct BatchSlot {
-  void* dX = nullptr;
-  size_t xBytes = 0;
-  void* dRes = nullptr;
-  size_t resBytes = 0;
-  void* hRes = nullptr;  // pinned
-  size_t hResBytes = 0;
-  void* dFall = nullptr;
-  size_t fallBytes = 0;
-  void* dIdx = nullptr;
-  size_t idxBytes = 0;
-  int* dCnt = nullptr;  // [0, 8): task counters, [8, 12): fallback counts
-  cudaEvent_t ev[8] = {};  // perm start/end, tables start, -, exhaustive start/end, tables done, batch done
-  bool busy = false;
-  long long b0 = 0;
-  int cnt = 0;
-};
-
-struct dto_ctx {
-  int device = 0;
-  int nsm = 0;
-  size_t smem_optin = 0;
-  cudaStream_t stream = nullptr;
-  cudaStream_t side = nullptr;  // the unpermuted task runs here next to the first batch
-  cudaEvent_t evSide = nullptr;
-  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
-  cudaEvent_t evk[4] = {nullptr, nullptr, nullptr, nullptr};  // perm start/end, grid start/end
-  // per-call accounting (reset by dto_run)
-  double acc_grid_ms = 0.0, acc_perm_ms = 0.0;
-  long long acc_launches = 0, acc_h2d = 0, acc_d2h = 0;
-  std::string err;
-  std::mutex mu;
-  // ln(m!) as double-double, m = 0..lf_cap
-  long long lf_cap = -1;
-  std::vector<double> lf_hi, lf_lo;
-  double2* dLF = nullptr;
-  // scratch, grown on demand
-  void* dX = nullptr;
-  size_t xBytes = 0;
-  void* dSig = nullptr;
-  size_t sigBytes = 0;
-  void* dRes = nullptr;
-  size_t resBytes = 0;
-  void* hRes = nullptr;  // pinned
-  size_t hResBytes = 0;
-  int* dWork = nullptr;
-  unsigned long long* dRefined = nullptr;
-  unsigned* dGuess = nullptr;  // bound histogram shared by the batches of one run
-  void* dHits[2] = {nullptr, nullptr};  // per-warp hit buffers of the table screen, one per stream
-  size_t hitBytes[2] = {0, 0};
-  BatchSlot slot[2];           // double-buffered batches of the table-screen pipeline
-  int* dNFall = nullptr;
-};
-
-struct dto_pair {
-  dto_ctx* ctx = nullptr;
-  uint32_t pair_id = 0;
-  long long N1 = 0, N2 = 0, npop = 0, nfeat = 0, ncommon = 0;
-  bool same_set = false;
-  std::vector<uint32_t> r1, r2, T1, T2;
-  std::vector<int32_t> order1, order2, f1, f2;
-  std::vector<int> c1, c2, map12;
-  std::vector<int16_t> lab2, ylab;
-  int C = 0, fshift = 0;
-  long long upload_bytes = 0;  // host-to-device bytes of dto_pair_create
-  // device
-  int* dRow = nullptr;
-  int* dNcnt = nullptr;
-  uint32_t* dF = nullptr;
-  int16_t* dYlab = nullptr;
-  int16_t* dLab2 = nullptr;
-  int* dMap12 = nullptr;
-  uint16_t* dKthr[3] = {nullptr, nullptr, nullptr};  // table screens, built for bounds kthr_tau
-  int kthr_tau[3] = {0, 0, 0};
-  bool kthr_ok[3] = {false, false, false};
-  PairDev dev{};
-};
 
 namespace {
 
@@ -171,56 +91,24 @@ long long dd_round_scaled(double hi, double lo, int f) {
   return (long long)r;
 }
 
-int set_err(dto_ctx* ctx, int code, const std::string& msg) {
-  if (ctx) ctx->err = msg;
-  return code;
-}
-
-int cuda_err(dto_ctx* ctx, cudaError_t e, const char* what) {
-  std::string m = std::string(what) + ": " + cudaGetErrorString(e);
-  return set_err(ctx, e == cudaErrorMemoryAllocation ? DTO_ERR_OOM : DTO_ERR_CUDA, m);
-}
-
-#define CK(call)                                     \
-  do {                                               \
-    cudaError_t e_ = (call);                         \
-    if (e_ != cudaSuccess) return cuda_err(ctx, e_, #call); \
-  } while (0)
-
-int grow(dto_ctx* ctx, void** p, size_t* cap, size_t need) {
-  if (need <= *cap) return DTO_OK;
-  if (*p) cudaFree(*p);
-  *p = nullptr;
-  *cap = 0;
-  size_t sz = std::max(need, (size_t)4096);
-  CK(cudaMalloc(p, sz));
-  *cap = sz;
-  return DTO_OK;
-}
-
-int grow_host(dto_ctx* ctx, void** p, size_t* cap, size_t need) {
-  if (need <= *cap) return DTO_OK;
-  if (*p) cudaFreeHost(*p);
-  *p = nullptr;
-  *cap = 0;
-  size_t sz = std::max(need, (size_t)4096);
-  CK(cudaMallocHost(p, sz));
-  *cap = sz;
-  return DTO_OK;
-}
-
 int ensure_lf(dto_ctx* ctx, long long nmax) {
+  std::lock_guard<std::mutex> g(ctx->lf_mu);
   if (nmax <= ctx->lf_cap) return DTO_OK;
   long long cap = std::max(nmax, 2 * ctx->lf_cap);
   cap = std::max(cap, 1024LL);
   lf_table_dd(cap, ctx->lf_hi, ctx->lf_lo);
   std::vector<double2> h((size_t)cap + 1);
   for (size_t m = 0; m <= (size_t)cap; ++m) h[m] = make_double2(ctx->lf_hi[m], ctx->lf_lo[m]);
-  if (ctx->dLF) cudaFree(ctx->dLF);
-  ctx->dLF = nullptr;
-  ctx->lf_cap = -1;
-  CK(cudaMalloc(&ctx->dLF, h.size() * sizeof(double2)));
-  CK(cudaMemcpy(ctx->dLF, h.data(), h.size() * sizeof(double2), cudaMemcpyHostToDevice));
+  double2* d = nullptr;
+  CK(cudaMalloc(&d, h.size() * sizeof(double2)));
+  cudaError_t e = cudaMemcpy(d, h.data(), h.size() * sizeof(double2), cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) {
+    cudaFree(d);
+    return cuda_err(ctx, e, "log-factorial table upload");
+  }
+  // kernels of other lanes may still read the old table: retire it, do not free it
+  double2* old = ctx->dLF.exchange(d);
+  if (old) ctx->lf_old.push_back(old);
   ctx->lf_cap = cap;
   return DTO_OK;
 }
@@ -239,244 +127,10 @@ std::vector<uint32_t> thresholds_of(uint32_t max_rank) {
 
 constexpr int kCs[] = {4, 8, 12, 16, 20, 24, 28, 32};
 
-// Quantile of the first batch's minimum p-values that sets the level-0 table.
-#ifndef DTO_L0_QUANTILE
-#define DTO_L0_QUANTILE 0.90
-#endif
-constexpr double kLevel0Quantile = DTO_L0_QUANTILE;
-
 int pick_C(int n2) {
   for (int c : kCs)
     if (32 * c >= n2) return c;
   return -1;
-}
-
-// Rows of the grid kernel need 16-byte aligned starts for vector loads.
-long long xstride_of(long long N1) { return (N1 + 7) & ~7LL; }
-
-int check_perm(const int32_t* idx, long long L) {
-  std::vector<char> seen((size_t)L, 0);
-  for (long long p = 0; p < L; ++p) {
-    int32_t v = idx[p];
-    if (v < 0 || v >= L || seen[(size_t)v]) return 0;
-    seen[(size_t)v] = 1;
-  }
-  return 1;
-}
-
-void fill_result(const dto_pair* P, const TaskResult& r, int permuted, dto_result* o) {
-  o->rank1 = P->T1[(size_t)r.i];
-  o->rank2 = P->T2[(size_t)r.j];
-  o->set1_len = P->c1[(size_t)r.i];
-  o->set2_len = P->c2[(size_t)r.j];
-  o->population_size = P->npop;
-  o->intersection_size = r.k;
-  o->pvalue = r.p;
-  o->permuted = permuted;
-  o->i = r.i;
-  o->j = r.j;
-  o->status = r.status;
-}
-
-int grid_tasks(dto_ctx* ctx, dto_pair* P, const int16_t* dX, long long xstride, int ntask, int mode,
-               TaskResult* dOut, int* dumpK = nullptr, double* dumpP = nullptr, bool guess = false,
-               cudaStream_t stream = nullptr) {
-  if (!stream) stream = ctx->stream;
-  GridArgs a{};
-  a.P = P->dev;
-  a.P.LF = ctx->dLF;  // the context's table may have grown since the pair was created
-  a.X = dX;
-  a.xstride = xstride;
-  a.ntask = ntask;
-  a.mode = mode;
-  size_t smemF = grid_smem_bytes(P->C, P->dev.n1, P->npop, 1);
-  a.smemF = smemF <= ctx->smem_optin ? 1 : 0;
-  a.out = dOut;
-  a.work = ctx->dWork;
-  a.n_refined = ctx->dRefined;
-  a.guess_hist = (guess && mode == kModeScreen) ? ctx->dGuess : nullptr;
-  a.dump_k = dumpK;
-  a.dump_p = dumpP;
-  CK(cudaMemsetAsync(ctx->dWork, 0, sizeof(int), stream));
-  int ctas = std::min(ctx->nsm, (ntask + kGridWarps - 1) / kGridWarps);
-  ctas = std::max(ctas, 1);
-  CK(cudaEventRecord(ctx->evk[2], stream));
-  CK(launch_grid(a, ctas, stream));
-  CK(cudaEventRecord(ctx->evk[3], stream));
-  ctx->acc_launches += 1;
-  return DTO_OK;
-}
-
-// Table screen `level` for bound tau (fixed-point ln p), built on the device.
-int ensure_table(dto_ctx* ctx, dto_pair* P, int level, int tau) {
-  if (P->kthr_ok[level] && P->kthr_tau[level] == tau) return DTO_OK;
-  if (!P->dKthr[level]) CK(cudaMalloc(&P->dKthr[level], table_entries(P->C, P->dev.n1) * 2));
-  TableArgs t{};
-  t.n1 = P->dev.n1;
-  t.n2 = P->dev.n2;
-  t.N = (int)P->npop;
-  t.C = P->C;
-  t.rowstart = P->dRow;
-  t.ncnt = P->dNcnt;
-  t.F = P->dF;
-  t.fshift = P->fshift;
-  t.tau = tau;
-  t.packed = P->ncommon <= kPackedMaxCommon ? 1 : 0;
-  t.kthr = P->dKthr[level];
-  CK(launch_table_build(t, ctx->nsm, ctx->stream));
-  ctx->acc_launches += 1;
-  P->kthr_tau[level] = tau;
-  P->kthr_ok[level] = true;
-  return DTO_OK;
-}
-
-// Tasks [0, ntask) of X through the table ladder: level l takes the tasks
-// that level l-1 could not settle (their minimum lies above its bound), and
-// the exhaustive screen takes what the last level leaves.  The lists and
-// their counts stay on the device.  `fall` holds nlev lists of cap entries,
-// `cnts` 8 task counters then 4 list counts.  The levels run on the context's
-// stream; the exhaustive screen runs on `xstream` after `evTab` (which may be
-// the same stream).
-int table_levels(dto_ctx* ctx, dto_pair* P, const int16_t* X, long long xstride, int ntask, TaskResult* dOut,
-                 int lev_begin, int lev_end, int* fall, int* cnts, cudaStream_t stream, int hb) {
-  const int cap = std::max(ntask, 1);
-  const int hitcap = 8192;
-  int rc = grow(ctx, &ctx->dHits[hb], &ctx->hitBytes[hb], (size_t)kTableCtasPerSm * ctx->nsm * kTableWarps * hitcap * 8);
-  if (rc) return rc;
-  if (lev_begin == 0) CK(cudaMemsetAsync(cnts, 0, 12 * sizeof(int), stream));
-  for (int level = lev_begin; level < lev_end; ++level) {
-    TableGridArgs a{};
-    a.P = P->dev;
-    a.P.LF = ctx->dLF;
-    a.X = X;
-    a.xstride = xstride;
-    a.ntask = ntask;
-    a.tau = P->kthr_tau[level];
-    a.kthr = P->dKthr[level];
-    a.packed = P->ncommon <= kPackedMaxCommon ? 1 : 0;
-    a.out = dOut;
-    a.work = cnts + level;
-    a.n_refined = ctx->dRefined;
-    a.fallback = fall + (size_t)level * cap;
-    a.nfallback = cnts + 8 + level;
-    a.task_list = level == 0 ? nullptr : fall + (size_t)(level - 1) * cap;
-    a.ntask_dev = level == 0 ? nullptr : cnts + 8 + level - 1;
-    a.hitbuf = (int2*)ctx->dHits[hb];
-    a.hitcap = hitcap;
-    // a later level sees the tasks the earlier ones left (about 10 % and 1 %
-    // of the batch); one warp per expected task keeps its latency to one sweep
-    const double expect = level == 0 ? 1.0 : level == 1 ? 0.15 : 0.03;
-    const int want = (int)(expect * (double)ntask / kTableWarps) + 1;
-    const int ctas = std::max(1, std::min(kTableCtasPerSm * ctx->nsm, want));
-    CK(launch_table_grid(a, P->C, ctas, stream));
-  }
-  ctx->acc_launches += lev_end - lev_begin;
-  return DTO_OK;
-}
-
-// The exhaustive screen of what the last table level left, on `stream`.
-int table_exhaustive(dto_ctx* ctx, dto_pair* P, const int16_t* X, long long xstride, int ntask, TaskResult* dOut,
-                     int nlev, const int* fall, int* cnts, cudaStream_t stream) {
-  const int cap = std::max(ntask, 1);
-  GridArgs g{};
-  g.P = P->dev;
-  g.P.LF = ctx->dLF;
-  g.X = X;
-  g.xstride = xstride;
-  g.ntask = ntask;
-  g.mode = kModeScreen;
-  g.smemF = grid_smem_bytes(P->C, P->dev.n1, P->npop, 1) <= ctx->smem_optin ? 1 : 0;
-  g.out = dOut;
-  g.work = cnts + nlev;
-  g.n_refined = ctx->dRefined;
-  g.task_list = fall + (size_t)(nlev - 1) * cap;
-  g.ntask_dev = cnts + 8 + nlev - 1;
-  CK(launch_grid(g, ctx->nsm, stream));
-  ctx->acc_launches += 1;
-  return DTO_OK;
-}
-
-int fixed_log(double p, int fshift) {
-  double t = std::floor(std::log(p) * std::ldexp(1.0, fshift));
-  return (int)std::max(-2.0e9, std::min(0.0, t));
-}
-
-// Labels of n_perm permutations starting at perm id `first` into ctx->dX.
-int make_labels_launch(dto_ctx* ctx, dto_pair* P, uint64_t seed, uint32_t first, int count,
-                       const int32_t* dIdx, int16_t* X, long long xs);
-
-int make_labels(dto_ctx* ctx, dto_pair* P, uint64_t seed, uint32_t first, int count,
-                const int32_t* dIdx /* nullable: test mode, [count][N1+N2] */, int row0 = 0) {
-  long long xs = xstride_of(P->N1);
-  int rc = grow(ctx, &ctx->dX, &ctx->xBytes, (size_t)(count + row0) * xs * 2);
-  if (rc) return rc;
-  int16_t* X = (int16_t*)ctx->dX + (size_t)row0 * xs;
-  CK(cudaEventRecord(ctx->evk[0], ctx->stream));
-  rc = make_labels_launch(ctx, P, seed, first, count, dIdx, X, xs);
-  CK(cudaEventRecord(ctx->evk[1], ctx->stream));
-  return rc;
-}
-
-int make_labels_launch(dto_ctx* ctx, dto_pair* P, uint64_t seed, uint32_t first, int count,
-                       const int32_t* dIdx, int16_t* X, long long xs) {
-  int rc = DTO_OK;
-  if (dIdx) {
-    ComposeArgs c{};
-    c.N1 = (int)P->N1;
-    c.N2 = (int)P->N2;
-    c.idx1 = dIdx;
-    c.idx2 = dIdx + P->N1;
-    c.stride = P->N1 + P->N2;
-    c.map12 = P->dMap12;
-    c.lab2 = P->dLab2;
-    c.X = X;
-    c.xstride = xs;
-    CK(launch_compose(c, count, ctx->stream));
-    ctx->acc_launches += 1;
-    return DTO_OK;
-  }
-  PermArgs a{};
-  a.seed = seed;
-  a.pair_id = P->pair_id;
-  a.perm_base = first;
-  a.xstride = xs;
-  if (P->same_set) {
-    // With identical feature sets only the relative order of the two lists
-    // matters: list 1 is shuffled, list 2 kept (idx2 = identity).
-    a.L = (int)P->N1;
-    a.list_tag = 1;
-    a.Ylab = P->dYlab;
-    a.X = X;
-    CK(launch_perm(a, count, ctx->stream));
-    ctx->acc_launches += 1;
-    return DTO_OK;
-  }
-  long long ss = P->N1 + P->N2;
-  rc = grow(ctx, &ctx->dSig, &ctx->sigBytes, (size_t)count * ss * 4);
-  if (rc) return rc;
-  int* sig = (int*)ctx->dSig;
-  a.L = (int)P->N1;
-  a.list_tag = 1;
-  a.sigma = sig;
-  a.sstride = ss;
-  CK(launch_perm(a, count, ctx->stream));
-  a.L = (int)P->N2;
-  a.list_tag = 2;
-  a.sigma = sig + P->N1;
-  CK(launch_perm(a, count, ctx->stream));
-  ComposeArgs c{};
-  c.N1 = (int)P->N1;
-  c.N2 = (int)P->N2;
-  c.idx1 = sig;
-  c.idx2 = sig + P->N1;
-  c.stride = ss;
-  c.map12 = P->dMap12;
-  c.lab2 = P->dLab2;
-  c.X = X;
-  c.xstride = xs;
-  CK(launch_compose(c, count, ctx->stream));
-  ctx->acc_launches += 3;
-  return DTO_OK;
 }
 
 }  // namespace
@@ -502,28 +156,20 @@ int dto_ctx_create(int device, dto_ctx** out) {
   *out = nullptr;
   dto_ctx* ctx = new dto_ctx();
   ctx->device = device;
-  auto fail = [&](cudaError_t e) {
+  cudaError_t e = cudaSetDevice(device);
+  cudaDeviceProp prop;
+  if (e == cudaSuccess) e = cudaGetDeviceProperties(&prop, device);
+  if (e != cudaSuccess) {
     delete ctx;
     return e == cudaErrorMemoryAllocation ? DTO_ERR_OOM : DTO_ERR_CUDA;
-  };
-  cudaError_t e = cudaSetDevice(device);
-  if (e != cudaSuccess) return fail(e);
-  cudaDeviceProp prop;
-  e = cudaGetDeviceProperties(&prop, device);
-  if (e != cudaSuccess) return fail(e);
+  }
   ctx->nsm = prop.multiProcessorCount;
   ctx->smem_optin = prop.sharedMemPerBlockOptin;
-  if ((e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking)) != cudaSuccess) return fail(e);
-  if ((e = cudaStreamCreateWithFlags(&ctx->side, cudaStreamNonBlocking)) != cudaSuccess) return fail(e);
-  if ((e = cudaEventCreateWithFlags(&ctx->evSide, cudaEventDisableTiming)) != cudaSuccess) return fail(e);
-  if ((e = cudaEventCreate(&ctx->ev0)) != cudaSuccess) return fail(e);
-  if ((e = cudaEventCreate(&ctx->ev1)) != cudaSuccess) return fail(e);
-  for (int q = 0; q < 4; ++q)
-    if ((e = cudaEventCreate(&ctx->evk[q])) != cudaSuccess) return fail(e);
-  if ((e = cudaMalloc(&ctx->dWork, 256)) != cudaSuccess) return fail(e);
-  if ((e = cudaMalloc(&ctx->dRefined, 256)) != cudaSuccess) return fail(e);
-  if ((e = cudaMalloc(&ctx->dGuess, 2048)) != cudaSuccess) return fail(e);
-  if ((e = cudaMalloc(&ctx->dNFall, 256)) != cudaSuccess) return fail(e);
+  const int rc = lane_create(ctx, &ctx->lane0, &ctx->err);
+  if (rc) {
+    delete ctx;
+    return rc;
+  }
   *out = ctx;
   return DTO_OK;
 }
@@ -531,43 +177,16 @@ int dto_ctx_create(int device, dto_ctx** out) {
 int dto_ctx_destroy(dto_ctx* ctx) {
   if (!ctx) return DTO_ERR_INVALID;
   cudaSetDevice(ctx->device);
-  if (ctx->stream) cudaStreamSynchronize(ctx->stream);
-  if (ctx->side) cudaStreamSynchronize(ctx->side);
-  cudaFree(ctx->dLF);
-  cudaFree(ctx->dX);
-  cudaFree(ctx->dSig);
-  cudaFree(ctx->dRes);
-  cudaFreeHost(ctx->hRes);
-  cudaFree(ctx->dWork);
-  cudaFree(ctx->dRefined);
-  cudaFree(ctx->dGuess);
-  cudaFree(ctx->dHits[0]);
-  cudaFree(ctx->dHits[1]);
-  for (BatchSlot& sl : ctx->slot) {
-    cudaFree(sl.dX);
-    cudaFree(sl.dRes);
-    cudaFreeHost(sl.hRes);
-    cudaFree(sl.dFall);
-    cudaFree(sl.dIdx);
-    cudaFree(sl.dCnt);
-    for (cudaEvent_t e : sl.ev)
-      if (e) cudaEventDestroy(e);
-  }
-  cudaFree(ctx->dNFall);
-  if (ctx->ev0) cudaEventDestroy(ctx->ev0);
-  if (ctx->ev1) cudaEventDestroy(ctx->ev1);
-  for (int q = 0; q < 4; ++q)
-    if (ctx->evk[q]) cudaEventDestroy(ctx->evk[q]);
-  if (ctx->evSide) cudaEventDestroy(ctx->evSide);
-  if (ctx->side) cudaStreamDestroy(ctx->side);
-  if (ctx->stream) cudaStreamDestroy(ctx->stream);
+  lane_destroy(ctx->lane0);
+  cudaFree(ctx->dLF.load());
+  for (double2* d : ctx->lf_old) cudaFree(d);
   delete ctx;
   return DTO_OK;
 }
 
 const char* dto_last_error(const dto_ctx* ctx) { return ctx ? ctx->err.c_str() : "null context"; }
 
-void* dto_ctx_stream(dto_ctx* ctx) { return ctx ? (void*)ctx->stream : nullptr; }
+void* dto_ctx_stream(dto_ctx* ctx) { return ctx ? (void*)ctx->lane0->stream : nullptr; }
 
 int64_t dto_generate_thresholds(uint32_t max_rank, uint32_t* out, int64_t cap) {
   std::vector<uint32_t> t = thresholds_of(max_rank);
@@ -598,6 +217,7 @@ int dto_pair_create(dto_ctx* ctx, const uint32_t* ranks1, const int32_t* feat1, 
   CK(cudaSetDevice(ctx->device));
   dto_pair* P = new dto_pair();
   P->ctx = ctx;
+  P->serial = ctx->next_serial.fetch_add(1);
   P->pair_id = 0;  // Philox stream id; dto_pair_set_stream changes it
   P->N1 = n1;
   P->N2 = n2;
@@ -688,7 +308,7 @@ int dto_pair_create(dto_ctx* ctx, const uint32_t* ranks1, const int32_t* feat1, 
     cudaError_t e = cudaMalloc(d, std::max(bytes, (size_t)16));
     if (e != cudaSuccess) return e;
     P->upload_bytes += (long long)bytes;
-    return cudaMemcpyAsync(*d, h, bytes, cudaMemcpyHostToDevice, ctx->stream);
+    return cudaMemcpyAsync(*d, h, bytes, cudaMemcpyHostToDevice, ctx->lane0->stream);
   };
   cudaError_t e = cudaSuccess;
   if (e == cudaSuccess) e = up((void**)&P->dRow, row.data(), row.size() * 4);
@@ -697,7 +317,7 @@ int dto_pair_create(dto_ctx* ctx, const uint32_t* ranks1, const int32_t* feat1, 
   if (e == cudaSuccess) e = up((void**)&P->dYlab, P->ylab.data(), P->ylab.size() * 2);
   if (e == cudaSuccess) e = up((void**)&P->dLab2, P->lab2.data(), P->lab2.size() * 2);
   if (e == cudaSuccess) e = up((void**)&P->dMap12, P->map12.data(), P->map12.size() * 4);
-  if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->lane0->stream);
   if (e != cudaSuccess) {
     dto_pair_destroy(P);
     return cuda_err(ctx, e, "pair upload");
@@ -729,7 +349,6 @@ int dto_pair_destroy(dto_pair* P) {
   cudaFree(P->dYlab);
   cudaFree(P->dLab2);
   cudaFree(P->dMap12);
-  for (int l = 0; l < 3; ++l) cudaFree(P->dKthr[l]);
   delete P;
   return DTO_OK;
 }
@@ -775,257 +394,9 @@ int dto_run_range(dto_ctx* ctx, dto_pair* P, uint32_t perm_first, int64_t n_perm
                   const int32_t* perm_idx, int precision, dto_result* out_unpermuted, double* out_minp,
                   dto_result* out_perm, dto_summary* out_summary) {
   if (!ctx || !P || P->ctx != ctx || !out_unpermuted) return set_err(ctx, DTO_ERR_INVALID, "null argument");
-  if (n_perm < 0 || n_perm > 0x7fffffffLL || (long long)perm_first + n_perm > 0xffffffffLL)
-    return set_err(ctx, DTO_ERR_INVALID, "n_perm out of range");
-  if (precision != DTO_PRECISION_FP64 && precision != DTO_PRECISION_SCREEN)
-    return set_err(ctx, DTO_ERR_INVALID, "unknown precision");
   std::lock_guard<std::mutex> g(ctx->mu);
-  CK(cudaSetDevice(ctx->device));
-  const long long L12 = P->N1 + P->N2;
-  if (perm_idx) {
-    for (long long b = 0; b < n_perm; ++b) {
-      if (!check_perm(perm_idx + b * L12, P->N1) || !check_perm(perm_idx + b * L12 + P->N1, P->N2))
-        return set_err(ctx, DTO_ERR_INVALID, "perm_idx row is not a permutation");
-    }
-  }
-  const int mode = precision == DTO_PRECISION_FP64 ? kModeFull64 : kModeScreen;
-  const long long xs = xstride_of(P->N1);
-  // batch size: bounded by 1 GiB of labels (and of test-mode indices)
-  long long batch = std::max(1LL, std::min<long long>((1LL << 30) / (xs * 2), 1LL << 20));
-  if (perm_idx) batch = std::min(batch, std::max(1LL, (1LL << 30) / (L12 * 4)));
-  if (!P->same_set && !perm_idx) batch = std::min(batch, std::max(1LL, (1LL << 30) / (L12 * 4)));
-  batch = std::min<long long>(batch, std::max<long long>(n_perm, 1));
-  int rc = grow(ctx, &ctx->dRes, &ctx->resBytes, (size_t)(batch + 1) * sizeof(TaskResult));
-  if (rc) return rc;
-  rc = grow_host(ctx, &ctx->hRes, &ctx->hResBytes, (size_t)(batch + 1) * sizeof(TaskResult));
-  if (rc) return rc;
-  void* dIdx = nullptr;
-  size_t idxBytes = 0;
-  struct Guard { void*& p; ~Guard() { if (p) cudaFree(p); } } guard{dIdx};
-  TaskResult* dRes = (TaskResult*)ctx->dRes;
-  TaskResult* hRes = (TaskResult*)ctx->hRes;
-  ctx->acc_grid_ms = ctx->acc_perm_ms = 0.0;
-  ctx->acc_launches = ctx->acc_h2d = ctx->acc_d2h = 0;
-  CK(cudaMemsetAsync(ctx->dRefined, 0, 3 * sizeof(unsigned long long), ctx->stream));
-  CK(cudaMemsetAsync(ctx->dGuess, 0, 2048, ctx->stream));
-  CK(cudaEventRecord(ctx->ev0, ctx->stream));
-  std::vector<double> minp((size_t)n_perm);
-  TaskResult unperm{};
-  // The unpermuted task (task 0) rides in row 0 of the first batch, through
-  // the exhaustive screen.  With the table screen (long runs), the first
-  // batch holds first_batch permutations; its 90th and 99th percentiles and
-  // maximum of the minimum p set the three-level table ladder of the
-  // remaining batches.
-  const long long first_batch = 1024;
-  const bool use_table = (mode == kModeScreen) && n_perm > 2 * first_batch;
-  auto take = [&](const TaskResult* hr, long long b0, int cnt) {
-    for (int q = 0; q < cnt; ++q) {
-      const TaskResult& r = hr[q];
-      minp[(size_t)(b0 + q)] = r.p;
-      if (out_minp) out_minp[b0 + q] = r.p;
-      if (out_perm) fill_result(P, r, 1, &out_perm[b0 + q]);
-    }
-  };
-  auto upload_idx = [&](void** buf, size_t* cap, long long b0, int cnt, const int32_t** dI) -> int {
-    *dI = nullptr;
-    if (!perm_idx || cnt <= 0) return DTO_OK;
-    const size_t bytes = (size_t)cnt * L12 * 4;
-    int r = grow(ctx, buf, cap, bytes);
-    if (r) return r;
-    CK(cudaMemcpyAsync(*buf, perm_idx + b0 * L12, bytes, cudaMemcpyHostToDevice, ctx->stream));
-    ctx->acc_h2d += (long long)bytes;
-    *dI = (const int32_t*)*buf;
-    return DTO_OK;
-  };
-  if (!use_table) {
-    for (long long b0 = 0; b0 < std::max<long long>(n_perm, 1); b0 += batch) {
-      const int row0 = (b0 == 0) ? 1 : 0;
-      const int cnt = (int)std::max(0LL, std::min(batch, n_perm - b0));
-      const int32_t* dI = nullptr;
-      rc = upload_idx(&dIdx, &idxBytes, b0, cnt, &dI);
-      if (rc) return rc;
-      if (cnt > 0) {
-        rc = make_labels(ctx, P, seed, (uint32_t)(perm_first + b0), cnt, dI, row0);
-        if (rc) return rc;
-      } else {
-        rc = grow(ctx, &ctx->dX, &ctx->xBytes, (size_t)xs * 2);
-        if (rc) return rc;
-      }
-      if (row0) CK(cudaMemcpyAsync(ctx->dX, P->dYlab, (size_t)P->N1 * 2, cudaMemcpyDeviceToDevice, ctx->stream));
-      const int ntask = cnt + row0;
-      rc = grid_tasks(ctx, P, (const int16_t*)ctx->dX, xs, ntask, mode, dRes, nullptr, nullptr, true);
-      if (rc) return rc;
-      CK(cudaMemcpyAsync(hRes, dRes, (size_t)ntask * sizeof(TaskResult), cudaMemcpyDeviceToHost, ctx->stream));
-      ctx->acc_d2h += (long long)ntask * (long long)sizeof(TaskResult);
-      CK(cudaStreamSynchronize(ctx->stream));
-      float ms = 0.f;
-      if (cnt > 0 && cudaEventElapsedTime(&ms, ctx->evk[0], ctx->evk[1]) == cudaSuccess) ctx->acc_perm_ms += ms;
-      if (cudaEventElapsedTime(&ms, ctx->evk[2], ctx->evk[3]) == cudaSuccess) ctx->acc_grid_ms += ms;
-      if (row0) unperm = hRes[0];
-      take(hRes + row0, b0, cnt);
-    }
-  } else {
-    // Slots left busy by a call that returned early hold nothing of this call.
-    CK(cudaStreamSynchronize(ctx->side));
-    for (BatchSlot& sl : ctx->slot) sl.busy = false;
-    // Batch 0 (task 0 + first_batch permutations) runs through the exhaustive
-    // screen on the side stream.  Its slowest tasks (the permutations with
-    // the largest minimum p) take several times a typical task; meanwhile the
-    // main stream draws the labels of the first two pipelined batches.
-    const int cnt0 = (int)first_batch;
-    const int32_t* dI0 = nullptr;
-    rc = upload_idx(&dIdx, &idxBytes, 0, cnt0, &dI0);
-    if (rc) return rc;
-    rc = make_labels(ctx, P, seed, perm_first, cnt0, dI0, 1);
-    if (rc) return rc;
-    CK(cudaMemcpyAsync(ctx->dX, P->dYlab, (size_t)P->N1 * 2, cudaMemcpyDeviceToDevice, ctx->stream));
-    CK(cudaEventRecord(ctx->evSide, ctx->stream));
-    CK(cudaStreamWaitEvent(ctx->side, ctx->evSide, 0));
-    rc = grid_tasks(ctx, P, (const int16_t*)ctx->dX, xs, cnt0 + 1, mode, dRes, nullptr, nullptr, true, ctx->side);
-    if (rc) return rc;
-    CK(cudaMemcpyAsync(hRes, dRes, (size_t)(cnt0 + 1) * sizeof(TaskResult), cudaMemcpyDeviceToHost, ctx->side));
-    ctx->acc_d2h += (long long)(cnt0 + 1) * (long long)sizeof(TaskResult);
-    CK(cudaEventRecord(ctx->evSide, ctx->side));
-    // Labels of the pipelined batches b = 0, 1, ... (permutations
-    // first_batch + b * batch on), slot b & 1; the first two are drawn now.
-    const long long pipe_from = first_batch;
-    const long long npipe = (n_perm - pipe_from + batch - 1) / batch;
-    bool drawn[2] = {false, false};
-    auto draw = [&](long long it) -> int {
-      BatchSlot& sl = ctx->slot[it & 1];
-      const long long b0 = pipe_from + it * batch;
-      const int cnt = (int)std::min(batch, n_perm - b0);
-      if (!sl.ev[0])
-        for (cudaEvent_t& e : sl.ev) CK(cudaEventCreate(&e));
-      if (!sl.dCnt) CK(cudaMalloc(&sl.dCnt, 256));
-      int r = grow(ctx, &sl.dX, &sl.xBytes, (size_t)cnt * xs * 2);
-      if (!r) r = grow(ctx, &sl.dRes, &sl.resBytes, (size_t)cnt * sizeof(TaskResult));
-      if (!r) r = grow_host(ctx, &sl.hRes, &sl.hResBytes, (size_t)cnt * sizeof(TaskResult));
-      if (!r) r = grow(ctx, &sl.dFall, &sl.fallBytes, (size_t)3 * cnt * 4);
-      if (r) return r;
-      const int32_t* dI = nullptr;
-      r = upload_idx(&sl.dIdx, &sl.idxBytes, b0, cnt, &dI);
-      if (r) return r;
-      CK(cudaEventRecord(sl.ev[0], ctx->stream));
-      r = make_labels_launch(ctx, P, seed, (uint32_t)(perm_first + b0), cnt, dI, (int16_t*)sl.dX, xs);
-      if (r) return r;
-      CK(cudaEventRecord(sl.ev[1], ctx->stream));
-      sl.b0 = b0;
-      sl.cnt = cnt;
-      return DTO_OK;
-    };
-    for (long long it = 0; it < std::min<long long>(npipe, 2); ++it) {
-      rc = draw(it);
-      if (rc) return rc;
-      drawn[it] = true;
-    }
-    // the first batch's results set the ladder
-    CK(cudaEventSynchronize(ctx->evSide));
-    {
-      float ms = 0.f;
-      if (cudaEventElapsedTime(&ms, ctx->evk[0], ctx->evk[1]) == cudaSuccess) ctx->acc_perm_ms += ms;
-      if (cudaEventElapsedTime(&ms, ctx->evk[2], ctx->evk[3]) == cudaSuccess) ctx->acc_grid_ms += ms;
-    }
-    unperm = hRes[0];
-    take(hRes + 1, 0, cnt0);
-    std::vector<double> v(minp.begin(), minp.begin() + cnt0);
-    std::sort(v.begin(), v.end());
-    const double p90 = std::max(v[(size_t)(kLevel0Quantile * (double)(v.size() - 1))], 1e-300);
-    const double p99 = std::max(v[(size_t)(0.99 * (double)(v.size() - 1))], 1e-300);
-    const double pmax = std::max(v.back(), 1e-300);
-    const int sc = P->fshift;
-    const int t0 = fixed_log(p90, sc);
-    const int t1 = std::max(fixed_log(p99, sc), t0 + 1);
-    const int t2 = std::max((int)std::min(0.0, std::floor((std::log(pmax) + 1.0) * std::ldexp(1.0, sc))), t1 + 1);
-    rc = ensure_table(ctx, P, 0, t0);
-    if (rc) return rc;
-    rc = ensure_table(ctx, P, 1, t1);
-    if (rc) return rc;
-    rc = ensure_table(ctx, P, 2, t2);
-    if (rc) return rc;
-    const int nlev = 3;
-    // Two batches in flight: while batch b's later table levels, exhaustive
-    // fallback and result copy run on the side stream, batch b+1's labels and
-    // level-0 table sweep run on the main stream.
-    auto harvest = [&](BatchSlot& sl) -> int {
-      CK(cudaEventSynchronize(sl.ev[7]));
-      float ms = 0.f;
-      if (cudaEventElapsedTime(&ms, sl.ev[0], sl.ev[1]) == cudaSuccess) ctx->acc_perm_ms += ms;
-      if (cudaEventElapsedTime(&ms, sl.ev[2], sl.ev[6]) == cudaSuccess) ctx->acc_grid_ms += ms;
-      if (cudaEventElapsedTime(&ms, sl.ev[4], sl.ev[5]) == cudaSuccess) ctx->acc_grid_ms += ms;
-      take((const TaskResult*)sl.hRes, sl.b0, sl.cnt);
-      ctx->acc_d2h += (long long)sl.cnt * (long long)sizeof(TaskResult);
-      sl.busy = false;
-      return DTO_OK;
-    };
-    for (long long it = 0; it < npipe; ++it) {
-      BatchSlot& sl = ctx->slot[it & 1];
-      if (sl.busy) {
-        rc = harvest(sl);
-        if (rc) return rc;
-      }
-      if (!(it < 2 && drawn[it])) {
-        rc = draw(it);
-        if (rc) return rc;
-      }
-      const int cnt = sl.cnt;
-      int16_t* X = (int16_t*)sl.dX;
-      TaskResult* dR = (TaskResult*)sl.dRes;
-      CK(cudaEventRecord(sl.ev[2], ctx->stream));
-      rc = table_levels(ctx, P, X, xs, cnt, dR, 0, 1, (int*)sl.dFall, sl.dCnt, ctx->stream, 0);
-      if (rc) return rc;
-      CK(cudaEventRecord(sl.ev[6], ctx->stream));
-      CK(cudaStreamWaitEvent(ctx->side, sl.ev[6], 0));
-      CK(cudaEventRecord(sl.ev[4], ctx->side));
-      rc = table_levels(ctx, P, X, xs, cnt, dR, 1, nlev, (int*)sl.dFall, sl.dCnt, ctx->side, 1);
-      if (rc) return rc;
-      rc = table_exhaustive(ctx, P, X, xs, cnt, dR, nlev, (const int*)sl.dFall, sl.dCnt, ctx->side);
-      if (rc) return rc;
-      CK(cudaEventRecord(sl.ev[5], ctx->side));
-      CK(cudaMemcpyAsync(sl.hRes, dR, (size_t)cnt * sizeof(TaskResult), cudaMemcpyDeviceToHost, ctx->side));
-      CK(cudaEventRecord(sl.ev[7], ctx->side));
-      sl.busy = true;
-    }
-    for (BatchSlot& sl : ctx->slot) {
-      if (sl.busy) {
-        rc = harvest(sl);
-        if (rc) return rc;
-      }
-    }
-    // the main stream's timing event follows the side stream's last work
-    CK(cudaEventRecord(ctx->evSide, ctx->side));
-    CK(cudaStreamWaitEvent(ctx->stream, ctx->evSide, 0));
-  }
-  fill_result(P, unperm, 0, out_unpermuted);
-  const double p_obs = unperm.p;
-  long long count_le = 0;
-  for (long long q = 0; q < n_perm; ++q) count_le += (minp[(size_t)q] <= p_obs);
-  CK(cudaEventRecord(ctx->ev1, ctx->stream));
-  unsigned long long refined[3] = {0, 0, 0};
-  CK(cudaMemcpyAsync(refined, ctx->dRefined, sizeof(refined), cudaMemcpyDeviceToHost, ctx->stream));
-  CK(cudaStreamSynchronize(ctx->stream));
-  if (out_summary) {
-    float ms = 0.f;
-    cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
-    dto_summary& s = *out_summary;
-    s.n_perm = n_perm;
-    s.count_le = count_le;
-    s.empirical_pvalue = n_perm > 0 ? (double)count_le / (double)n_perm : 1.0;
-    s.fdr = dto_fdr(out_unpermuted->set1_len, out_unpermuted->set2_len, out_unpermuted->intersection_size,
-                    P->npop, 0.8);
-    s.logp_err_bound_screen = precision == DTO_PRECISION_SCREEN ? 4.5 * std::ldexp(1.0, -P->fshift) : 0.0;
-    s.logp_err_bound_fp64 = 2.0e-13;
-    s.n_fallback = (int64_t)refined[2];
-    s.n_refined = (int64_t)refined[0];
-    s.n_stage2 = (int64_t)refined[1];
-    s.device_ms = ms;
-    s.grid_ms = ctx->acc_grid_ms;
-    s.perm_ms = ctx->acc_perm_ms;
-    s.n_launches = ctx->acc_launches;
-    s.h2d_bytes = ctx->acc_h2d;
-    s.d2h_bytes = ctx->acc_d2h + 16;
-  }
-  return DTO_OK;
+  return lane_run_range(ctx->lane0, P, perm_first, n_perm, seed, perm_idx, precision, out_unpermuted, out_minp,
+                        out_perm, out_summary);
 }
 
 int dto_optimize(dto_ctx* ctx, dto_pair* P, int permute, uint64_t seed, uint32_t perm_id, const int32_t* idx1,
@@ -1034,11 +405,12 @@ int dto_optimize(dto_ctx* ctx, dto_pair* P, int permute, uint64_t seed, uint32_t
   if (precision != DTO_PRECISION_FP64 && precision != DTO_PRECISION_SCREEN)
     return set_err(ctx, DTO_ERR_INVALID, "unknown precision");
   std::lock_guard<std::mutex> g(ctx->mu);
+  Lane* L = ctx->lane0;
   CK(cudaSetDevice(ctx->device));
   const int mode = precision == DTO_PRECISION_FP64 ? kModeFull64 : kModeScreen;
-  int rc = grow(ctx, &ctx->dRes, &ctx->resBytes, 2 * sizeof(TaskResult));
+  int rc = lane_grow(L, &L->dRes, &L->resBytes, 2 * sizeof(TaskResult));
   if (rc) return rc;
-  rc = grow_host(ctx, &ctx->hRes, &ctx->hResBytes, 2 * sizeof(TaskResult));
+  rc = lane_grow_host(L, &L->hRes, &L->hResBytes, 2 * sizeof(TaskResult));
   if (rc) return rc;
   const int16_t* dX = P->dYlab;
   void* dIdx = nullptr;
@@ -1049,28 +421,29 @@ int dto_optimize(dto_ctx* ctx, dto_pair* P, int permute, uint64_t seed, uint32_t
       if (!check_perm(idx1, P->N1) || !check_perm(idx2, P->N2))
         return set_err(ctx, DTO_ERR_INVALID, "index array is not a permutation");
       CK(cudaMalloc(&dIdx, (size_t)(P->N1 + P->N2) * 4));
-      CK(cudaMemcpyAsync(dIdx, idx1, (size_t)P->N1 * 4, cudaMemcpyHostToDevice, ctx->stream));
-      CK(cudaMemcpyAsync((int32_t*)dIdx + P->N1, idx2, (size_t)P->N2 * 4, cudaMemcpyHostToDevice, ctx->stream));
+      CK(cudaMemcpyAsync(dIdx, idx1, (size_t)P->N1 * 4, cudaMemcpyHostToDevice, L->stream));
+      CK(cudaMemcpyAsync((int32_t*)dIdx + P->N1, idx2, (size_t)P->N2 * 4, cudaMemcpyHostToDevice, L->stream));
       dI = (const int32_t*)dIdx;
     }
-    rc = make_labels(ctx, P, seed, perm_id, 1, dI);
+    rc = lane_make_labels(L, P, seed, perm_id, 1, dI);
     if (rc) return rc;
-    dX = (const int16_t*)ctx->dX;
+    dX = (const int16_t*)L->dX;
   }
-  rc = grid_tasks(ctx, P, dX, xstride_of(P->N1), 1, mode, (TaskResult*)ctx->dRes);
+  rc = lane_grid_tasks(L, P, dX, xstride_of(P->N1), 1, mode, (TaskResult*)L->dRes);
   if (rc) return rc;
-  CK(cudaMemcpyAsync(ctx->hRes, ctx->dRes, sizeof(TaskResult), cudaMemcpyDeviceToHost, ctx->stream));
-  CK(cudaStreamSynchronize(ctx->stream));
-  fill_result(P, ((TaskResult*)ctx->hRes)[0], permute ? 1 : 0, out);
+  CK(cudaMemcpyAsync(L->hRes, L->dRes, sizeof(TaskResult), cudaMemcpyDeviceToHost, L->stream));
+  CK(cudaStreamSynchronize(L->stream));
+  fill_result(P, ((TaskResult*)L->hRes)[0], permute ? 1 : 0, out);
   return DTO_OK;
 }
 
 int dto_grid_dump(dto_ctx* ctx, dto_pair* P, const int32_t* idx1, const int32_t* idx2, dto_result* records) {
   if (!ctx || !P || P->ctx != ctx || !records) return set_err(ctx, DTO_ERR_INVALID, "null argument");
   std::lock_guard<std::mutex> g(ctx->mu);
+  Lane* L = ctx->lane0;
   CK(cudaSetDevice(ctx->device));
   const long long ncell = (long long)P->T1.size() * (long long)P->T2.size();
-  int rc = grow(ctx, &ctx->dRes, &ctx->resBytes, 2 * sizeof(TaskResult));
+  int rc = lane_grow(L, &L->dRes, &L->resBytes, 2 * sizeof(TaskResult));
   if (rc) return rc;
   void* dK = nullptr;
   void* dP = nullptr;
@@ -1083,19 +456,19 @@ int dto_grid_dump(dto_ctx* ctx, dto_pair* P, const int32_t* idx1, const int32_t*
     if (!check_perm(idx1, P->N1) || !check_perm(idx2, P->N2))
       return set_err(ctx, DTO_ERR_INVALID, "index array is not a permutation");
     CK(cudaMalloc(&dIdx, (size_t)(P->N1 + P->N2) * 4));
-    CK(cudaMemcpyAsync(dIdx, idx1, (size_t)P->N1 * 4, cudaMemcpyHostToDevice, ctx->stream));
-    CK(cudaMemcpyAsync((int32_t*)dIdx + P->N1, idx2, (size_t)P->N2 * 4, cudaMemcpyHostToDevice, ctx->stream));
-    rc = make_labels(ctx, P, 0, 0, 1, (const int32_t*)dIdx);
+    CK(cudaMemcpyAsync(dIdx, idx1, (size_t)P->N1 * 4, cudaMemcpyHostToDevice, L->stream));
+    CK(cudaMemcpyAsync((int32_t*)dIdx + P->N1, idx2, (size_t)P->N2 * 4, cudaMemcpyHostToDevice, L->stream));
+    rc = lane_make_labels(L, P, 0, 0, 1, (const int32_t*)dIdx);
     if (rc) return rc;
-    dX = (const int16_t*)ctx->dX;
+    dX = (const int16_t*)L->dX;
   }
-  rc = grid_tasks(ctx, P, dX, xstride_of(P->N1), 1, kModeDump, (TaskResult*)ctx->dRes, (int*)dK, (double*)dP);
+  rc = lane_grid_tasks(L, P, dX, xstride_of(P->N1), 1, kModeDump, (TaskResult*)L->dRes, (int*)dK, (double*)dP);
   if (rc) return rc;
   std::vector<int> hk((size_t)ncell);
   std::vector<double> hp((size_t)ncell);
-  CK(cudaMemcpyAsync(hk.data(), dK, (size_t)ncell * 4, cudaMemcpyDeviceToHost, ctx->stream));
-  CK(cudaMemcpyAsync(hp.data(), dP, (size_t)ncell * 8, cudaMemcpyDeviceToHost, ctx->stream));
-  CK(cudaStreamSynchronize(ctx->stream));
+  CK(cudaMemcpyAsync(hk.data(), dK, (size_t)ncell * 4, cudaMemcpyDeviceToHost, L->stream));
+  CK(cudaMemcpyAsync(hp.data(), dP, (size_t)ncell * 8, cudaMemcpyDeviceToHost, L->stream));
+  CK(cudaStreamSynchronize(L->stream));
   const int permuted = (idx1 && idx2) ? 1 : 0;
   const long long nt2 = (long long)P->T2.size();
   for (long long c = 0; c < ncell; ++c) {
@@ -1110,6 +483,7 @@ int dto_hypergeom_sf(dto_ctx* ctx, const int64_t* N, const int64_t* K, const int
   if (!ctx || count < 0 || (count > 0 && (!N || !K || !n || !k || !out))) return set_err(ctx, DTO_ERR_INVALID, "null argument");
   if (count == 0) return DTO_OK;
   std::lock_guard<std::mutex> g(ctx->mu);
+  Lane* L = ctx->lane0;
   long long nmax = 0;
   std::vector<long long> q((size_t)count * 4);
   for (int64_t t = 0; t < count; ++t) {
@@ -1129,10 +503,10 @@ int dto_hypergeom_sf(dto_ctx* ctx, const int64_t* N, const int64_t* K, const int
   struct Guard2 { void*& a; void*& b; ~Guard2() { if (a) cudaFree(a); if (b) cudaFree(b); } } guard{dq, dout};
   CK(cudaMalloc(&dq, q.size() * 8));
   CK(cudaMalloc(&dout, (size_t)count * 8));
-  CK(cudaMemcpyAsync(dq, q.data(), q.size() * 8, cudaMemcpyHostToDevice, ctx->stream));
-  CK(launch_sf_batch(ctx->dLF, (const long long*)dq, (double*)dout, count, ctx->stream));
-  CK(cudaMemcpyAsync(out, dout, (size_t)count * 8, cudaMemcpyDeviceToHost, ctx->stream));
-  CK(cudaStreamSynchronize(ctx->stream));
+  CK(cudaMemcpyAsync(dq, q.data(), q.size() * 8, cudaMemcpyHostToDevice, L->stream));
+  CK(launch_sf_batch(ctx->dLF.load(), (const long long*)dq, (double*)dout, count, L->stream));
+  CK(cudaMemcpyAsync(out, dout, (size_t)count * 8, cudaMemcpyDeviceToHost, L->stream));
+  CK(cudaStreamSynchronize(L->stream));
   return DTO_OK;
 }
 
@@ -1142,10 +516,11 @@ int dto_export_permutations(dto_ctx* ctx, dto_pair* P, uint64_t seed, uint32_t p
     return set_err(ctx, DTO_ERR_INVALID, "null argument");
   if (count == 0) return DTO_OK;
   std::lock_guard<std::mutex> g(ctx->mu);
+  Lane* L = ctx->lane0;
   CK(cudaSetDevice(ctx->device));
-  int rc = grow(ctx, &ctx->dSig, &ctx->sigBytes, (size_t)count * (P->N1 + P->N2) * 4);
+  int rc = lane_grow(L, &L->dSig, &L->sigBytes, (size_t)count * (P->N1 + P->N2) * 4);
   if (rc) return rc;
-  int* sig = (int*)ctx->dSig;
+  int* sig = (int*)L->dSig;
   PermArgs a{};
   a.seed = seed;
   a.pair_id = P->pair_id;
@@ -1154,18 +529,18 @@ int dto_export_permutations(dto_ctx* ctx, dto_pair* P, uint64_t seed, uint32_t p
   a.list_tag = 1;
   a.sigma = sig;
   a.sstride = P->N1;
-  CK(launch_perm(a, (int)count, ctx->stream));
+  CK(launch_perm(a, (int)count, L->stream));
   if (!P->same_set) {
     a.L = (int)P->N2;
     a.list_tag = 2;
     a.sigma = sig + count * P->N1;
     a.sstride = P->N2;
-    CK(launch_perm(a, (int)count, ctx->stream));
+    CK(launch_perm(a, (int)count, L->stream));
   }
-  CK(cudaMemcpyAsync(idx1, sig, (size_t)count * P->N1 * 4, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaMemcpyAsync(idx1, sig, (size_t)count * P->N1 * 4, cudaMemcpyDeviceToHost, L->stream));
   if (!P->same_set)
-    CK(cudaMemcpyAsync(idx2, sig + count * P->N1, (size_t)count * P->N2 * 4, cudaMemcpyDeviceToHost, ctx->stream));
-  CK(cudaStreamSynchronize(ctx->stream));
+    CK(cudaMemcpyAsync(idx2, sig + count * P->N1, (size_t)count * P->N2 * 4, cudaMemcpyDeviceToHost, L->stream));
+  CK(cudaStreamSynchronize(L->stream));
   if (P->same_set)
     for (int64_t b = 0; b < count; ++b)
       for (int64_t p = 0; p < P->N2; ++p) idx2[b * P->N2 + p] = (int32_t)p;
@@ -1179,6 +554,7 @@ int dto_run_range_noalloc(dto_ctx* ctx, dto_pair* P, uint32_t perm_first, int64_
   if ((long long)perm_first + n_perm > 0xffffffffLL)
     return set_err(ctx, DTO_ERR_INVALID, "dto_run_range_noalloc: permutation ids out of range");
   std::lock_guard<std::mutex> g(ctx->mu);
+  Lane* L = ctx->lane0;
   CK(cudaSetDevice(ctx->device));
   void* base = nullptr;
   size_t cap = 0;
@@ -1216,18 +592,18 @@ int dto_run_range_noalloc(dto_ctx* ctx, dto_pair* P, uint32_t perm_first, int64_
     a.list_tag = 1;
     a.Ylab = P->dYlab;
     a.X = X;
-    CK(launch_perm(a, cnt, ctx->stream));
+    CK(launch_perm(a, cnt, L->stream));
   } else {
     const long long ss = P->N1 + P->N2;
     a.L = (int)P->N1;
     a.list_tag = 1;
     a.sigma = sig;
     a.sstride = ss;
-    CK(launch_perm(a, cnt, ctx->stream));
+    CK(launch_perm(a, cnt, L->stream));
     a.L = (int)P->N2;
     a.list_tag = 2;
     a.sigma = sig + P->N1;
-    CK(launch_perm(a, cnt, ctx->stream));
+    CK(launch_perm(a, cnt, L->stream));
     ComposeArgs c{};
     c.N1 = (int)P->N1;
     c.N2 = (int)P->N2;
@@ -1238,12 +614,12 @@ int dto_run_range_noalloc(dto_ctx* ctx, dto_pair* P, uint32_t perm_first, int64_
     c.lab2 = P->dLab2;
     c.X = X;
     c.xstride = xs;
-    CK(launch_compose(c, cnt, ctx->stream));
+    CK(launch_compose(c, cnt, L->stream));
   }
-  CK(cudaMemsetAsync(work, 0, 256, ctx->stream));  // the shared task counter starts at zero
+  CK(cudaMemsetAsync(work, 0, 256, L->stream));  // the shared task counter starts at zero
   GridArgs gk{};
   gk.P = P->dev;
-  gk.P.LF = ctx->dLF;
+  gk.P.LF = ctx->dLF.load();
   gk.X = X;
   gk.xstride = xs;
   gk.ntask = cnt;
@@ -1252,8 +628,8 @@ int dto_run_range_noalloc(dto_ctx* ctx, dto_pair* P, uint32_t perm_first, int64_
   gk.out = res;
   gk.work = work;
   const int ctas = std::max(1, std::min(ctx->nsm, (cnt + kGridWarps - 1) / kGridWarps));
-  CK(launch_grid(gk, ctas, ctx->stream));
-  CK(launch_noalloc_copy_p(res, d_minp, cnt, ctx->stream));
+  CK(launch_grid(gk, ctas, L->stream));
+  CK(launch_noalloc_copy_p(res, d_minp, cnt, L->stream));
   return DTO_OK;
 }
 

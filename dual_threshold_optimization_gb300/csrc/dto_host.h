@@ -1,0 +1,167 @@
+// dto_host.h -- host-side state of libdto.so shared by the C ABI
+// (dto_capi.cpp), the permutation-null driver (dto_lane.cpp) and the
+// request executor (dto_serve.cpp).
+//
+// A context owns the device, the shared log-factorial table and one default
+// lane.  A lane is everything one run of the permutation null needs while it
+// is in flight: two streams, events, scratch buffers and the table screens of
+// the pair it last ran.  dto_run and the other context-level calls use the
+// default lane under the context's mutex; an executor owns further lanes and
+// runs one request on each at a time, so that requests overlap on the device.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <atomic>
+#include <cstdint>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/dto.h"
+#include "dto_internal.h"
+
+namespace dto {
+
+// Buffers of one in-flight batch of the table-screen pipeline.
+struct BatchSlot {
+  void* dX = nullptr;
+  size_t xBytes = 0;
+  void* dRes = nullptr;
+  size_t resBytes = 0;
+  void* hRes = nullptr;  // pinned
+  size_t hResBytes = 0;
+  void* dFall = nullptr;
+  size_t fallBytes = 0;
+  void* dIdx = nullptr;
+  size_t idxBytes = 0;
+  int* dCnt = nullptr;  // [0, 8): task counters, [8, 12): fallback counts
+  cudaEvent_t ev[8] = {};  // perm start/end, tables start, -, exhaustive start/end, tables done, batch done
+  bool busy = false;
+  long long b0 = 0;
+  int cnt = 0;
+};
+
+struct Lane {
+  dto_ctx* ctx = nullptr;
+  std::string* err = nullptr;  // where this lane's error messages go
+  std::string own_err;
+  cudaStream_t stream = nullptr;
+  cudaStream_t side = nullptr;  // first batch, later table levels and fallbacks
+  cudaEvent_t evSide = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  cudaEvent_t evk[4] = {nullptr, nullptr, nullptr, nullptr};  // perm start/end, grid start/end
+  // per-run accounting
+  double acc_grid_ms = 0.0, acc_perm_ms = 0.0;
+  long long acc_launches = 0, acc_h2d = 0, acc_d2h = 0;
+  // scratch, grown on demand
+  void* dX = nullptr;
+  size_t xBytes = 0;
+  void* dSig = nullptr;
+  size_t sigBytes = 0;
+  void* dRes = nullptr;
+  size_t resBytes = 0;
+  void* hRes = nullptr;  // pinned
+  size_t hResBytes = 0;
+  int* dWork = nullptr;
+  unsigned long long* dRefined = nullptr;
+  unsigned* dGuess = nullptr;  // bound histogram shared by the batches of one run
+  void* dHits[2] = {nullptr, nullptr};  // per-warp hit buffers of the table screen, one per stream
+  size_t hitBytes[2] = {0, 0};
+  BatchSlot slot[2];  // double-buffered batches of the table-screen pipeline
+  // table screens (the ladder) of the pair this lane last ran
+  uint16_t* dKthr[3] = {nullptr, nullptr, nullptr};
+  size_t kthrBytes[3] = {0, 0, 0};
+  unsigned long long kthr_pair[3] = {0, 0, 0};  // pair serial the table was built for (0: none)
+  int kthr_tau[3] = {0, 0, 0};
+};
+
+}  // namespace dto
+
+struct dto_ctx {
+  int device = 0;
+  int nsm = 0;
+  size_t smem_optin = 0;
+  std::string err;
+  std::mutex mu;       // serialises the context-level calls (default lane, pair creation)
+  std::mutex lf_mu;    // guards the log-factorial table
+  // ln(m!) as double-double, m = 0..lf_cap; a grown table replaces the old
+  // one, which stays allocated until the context is destroyed (kernels of
+  // other lanes may still read it)
+  long long lf_cap = -1;
+  std::vector<double> lf_hi, lf_lo;
+  std::atomic<double2*> dLF{nullptr};
+  std::vector<double2*> lf_old;
+  std::atomic<unsigned long long> next_serial{1};
+  dto::Lane* lane0 = nullptr;
+};
+
+struct dto_pair {
+  dto_ctx* ctx = nullptr;
+  unsigned long long serial = 0;  // unique per context: keys the lanes' table caches
+  uint32_t pair_id = 0;
+  long long N1 = 0, N2 = 0, npop = 0, nfeat = 0, ncommon = 0;
+  bool same_set = false;
+  std::vector<uint32_t> r1, r2, T1, T2;
+  std::vector<int32_t> order1, order2, f1, f2;
+  std::vector<int> c1, c2, map12;
+  std::vector<int16_t> lab2, ylab;
+  int C = 0, fshift = 0;
+  long long upload_bytes = 0;  // host-to-device bytes of dto_pair_create
+  // device
+  int* dRow = nullptr;
+  int* dNcnt = nullptr;
+  uint32_t* dF = nullptr;
+  int16_t* dYlab = nullptr;
+  int16_t* dLab2 = nullptr;
+  int* dMap12 = nullptr;
+  dto::PairDev dev{};
+};
+
+namespace dto {
+
+int set_err(dto_ctx* ctx, int code, const std::string& msg);
+int cuda_err(dto_ctx* ctx, cudaError_t e, const char* what);
+int lane_err(Lane* L, int code, const std::string& msg);
+int lane_cuda_err(Lane* L, cudaError_t e, const char* what);
+
+#define CK(call)                                                \
+  do {                                                          \
+    cudaError_t e_ = (call);                                    \
+    if (e_ != cudaSuccess) return dto::cuda_err(ctx, e_, #call); \
+  } while (0)
+
+#define LCK(call)                                                 \
+  do {                                                            \
+    cudaError_t e_ = (call);                                      \
+    if (e_ != cudaSuccess) return dto::lane_cuda_err(L, e_, #call); \
+  } while (0)
+
+int lane_create(dto_ctx* ctx, Lane** out, std::string* err_sink);
+void lane_destroy(Lane* L);
+int lane_grow(Lane* L, void** p, size_t* cap, size_t need);
+int lane_grow_host(Lane* L, void** p, size_t* cap, size_t need);
+
+long long xstride_of(long long N1);
+int check_perm(const int32_t* idx, long long L);
+void fill_result(const dto_pair* P, const TaskResult& r, int permuted, dto_result* o);
+
+// One task per launch through the exhaustive screen (or FP64 / dump modes).
+int lane_grid_tasks(Lane* L, dto_pair* P, const int16_t* dX, long long xstride, int ntask, int mode,
+                    TaskResult* dOut, int* dumpK = nullptr, double* dumpP = nullptr, bool guess = false,
+                    cudaStream_t stream = nullptr);
+// Labels of `count` permutations from perm id `first` (or of uploaded index
+// rows dIdx) into L->dX from row `row0`.
+int lane_make_labels(Lane* L, dto_pair* P, uint64_t seed, uint32_t first, int count, const int32_t* dIdx,
+                     int row0 = 0);
+
+// The permutation null of one pair on one lane (dto_run_range's semantics).
+// `minp` receives every permutation's minimum p (n_perm entries).
+int lane_run_range(Lane* L, dto_pair* P, uint32_t perm_first, int64_t n_perm, uint64_t seed,
+                   const int32_t* perm_idx, int precision, dto_result* out_unpermuted, double* out_minp,
+                   dto_result* out_perm, dto_summary* out_summary);
+
+// Bytes of device scratch a run of the pair holds at its peak (labels of the
+// batches in flight, results, hit buffers, table screens).
+long long run_device_bytes(const dto_ctx* ctx, const dto_pair* P, int64_t n_perm, bool test_mode);
+
+}  // namespace dto

@@ -1,0 +1,636 @@
+// dto_lane.cpp -- the permutation-null driver: one run of dto_run_range on
+// one lane (streams, events, scratch and table screens of its own).
+//
+// A run replaces run_single_node (src/run/single_node.rs:83-137) over the
+// tasks of src/main.rs:122-126: task 0 is the unpermuted pair, tasks 1..P the
+// permutations, each reduced to its minimum p (src/dto/optimize_main.rs:53-118),
+// and the empirical p-value is #{perm p <= observed p} / P
+// (src/stat_operations/empirical_pvalue.rs:109-187).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "dto_host.h"
+
+namespace dto {
+
+// Quantile of the first batch's minimum p-values that sets the level-0 table.
+#ifndef DTO_L0_QUANTILE
+#define DTO_L0_QUANTILE 0.90
+#endif
+constexpr double kLevel0Quantile = DTO_L0_QUANTILE;
+
+int set_err(dto_ctx* ctx, int code, const std::string& msg) {
+  if (ctx) ctx->err = msg;
+  return code;
+}
+
+int cuda_err(dto_ctx* ctx, cudaError_t e, const char* what) {
+  std::string m = std::string(what) + ": " + cudaGetErrorString(e);
+  return set_err(ctx, e == cudaErrorMemoryAllocation ? DTO_ERR_OOM : DTO_ERR_CUDA, m);
+}
+
+int lane_err(Lane* L, int code, const std::string& msg) {
+  if (L && L->err) *L->err = msg;
+  return code;
+}
+
+int lane_cuda_err(Lane* L, cudaError_t e, const char* what) {
+  std::string m = std::string(what) + ": " + cudaGetErrorString(e);
+  return lane_err(L, e == cudaErrorMemoryAllocation ? DTO_ERR_OOM : DTO_ERR_CUDA, m);
+}
+
+int lane_grow(Lane* L, void** p, size_t* cap, size_t need) {
+  if (need <= *cap) return DTO_OK;
+  if (*p) cudaFree(*p);
+  *p = nullptr;
+  *cap = 0;
+  size_t sz = std::max(need, (size_t)4096);
+  LCK(cudaMalloc(p, sz));
+  *cap = sz;
+  return DTO_OK;
+}
+
+int lane_grow_host(Lane* L, void** p, size_t* cap, size_t need) {
+  if (need <= *cap) return DTO_OK;
+  if (*p) cudaFreeHost(*p);
+  *p = nullptr;
+  *cap = 0;
+  size_t sz = std::max(need, (size_t)4096);
+  LCK(cudaMallocHost(p, sz));
+  *cap = sz;
+  return DTO_OK;
+}
+
+int lane_create(dto_ctx* ctx, Lane** out, std::string* err_sink) {
+  *out = nullptr;
+  Lane* L = new Lane();
+  L->ctx = ctx;
+  L->err = err_sink ? err_sink : &L->own_err;
+  auto fail = [&](cudaError_t e, const char* what) {
+    const int rc = lane_cuda_err(L, e, what);
+    if (!err_sink && ctx) ctx->err = L->own_err;
+    lane_destroy(L);
+    return rc;
+  };
+  cudaError_t e;
+  if ((e = cudaStreamCreateWithFlags(&L->stream, cudaStreamNonBlocking)) != cudaSuccess) return fail(e, "stream");
+  if ((e = cudaStreamCreateWithFlags(&L->side, cudaStreamNonBlocking)) != cudaSuccess) return fail(e, "stream");
+  if ((e = cudaEventCreateWithFlags(&L->evSide, cudaEventDisableTiming)) != cudaSuccess) return fail(e, "event");
+  if ((e = cudaEventCreate(&L->ev0)) != cudaSuccess) return fail(e, "event");
+  if ((e = cudaEventCreate(&L->ev1)) != cudaSuccess) return fail(e, "event");
+  for (int q = 0; q < 4; ++q)
+    if ((e = cudaEventCreate(&L->evk[q])) != cudaSuccess) return fail(e, "event");
+  if ((e = cudaMalloc(&L->dWork, 256)) != cudaSuccess) return fail(e, "scratch");
+  if ((e = cudaMalloc(&L->dRefined, 256)) != cudaSuccess) return fail(e, "scratch");
+  if ((e = cudaMalloc(&L->dGuess, 2048)) != cudaSuccess) return fail(e, "scratch");
+  *out = L;
+  return DTO_OK;
+}
+
+void lane_destroy(Lane* L) {
+  if (!L) return;
+  if (L->stream) cudaStreamSynchronize(L->stream);
+  if (L->side) cudaStreamSynchronize(L->side);
+  cudaFree(L->dX);
+  cudaFree(L->dSig);
+  cudaFree(L->dRes);
+  cudaFreeHost(L->hRes);
+  cudaFree(L->dWork);
+  cudaFree(L->dRefined);
+  cudaFree(L->dGuess);
+  cudaFree(L->dHits[0]);
+  cudaFree(L->dHits[1]);
+  for (int l = 0; l < 3; ++l) cudaFree(L->dKthr[l]);
+  for (BatchSlot& sl : L->slot) {
+    cudaFree(sl.dX);
+    cudaFree(sl.dRes);
+    cudaFreeHost(sl.hRes);
+    cudaFree(sl.dFall);
+    cudaFree(sl.dIdx);
+    cudaFree(sl.dCnt);
+    for (cudaEvent_t e : sl.ev)
+      if (e) cudaEventDestroy(e);
+  }
+  if (L->ev0) cudaEventDestroy(L->ev0);
+  if (L->ev1) cudaEventDestroy(L->ev1);
+  for (int q = 0; q < 4; ++q)
+    if (L->evk[q]) cudaEventDestroy(L->evk[q]);
+  if (L->evSide) cudaEventDestroy(L->evSide);
+  if (L->side) cudaStreamDestroy(L->side);
+  if (L->stream) cudaStreamDestroy(L->stream);
+  delete L;
+}
+
+// Rows of the grid kernel need 16-byte aligned starts for vector loads.
+long long xstride_of(long long N1) { return (N1 + 7) & ~7LL; }
+
+int check_perm(const int32_t* idx, long long L) {
+  std::vector<char> seen((size_t)L, 0);
+  for (long long p = 0; p < L; ++p) {
+    int32_t v = idx[p];
+    if (v < 0 || v >= L || seen[(size_t)v]) return 0;
+    seen[(size_t)v] = 1;
+  }
+  return 1;
+}
+
+void fill_result(const dto_pair* P, const TaskResult& r, int permuted, dto_result* o) {
+  o->rank1 = P->T1[(size_t)r.i];
+  o->rank2 = P->T2[(size_t)r.j];
+  o->set1_len = P->c1[(size_t)r.i];
+  o->set2_len = P->c2[(size_t)r.j];
+  o->population_size = P->npop;
+  o->intersection_size = r.k;
+  o->pvalue = r.p;
+  o->permuted = permuted;
+  o->i = r.i;
+  o->j = r.j;
+  o->status = r.status;
+}
+
+// Batch size of a run: bounded by 1 GiB of labels (and of index scratch for
+// test mode and for pairs whose lists hold different features).
+long long batch_of(const dto_pair* P, int64_t n_perm, bool test_mode) {
+  const long long xs = xstride_of(P->N1);
+  const long long L12 = P->N1 + P->N2;
+  long long batch = std::max(1LL, std::min<long long>((1LL << 30) / (xs * 2), 1LL << 20));
+  if (test_mode || !P->same_set) batch = std::min(batch, std::max(1LL, (1LL << 30) / (L12 * 4)));
+  return std::min<long long>(batch, std::max<long long>(n_perm, 1));
+}
+
+long long run_device_bytes(const dto_ctx* ctx, const dto_pair* P, int64_t n_perm, bool test_mode) {
+  const long long xs = xstride_of(P->N1);
+  const long long L12 = P->N1 + P->N2;
+  const long long batch = batch_of(P, n_perm, test_mode);
+  const long long first = std::min<long long>(batch, 1025);
+  long long b = first * xs * 2 + (long long)(batch + 1) * (long long)sizeof(TaskResult);  // first batch
+  if (n_perm > 2048) {
+    b += 2 * batch * (xs * 2 + (long long)sizeof(TaskResult) + 12);                          // two slots
+    b += 2LL * kTableCtasPerSm * ctx->nsm * kTableWarps * 8192 * 8;                           // hit buffers
+    b += 3LL * (long long)table_entries(P->C, P->dev.n1) * 2;                                 // table ladder
+  }
+  if (test_mode || !P->same_set) b += 2 * batch * L12 * 4;  // index scratch
+  return b;
+}
+
+int lane_grid_tasks(Lane* L, dto_pair* P, const int16_t* dX, long long xstride, int ntask, int mode,
+                    TaskResult* dOut, int* dumpK, double* dumpP, bool guess, cudaStream_t stream) {
+  if (!stream) stream = L->stream;
+  GridArgs a{};
+  a.P = P->dev;
+  a.P.LF = L->ctx->dLF.load();  // the context's table may have grown since the pair was created
+  a.X = dX;
+  a.xstride = xstride;
+  a.ntask = ntask;
+  a.mode = mode;
+  size_t smemF = grid_smem_bytes(P->C, P->dev.n1, P->npop, 1);
+  a.smemF = smemF <= L->ctx->smem_optin ? 1 : 0;
+  a.out = dOut;
+  a.work = L->dWork;
+  a.n_refined = L->dRefined;
+  a.guess_hist = (guess && mode == kModeScreen) ? L->dGuess : nullptr;
+  a.dump_k = dumpK;
+  a.dump_p = dumpP;
+  LCK(cudaMemsetAsync(L->dWork, 0, sizeof(int), stream));
+  int ctas = std::min(L->ctx->nsm, (ntask + kGridWarps - 1) / kGridWarps);
+  ctas = std::max(ctas, 1);
+  LCK(cudaEventRecord(L->evk[2], stream));
+  LCK(launch_grid(a, ctas, stream));
+  LCK(cudaEventRecord(L->evk[3], stream));
+  L->acc_launches += 1;
+  return DTO_OK;
+}
+
+// Table screen `level` for bound tau (fixed-point ln p), built on the device
+// into the lane's buffer (kept while the lane runs the same pair and bound).
+int ensure_table(Lane* L, dto_pair* P, int level, int tau) {
+  if (L->kthr_pair[level] == P->serial && L->kthr_tau[level] == tau) return DTO_OK;
+  int rc = lane_grow(L, (void**)&L->dKthr[level], &L->kthrBytes[level], table_entries(P->C, P->dev.n1) * 2);
+  if (rc) return rc;
+  TableArgs t{};
+  t.n1 = P->dev.n1;
+  t.n2 = P->dev.n2;
+  t.N = (int)P->npop;
+  t.C = P->C;
+  t.rowstart = P->dRow;
+  t.ncnt = P->dNcnt;
+  t.F = P->dF;
+  t.fshift = P->fshift;
+  t.tau = tau;
+  t.packed = P->ncommon <= kPackedMaxCommon ? 1 : 0;
+  t.kthr = L->dKthr[level];
+  LCK(launch_table_build(t, L->ctx->nsm, L->stream));
+  L->acc_launches += 1;
+  L->kthr_pair[level] = P->serial;
+  L->kthr_tau[level] = tau;
+  return DTO_OK;
+}
+
+// Tasks [0, ntask) of X through the table ladder: level l takes the tasks
+// that level l-1 could not settle (their minimum lies above its bound), and
+// the exhaustive screen takes what the last level leaves.  The lists and
+// their counts stay on the device.  `fall` holds nlev lists of cap entries,
+// `cnts` 8 task counters then 4 list counts.  The levels run on the context's
+// stream; the exhaustive screen runs on `xstream` after `evTab` (which may be
+// the same stream).
+int table_levels(Lane* L, dto_pair* P, const int16_t* X, long long xstride, int ntask, TaskResult* dOut,
+                 int lev_begin, int lev_end, int* fall, int* cnts, cudaStream_t stream, int hb) {
+  const int cap = std::max(ntask, 1);
+  const int hitcap = 8192;
+  int rc = lane_grow(L, &L->dHits[hb], &L->hitBytes[hb], (size_t)kTableCtasPerSm * L->ctx->nsm * kTableWarps * hitcap * 8);
+  if (rc) return rc;
+  if (lev_begin == 0) LCK(cudaMemsetAsync(cnts, 0, 12 * sizeof(int), stream));
+  for (int level = lev_begin; level < lev_end; ++level) {
+    TableGridArgs a{};
+    a.P = P->dev;
+    a.P.LF = L->ctx->dLF.load();
+    a.X = X;
+    a.xstride = xstride;
+    a.ntask = ntask;
+    a.tau = L->kthr_tau[level];
+    a.kthr = L->dKthr[level];
+    a.packed = P->ncommon <= kPackedMaxCommon ? 1 : 0;
+    a.out = dOut;
+    a.work = cnts + level;
+    a.n_refined = L->dRefined;
+    a.fallback = fall + (size_t)level * cap;
+    a.nfallback = cnts + 8 + level;
+    a.task_list = level == 0 ? nullptr : fall + (size_t)(level - 1) * cap;
+    a.ntask_dev = level == 0 ? nullptr : cnts + 8 + level - 1;
+    a.hitbuf = (int2*)L->dHits[hb];
+    a.hitcap = hitcap;
+    // a later level sees the tasks the earlier ones left (about 10 % and 1 %
+    // of the batch); one warp per expected task keeps its latency to one sweep
+    const double expect = level == 0 ? 1.0 : level == 1 ? 0.15 : 0.03;
+    const int want = (int)(expect * (double)ntask / kTableWarps) + 1;
+    const int ctas = std::max(1, std::min(kTableCtasPerSm * L->ctx->nsm, want));
+    LCK(launch_table_grid(a, P->C, ctas, stream));
+  }
+  L->acc_launches += lev_end - lev_begin;
+  return DTO_OK;
+}
+
+// The exhaustive screen of what the last table level left, on `stream`.
+int table_exhaustive(Lane* L, dto_pair* P, const int16_t* X, long long xstride, int ntask, TaskResult* dOut,
+                     int nlev, const int* fall, int* cnts, cudaStream_t stream) {
+  const int cap = std::max(ntask, 1);
+  GridArgs g{};
+  g.P = P->dev;
+  g.P.LF = L->ctx->dLF.load();
+  g.X = X;
+  g.xstride = xstride;
+  g.ntask = ntask;
+  g.mode = kModeScreen;
+  g.smemF = grid_smem_bytes(P->C, P->dev.n1, P->npop, 1) <= L->ctx->smem_optin ? 1 : 0;
+  g.out = dOut;
+  g.work = cnts + nlev;
+  g.n_refined = L->dRefined;
+  g.task_list = fall + (size_t)(nlev - 1) * cap;
+  g.ntask_dev = cnts + 8 + nlev - 1;
+  LCK(launch_grid(g, L->ctx->nsm, stream));
+  L->acc_launches += 1;
+  return DTO_OK;
+}
+
+int fixed_log(double p, int fshift) {
+  double t = std::floor(std::log(p) * std::ldexp(1.0, fshift));
+  return (int)std::max(-2.0e9, std::min(0.0, t));
+}
+
+// Labels of n_perm permutations starting at perm id `first` into L->dX.
+int make_labels_launch(Lane* L, dto_pair* P, uint64_t seed, uint32_t first, int count,
+                       const int32_t* dIdx, int16_t* X, long long xs);
+
+int lane_make_labels(Lane* L, dto_pair* P, uint64_t seed, uint32_t first, int count,
+                     const int32_t* dIdx /* nullable: test mode, [count][N1+N2] */, int row0) {
+  long long xs = xstride_of(P->N1);
+  int rc = lane_grow(L, &L->dX, &L->xBytes, (size_t)(count + row0) * xs * 2);
+  if (rc) return rc;
+  int16_t* X = (int16_t*)L->dX + (size_t)row0 * xs;
+  LCK(cudaEventRecord(L->evk[0], L->stream));
+  rc = make_labels_launch(L, P, seed, first, count, dIdx, X, xs);
+  LCK(cudaEventRecord(L->evk[1], L->stream));
+  return rc;
+}
+
+int make_labels_launch(Lane* L, dto_pair* P, uint64_t seed, uint32_t first, int count,
+                       const int32_t* dIdx, int16_t* X, long long xs) {
+  int rc = DTO_OK;
+  if (dIdx) {
+    ComposeArgs c{};
+    c.N1 = (int)P->N1;
+    c.N2 = (int)P->N2;
+    c.idx1 = dIdx;
+    c.idx2 = dIdx + P->N1;
+    c.stride = P->N1 + P->N2;
+    c.map12 = P->dMap12;
+    c.lab2 = P->dLab2;
+    c.X = X;
+    c.xstride = xs;
+    LCK(launch_compose(c, count, L->stream));
+    L->acc_launches += 1;
+    return DTO_OK;
+  }
+  PermArgs a{};
+  a.seed = seed;
+  a.pair_id = P->pair_id;
+  a.perm_base = first;
+  a.xstride = xs;
+  if (P->same_set) {
+    // With identical feature sets only the relative order of the two lists
+    // matters: list 1 is shuffled, list 2 kept (idx2 = identity).
+    a.L = (int)P->N1;
+    a.list_tag = 1;
+    a.Ylab = P->dYlab;
+    a.X = X;
+    LCK(launch_perm(a, count, L->stream));
+    L->acc_launches += 1;
+    return DTO_OK;
+  }
+  long long ss = P->N1 + P->N2;
+  rc = lane_grow(L, &L->dSig, &L->sigBytes, (size_t)count * ss * 4);
+  if (rc) return rc;
+  int* sig = (int*)L->dSig;
+  a.L = (int)P->N1;
+  a.list_tag = 1;
+  a.sigma = sig;
+  a.sstride = ss;
+  LCK(launch_perm(a, count, L->stream));
+  a.L = (int)P->N2;
+  a.list_tag = 2;
+  a.sigma = sig + P->N1;
+  LCK(launch_perm(a, count, L->stream));
+  ComposeArgs c{};
+  c.N1 = (int)P->N1;
+  c.N2 = (int)P->N2;
+  c.idx1 = sig;
+  c.idx2 = sig + P->N1;
+  c.stride = ss;
+  c.map12 = P->dMap12;
+  c.lab2 = P->dLab2;
+  c.X = X;
+  c.xstride = xs;
+  LCK(launch_compose(c, count, L->stream));
+  L->acc_launches += 3;
+  return DTO_OK;
+}
+
+int lane_run_range(Lane* L, dto_pair* P, uint32_t perm_first, int64_t n_perm, uint64_t seed,
+                   const int32_t* perm_idx, int precision, dto_result* out_unpermuted, double* out_minp,
+                   dto_result* out_perm, dto_summary* out_summary) {
+  if (!P || P->ctx != L->ctx || !out_unpermuted) return lane_err(L, DTO_ERR_INVALID, "null argument");
+  if (n_perm < 0 || n_perm > 0x7fffffffLL || (long long)perm_first + n_perm > 0xffffffffLL)
+    return lane_err(L, DTO_ERR_INVALID, "n_perm out of range");
+  if (precision != DTO_PRECISION_FP64 && precision != DTO_PRECISION_SCREEN)
+    return lane_err(L, DTO_ERR_INVALID, "unknown precision");
+  LCK(cudaSetDevice(L->ctx->device));
+  const long long L12 = P->N1 + P->N2;
+  if (perm_idx) {
+    for (long long b = 0; b < n_perm; ++b) {
+      if (!check_perm(perm_idx + b * L12, P->N1) || !check_perm(perm_idx + b * L12 + P->N1, P->N2))
+        return lane_err(L, DTO_ERR_INVALID, "perm_idx row is not a permutation");
+    }
+  }
+  const int mode = precision == DTO_PRECISION_FP64 ? kModeFull64 : kModeScreen;
+  const long long xs = xstride_of(P->N1);
+  const long long batch = batch_of(P, n_perm, perm_idx != nullptr);
+  int rc = lane_grow(L, &L->dRes, &L->resBytes, (size_t)(batch + 1) * sizeof(TaskResult));
+  if (rc) return rc;
+  rc = lane_grow_host(L, &L->hRes, &L->hResBytes, (size_t)(batch + 1) * sizeof(TaskResult));
+  if (rc) return rc;
+  void* dIdx = nullptr;
+  size_t idxBytes = 0;
+  struct Guard { void*& p; ~Guard() { if (p) cudaFree(p); } } guard{dIdx};
+  TaskResult* dRes = (TaskResult*)L->dRes;
+  TaskResult* hRes = (TaskResult*)L->hRes;
+  L->acc_grid_ms = L->acc_perm_ms = 0.0;
+  L->acc_launches = L->acc_h2d = L->acc_d2h = 0;
+  LCK(cudaMemsetAsync(L->dRefined, 0, 3 * sizeof(unsigned long long), L->stream));
+  LCK(cudaMemsetAsync(L->dGuess, 0, 2048, L->stream));
+  LCK(cudaEventRecord(L->ev0, L->stream));
+  std::vector<double> minp((size_t)n_perm);
+  TaskResult unperm{};
+  // The unpermuted task (task 0) rides in row 0 of the first batch, through
+  // the exhaustive screen.  With the table screen (long runs), the first
+  // batch holds first_batch permutations; its 90th and 99th percentiles and
+  // maximum of the minimum p set the three-level table ladder of the
+  // remaining batches.
+  const long long first_batch = 1024;
+  const bool use_table = (mode == kModeScreen) && n_perm > 2 * first_batch;
+  auto take = [&](const TaskResult* hr, long long b0, int cnt) {
+    for (int q = 0; q < cnt; ++q) {
+      const TaskResult& r = hr[q];
+      minp[(size_t)(b0 + q)] = r.p;
+      if (out_minp) out_minp[b0 + q] = r.p;
+      if (out_perm) fill_result(P, r, 1, &out_perm[b0 + q]);
+    }
+  };
+  auto upload_idx = [&](void** buf, size_t* cap, long long b0, int cnt, const int32_t** dI) -> int {
+    *dI = nullptr;
+    if (!perm_idx || cnt <= 0) return DTO_OK;
+    const size_t bytes = (size_t)cnt * L12 * 4;
+    int r = lane_grow(L, buf, cap, bytes);
+    if (r) return r;
+    LCK(cudaMemcpyAsync(*buf, perm_idx + b0 * L12, bytes, cudaMemcpyHostToDevice, L->stream));
+    L->acc_h2d += (long long)bytes;
+    *dI = (const int32_t*)*buf;
+    return DTO_OK;
+  };
+  if (!use_table) {
+    for (long long b0 = 0; b0 < std::max<long long>(n_perm, 1); b0 += batch) {
+      const int row0 = (b0 == 0) ? 1 : 0;
+      const int cnt = (int)std::max(0LL, std::min(batch, n_perm - b0));
+      const int32_t* dI = nullptr;
+      rc = upload_idx(&dIdx, &idxBytes, b0, cnt, &dI);
+      if (rc) return rc;
+      if (cnt > 0) {
+        rc = lane_make_labels(L, P, seed, (uint32_t)(perm_first + b0), cnt, dI, row0);
+        if (rc) return rc;
+      } else {
+        rc = lane_grow(L, &L->dX, &L->xBytes, (size_t)xs * 2);
+        if (rc) return rc;
+      }
+      if (row0) LCK(cudaMemcpyAsync(L->dX, P->dYlab, (size_t)P->N1 * 2, cudaMemcpyDeviceToDevice, L->stream));
+      const int ntask = cnt + row0;
+      rc = lane_grid_tasks(L, P, (const int16_t*)L->dX, xs, ntask, mode, dRes, nullptr, nullptr, true);
+      if (rc) return rc;
+      LCK(cudaMemcpyAsync(hRes, dRes, (size_t)ntask * sizeof(TaskResult), cudaMemcpyDeviceToHost, L->stream));
+      L->acc_d2h += (long long)ntask * (long long)sizeof(TaskResult);
+      LCK(cudaStreamSynchronize(L->stream));
+      float ms = 0.f;
+      if (cnt > 0 && cudaEventElapsedTime(&ms, L->evk[0], L->evk[1]) == cudaSuccess) L->acc_perm_ms += ms;
+      if (cudaEventElapsedTime(&ms, L->evk[2], L->evk[3]) == cudaSuccess) L->acc_grid_ms += ms;
+      if (row0) unperm = hRes[0];
+      take(hRes + row0, b0, cnt);
+    }
+  } else {
+    // Slots left busy by a call that returned early hold nothing of this call.
+    LCK(cudaStreamSynchronize(L->side));
+    for (BatchSlot& sl : L->slot) sl.busy = false;
+    // Batch 0 (task 0 + first_batch permutations) runs through the exhaustive
+    // screen on the side stream.  Its slowest tasks (the permutations with
+    // the largest minimum p) take several times a typical task; meanwhile the
+    // main stream draws the labels of the first two pipelined batches.
+    const int cnt0 = (int)first_batch;
+    const int32_t* dI0 = nullptr;
+    rc = upload_idx(&dIdx, &idxBytes, 0, cnt0, &dI0);
+    if (rc) return rc;
+    rc = lane_make_labels(L, P, seed, perm_first, cnt0, dI0, 1);
+    if (rc) return rc;
+    LCK(cudaMemcpyAsync(L->dX, P->dYlab, (size_t)P->N1 * 2, cudaMemcpyDeviceToDevice, L->stream));
+    LCK(cudaEventRecord(L->evSide, L->stream));
+    LCK(cudaStreamWaitEvent(L->side, L->evSide, 0));
+    rc = lane_grid_tasks(L, P, (const int16_t*)L->dX, xs, cnt0 + 1, mode, dRes, nullptr, nullptr, true, L->side);
+    if (rc) return rc;
+    LCK(cudaMemcpyAsync(hRes, dRes, (size_t)(cnt0 + 1) * sizeof(TaskResult), cudaMemcpyDeviceToHost, L->side));
+    L->acc_d2h += (long long)(cnt0 + 1) * (long long)sizeof(TaskResult);
+    LCK(cudaEventRecord(L->evSide, L->side));
+    // Labels of the pipelined batches b = 0, 1, ... (permutations
+    // first_batch + b * batch on), slot b & 1; the first two are drawn now.
+    const long long pipe_from = first_batch;
+    const long long npipe = (n_perm - pipe_from + batch - 1) / batch;
+    bool drawn[2] = {false, false};
+    auto draw = [&](long long it) -> int {
+      BatchSlot& sl = L->slot[it & 1];
+      const long long b0 = pipe_from + it * batch;
+      const int cnt = (int)std::min(batch, n_perm - b0);
+      if (!sl.ev[0])
+        for (cudaEvent_t& e : sl.ev) LCK(cudaEventCreate(&e));
+      if (!sl.dCnt) LCK(cudaMalloc(&sl.dCnt, 256));
+      int r = lane_grow(L, &sl.dX, &sl.xBytes, (size_t)cnt * xs * 2);
+      if (!r) r = lane_grow(L, &sl.dRes, &sl.resBytes, (size_t)cnt * sizeof(TaskResult));
+      if (!r) r = lane_grow_host(L, &sl.hRes, &sl.hResBytes, (size_t)cnt * sizeof(TaskResult));
+      if (!r) r = lane_grow(L, &sl.dFall, &sl.fallBytes, (size_t)3 * cnt * 4);
+      if (r) return r;
+      const int32_t* dI = nullptr;
+      r = upload_idx(&sl.dIdx, &sl.idxBytes, b0, cnt, &dI);
+      if (r) return r;
+      LCK(cudaEventRecord(sl.ev[0], L->stream));
+      r = make_labels_launch(L, P, seed, (uint32_t)(perm_first + b0), cnt, dI, (int16_t*)sl.dX, xs);
+      if (r) return r;
+      LCK(cudaEventRecord(sl.ev[1], L->stream));
+      sl.b0 = b0;
+      sl.cnt = cnt;
+      return DTO_OK;
+    };
+    for (long long it = 0; it < std::min<long long>(npipe, 2); ++it) {
+      rc = draw(it);
+      if (rc) return rc;
+      drawn[it] = true;
+    }
+    // the first batch's results set the ladder
+    LCK(cudaEventSynchronize(L->evSide));
+    {
+      float ms = 0.f;
+      if (cudaEventElapsedTime(&ms, L->evk[0], L->evk[1]) == cudaSuccess) L->acc_perm_ms += ms;
+      if (cudaEventElapsedTime(&ms, L->evk[2], L->evk[3]) == cudaSuccess) L->acc_grid_ms += ms;
+    }
+    unperm = hRes[0];
+    take(hRes + 1, 0, cnt0);
+    std::vector<double> v(minp.begin(), minp.begin() + cnt0);
+    std::sort(v.begin(), v.end());
+    const double p90 = std::max(v[(size_t)(kLevel0Quantile * (double)(v.size() - 1))], 1e-300);
+    const double p99 = std::max(v[(size_t)(0.99 * (double)(v.size() - 1))], 1e-300);
+    const double pmax = std::max(v.back(), 1e-300);
+    const int sc = P->fshift;
+    const int t0 = fixed_log(p90, sc);
+    const int t1 = std::max(fixed_log(p99, sc), t0 + 1);
+    const int t2 = std::max((int)std::min(0.0, std::floor((std::log(pmax) + 1.0) * std::ldexp(1.0, sc))), t1 + 1);
+    rc = ensure_table(L, P, 0, t0);
+    if (rc) return rc;
+    rc = ensure_table(L, P, 1, t1);
+    if (rc) return rc;
+    rc = ensure_table(L, P, 2, t2);
+    if (rc) return rc;
+    const int nlev = 3;
+    // Two batches in flight: while batch b's later table levels, exhaustive
+    // fallback and result copy run on the side stream, batch b+1's labels and
+    // level-0 table sweep run on the main stream.
+    auto harvest = [&](BatchSlot& sl) -> int {
+      LCK(cudaEventSynchronize(sl.ev[7]));
+      float ms = 0.f;
+      if (cudaEventElapsedTime(&ms, sl.ev[0], sl.ev[1]) == cudaSuccess) L->acc_perm_ms += ms;
+      if (cudaEventElapsedTime(&ms, sl.ev[2], sl.ev[6]) == cudaSuccess) L->acc_grid_ms += ms;
+      if (cudaEventElapsedTime(&ms, sl.ev[4], sl.ev[5]) == cudaSuccess) L->acc_grid_ms += ms;
+      take((const TaskResult*)sl.hRes, sl.b0, sl.cnt);
+      L->acc_d2h += (long long)sl.cnt * (long long)sizeof(TaskResult);
+      sl.busy = false;
+      return DTO_OK;
+    };
+    for (long long it = 0; it < npipe; ++it) {
+      BatchSlot& sl = L->slot[it & 1];
+      if (sl.busy) {
+        rc = harvest(sl);
+        if (rc) return rc;
+      }
+      if (!(it < 2 && drawn[it])) {
+        rc = draw(it);
+        if (rc) return rc;
+      }
+      const int cnt = sl.cnt;
+      int16_t* X = (int16_t*)sl.dX;
+      TaskResult* dR = (TaskResult*)sl.dRes;
+      LCK(cudaEventRecord(sl.ev[2], L->stream));
+      rc = table_levels(L, P, X, xs, cnt, dR, 0, 1, (int*)sl.dFall, sl.dCnt, L->stream, 0);
+      if (rc) return rc;
+      LCK(cudaEventRecord(sl.ev[6], L->stream));
+      LCK(cudaStreamWaitEvent(L->side, sl.ev[6], 0));
+      LCK(cudaEventRecord(sl.ev[4], L->side));
+      rc = table_levels(L, P, X, xs, cnt, dR, 1, nlev, (int*)sl.dFall, sl.dCnt, L->side, 1);
+      if (rc) return rc;
+      rc = table_exhaustive(L, P, X, xs, cnt, dR, nlev, (const int*)sl.dFall, sl.dCnt, L->side);
+      if (rc) return rc;
+      LCK(cudaEventRecord(sl.ev[5], L->side));
+      LCK(cudaMemcpyAsync(sl.hRes, dR, (size_t)cnt * sizeof(TaskResult), cudaMemcpyDeviceToHost, L->side));
+      LCK(cudaEventRecord(sl.ev[7], L->side));
+      sl.busy = true;
+    }
+    for (BatchSlot& sl : L->slot) {
+      if (sl.busy) {
+        rc = harvest(sl);
+        if (rc) return rc;
+      }
+    }
+    // the main stream's timing event follows the side stream's last work
+    LCK(cudaEventRecord(L->evSide, L->side));
+    LCK(cudaStreamWaitEvent(L->stream, L->evSide, 0));
+  }
+  fill_result(P, unperm, 0, out_unpermuted);
+  const double p_obs = unperm.p;
+  long long count_le = 0;
+  for (long long q = 0; q < n_perm; ++q) count_le += (minp[(size_t)q] <= p_obs);
+  LCK(cudaEventRecord(L->ev1, L->stream));
+  unsigned long long refined[3] = {0, 0, 0};
+  LCK(cudaMemcpyAsync(refined, L->dRefined, sizeof(refined), cudaMemcpyDeviceToHost, L->stream));
+  LCK(cudaStreamSynchronize(L->stream));
+  if (out_summary) {
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, L->ev0, L->ev1);
+    dto_summary& s = *out_summary;
+    s.n_perm = n_perm;
+    s.count_le = count_le;
+    s.empirical_pvalue = n_perm > 0 ? (double)count_le / (double)n_perm : 1.0;
+    s.fdr = dto_fdr(out_unpermuted->set1_len, out_unpermuted->set2_len, out_unpermuted->intersection_size,
+                    P->npop, 0.8);
+    s.logp_err_bound_screen = precision == DTO_PRECISION_SCREEN ? 4.5 * std::ldexp(1.0, -P->fshift) : 0.0;
+    s.logp_err_bound_fp64 = 2.0e-13;
+    s.n_fallback = (int64_t)refined[2];
+    s.n_refined = (int64_t)refined[0];
+    s.n_stage2 = (int64_t)refined[1];
+    s.device_ms = ms;
+    s.grid_ms = L->acc_grid_ms;
+    s.perm_ms = L->acc_perm_ms;
+    s.n_launches = L->acc_launches;
+    s.h2d_bytes = L->acc_h2d;
+    s.d2h_bytes = L->acc_d2h + 16;
+  }
+  return DTO_OK;
+}
+
+}  // namespace dto

@@ -7,8 +7,8 @@ import ctypes as C
 
 import numpy as np
 
-from ._lib import (DtoResult, DtoSummary, PRECISION_FP64, PRECISION_SCREEN, RESULT_DTYPE, check,
-                   lib, ptr)
+from ._lib import (DtoError, DtoResult, DtoSummary, PRECISION_FP64, PRECISION_SCREEN, RESULT_DTYPE,
+                   check, lib, ptr)
 
 _PREC = {"fp64": PRECISION_FP64, "screen": PRECISION_SCREEN, "fp32screen": PRECISION_SCREEN}
 
@@ -61,6 +61,27 @@ class Engine:
     def pair(self, ranks1, feat1, ranks2, feat2, n_features, population):
         return DevicePair(self, ranks1, feat1, ranks2, feat2, n_features, population)
 
+    def server(self, lanes=4, mem_budget=0):
+        """A request executor on this device (dto_serve_create)."""
+        return Server(self, lanes, mem_budget)
+
+    def batch_run(self, pairs, n_perm, seeds, precision="screen", lanes=4, want_minp=True):
+        """The permutation null of many pairs at once (dto_batch_run): pair q
+        takes n_perm[q] permutations from id 1 of seeds[q].  Returns one
+        RunResult per pair."""
+        npairs = len(pairs)
+        n_perm = np.ascontiguousarray(np.broadcast_to(np.asarray(n_perm, np.int64), (npairs,)))
+        seeds = np.ascontiguousarray(np.broadcast_to(np.asarray(seeds, np.uint64), (npairs,)))
+        handles = (C.c_void_p * npairs)(*[p.handle.value for p in pairs])
+        unp = (DtoResult * npairs)()
+        summ = (DtoSummary * npairs)()
+        minps = [np.empty(int(n), np.float64) for n in n_perm] if want_minp else None
+        mp = (C.c_void_p * npairs)(*[m.ctypes.data for m in minps]) if want_minp else None
+        check(lib().dto_batch_run(self.handle, npairs, handles, ptr(n_perm), ptr(seeds),
+                                  precision_code(precision), int(lanes), unp, mp, summ), self.handle)
+        return [RunResult(unp[q].as_dict(), minps[q] if want_minp else None, None, summ[q].as_dict())
+                for q in range(npairs)]
+
     def hypergeom_sf(self, N, K, n, k):
         """P(X >= k), X ~ Hypergeometric(N, K, n), elementwise, on the device."""
         arrs = [np.ascontiguousarray(np.broadcast_to(np.asarray(v, np.int64), np.broadcast(N, K, n, k).shape))
@@ -70,6 +91,87 @@ class Engine:
         check(lib().dto_hypergeom_sf(self.handle, ptr(flat[0]), ptr(flat[1]), ptr(flat[2]),
                                      ptr(flat[3]), ptr(out), out.shape[0]), self.handle)
         return out.reshape(arrs[0].shape)
+
+
+class Server:
+    """A request executor (dto_server): ``lanes`` permutation nulls run at
+    once, admitted in arrival order as lanes and device memory free up."""
+
+    def __init__(self, engine, lanes=4, mem_budget=0):
+        self.engine = engine
+        self._srv = C.c_void_p()
+        check(lib().dto_serve_create(engine.handle, int(lanes), int(mem_budget), C.byref(self._srv)),
+              engine.handle)
+        self.lanes = int(lanes)
+
+    @property
+    def handle(self):
+        if not self._srv:
+            raise RuntimeError("server is closed")
+        return self._srv
+
+    def submit(self, pair, n_perm, seed=0, first=1, precision="screen", want_minp=True):
+        job = Job(self, pair, int(n_perm), want_minp)
+        st = lib().dto_serve_submit(self.handle, pair.handle, int(first), int(n_perm),
+                                    int(seed) & (2**64 - 1), precision_code(precision),
+                                    C.byref(job._unp), ptr(job._minp), C.byref(job._summ),
+                                    C.byref(job._id))
+        if st != 0:
+            raise DtoError(st, lib().dto_serve_last_error(self.handle).decode())
+        return job
+
+    def stats(self):
+        q, r, c, b = C.c_int64(), C.c_int64(), C.c_int64(), C.c_int64()
+        check(lib().dto_serve_stats(self.handle, C.byref(q), C.byref(r), C.byref(c), C.byref(b)))
+        return {"queued": q.value, "running": r.value, "completed": c.value, "reserved_bytes": b.value}
+
+    def close(self):
+        if getattr(self, "_srv", None):
+            lib().dto_serve_destroy(self._srv)
+            self._srv = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+
+class Job:
+    """One queued request; its output buffers live here until it is waited for."""
+
+    def __init__(self, server, pair, n_perm, want_minp):
+        self.server = server
+        self.pair = pair
+        self._id = C.c_int64(0)
+        self._unp = DtoResult()
+        self._summ = DtoSummary()
+        self._minp = np.empty(n_perm, np.float64) if want_minp else None
+        self._result = None
+        self.queue_ms = self.run_ms = None
+
+    def done(self):
+        if self._result is not None:
+            return True
+        d = C.c_int(0)
+        check(lib().dto_serve_poll(self.server.handle, self._id.value, C.byref(d)))
+        return bool(d.value)
+
+    def wait(self):
+        if self._result is None:
+            qm, rm = C.c_double(), C.c_double()
+            st = lib().dto_serve_wait(self.server.handle, self._id.value, C.byref(qm), C.byref(rm))
+            if st != 0:
+                raise DtoError(st, lib().dto_serve_last_error(self.server.handle).decode())
+            self.queue_ms, self.run_ms = qm.value, rm.value
+            self._result = RunResult(self._unp.as_dict(), self._minp, None, self._summ.as_dict())
+        return self._result
 
 
 class RunResult:

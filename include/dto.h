@@ -198,6 +198,48 @@ DTO_API int dto_export_permutations(dto_ctx* ctx, dto_pair* pair, uint64_t seed,
 DTO_API double dto_fdr(int64_t set1_len, int64_t set2_len, int64_t overlap, int64_t population,
                double sensitivity);
 
+/* ---- Many pairs, many requests ----
+ * The reference runs one permutation null per process (src/main.rs:122-166,
+ * tasks over threads in src/run/single_node.rs:83-137); these entry points run
+ * many at once on one GPU.  A server owns `lanes` lanes (streams, scratch and
+ * table screens of their own) and one worker thread per lane.  Requests queue
+ * in arrival order; the head is admitted when a lane is free and its device
+ * working set (dto_run_device_bytes) fits under mem_budget bytes next to the
+ * requests running (mem_budget 0: no budget; a request larger than the budget
+ * runs alone).  A request's results equal dto_run_range's for the same
+ * arguments, whatever runs beside it. */
+typedef struct dto_server dto_server;
+typedef int64_t dto_job;
+
+DTO_API int dto_serve_create(dto_ctx* ctx, int lanes, int64_t mem_budget, dto_server** out);
+/* Waits for every queued and running request, then frees the server. */
+DTO_API int dto_serve_destroy(dto_server* srv);
+/* Queues dto_run_range(pair, perm_first, n_perm, seed, precision) without a
+ * test-mode index array.  The output buffers (out_minp: n_perm doubles,
+ * nullable; out_summary nullable) must stay valid until the request is
+ * waited for. */
+DTO_API int dto_serve_submit(dto_server* srv, dto_pair* pair, uint32_t perm_first, int64_t n_perm,
+                             uint64_t seed, int precision, dto_result* out_unpermuted, double* out_minp,
+                             dto_summary* out_summary, dto_job* job);
+/* *done = 1 once the request has finished (its outputs are written). */
+DTO_API int dto_serve_poll(dto_server* srv, dto_job job, int* done);
+/* Blocks until the request finishes, returns its status and forgets it;
+ * queue_ms / run_ms (nullable) get the host wall time from submission to
+ * admission and from admission to completion. */
+DTO_API int dto_serve_wait(dto_server* srv, dto_job job, double* queue_ms, double* run_ms);
+DTO_API const char* dto_serve_last_error(dto_server* srv);
+DTO_API int dto_serve_stats(dto_server* srv, int64_t* queued, int64_t* running, int64_t* completed,
+                            int64_t* reserved_bytes);
+/* Device bytes a dto_run_range of n_perm permutations of the pair holds at
+ * its peak (the admission size of a request). */
+DTO_API int64_t dto_run_device_bytes(const dto_pair* pair, int64_t n_perm);
+/* The permutation null of npairs pairs (pair q: n_perm[q] permutations from
+ * id 1 of seeds[q]) over `lanes` lanes (<= 0: 4); per-pair outputs as in
+ * dto_run_range (out_minp[q] and out_summary nullable). */
+DTO_API int dto_batch_run(dto_ctx* ctx, int npairs, dto_pair* const* pairs, const int64_t* n_perm,
+                          const uint64_t* seeds, int precision, int lanes, dto_result* out_unpermuted,
+                          double* const* out_minp, dto_summary* out_summary);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1,0 +1,93 @@
+"""Many pairs and many requests on one GPU: dto_serve_* and dto_batch_run.
+
+A request's results must not depend on what runs beside it: every request is
+run alone through dto_run_range first, then all of them through a server
+whose lanes overlap them on the device (some submitted while others run), and
+the per-permutation minimum p-values and the unpermuted optimum must agree bit
+for bit.
+"""
+import time
+
+import numpy as np
+import pytest
+
+from dual_threshold_optimization_gb300 import synth
+from dual_threshold_optimization_gb300._lib import DtoError
+
+pytestmark = pytest.mark.gpu
+
+
+def _mix(engine):
+    specs = [  # (pair, n_perm, seed): table pipeline and exhaustive-only runs, same- and mixed-set lists
+        (synth.copula_pair(20000, 0.2, seed=71), 30000, 5),
+        (synth.copula_pair(6000, 0.3, seed=72, frac_tied2=0.1), 5000, 6),
+        (synth.small_pair(4000, 0.2, seed=73, subset1=3600, subset2=3800), 3000, 7),
+        (synth.copula_pair(2500, 0.0, seed=74), 800, 8),
+        (synth.background_pair(12000, 9000, 0.1, seed=75), 12000, 9),
+        (synth.copula_pair(20000, 0.2, seed=71), 4000, 10),  # same lists again, other seed
+    ]
+    out = []
+    for p, n, s in specs:
+        dp = engine.pair(p.ranks1, p.feat1, p.ranks2, p.feat2, p.n_features, p.population)
+        out.append((dp, n, s))
+    return out
+
+
+def test_requests_same_alone_and_in_the_mix(engine):
+    mix = _mix(engine)
+    alone = [dp.run(n, seed=s) for dp, n, s in mix]
+    with engine.server(lanes=3) as srv:
+        jobs = [srv.submit(dp, n, seed=s) for dp, n, s in mix[:3]]
+        time.sleep(0.002)  # the rest arrive while the first ones run
+        jobs += [srv.submit(dp, n, seed=s) for dp, n, s in mix[3:]]
+        res = [j.wait() for j in jobs]
+        st = srv.stats()
+    assert st["queued"] == 0 and st["running"] == 0 and st["reserved_bytes"] == 0
+    for a, r, (dp, n, s) in zip(alone, res, mix):
+        assert r.unpermuted == a.unpermuted, (n, s)
+        assert np.array_equal(r.minp, a.minp), (n, s)
+        assert r.summary["count_le"] == a.summary["count_le"]
+        assert r.summary["empirical_pvalue"] == a.summary["empirical_pvalue"]
+    for dp, _, _ in mix:
+        dp.close()
+
+
+def test_batch_run_equals_single_runs(engine):
+    pairs = [synth.copula_pair(n, r, seed=80 + q) for q, (n, r) in
+             enumerate([(2000, 0.1), (9000, 0.3), (15000, 0.0), (3000, 0.4)])]
+    dps = [engine.pair(p.ranks1, p.feat1, p.ranks2, p.feat2, p.n_features, p.population) for p in pairs]
+    n_perm = [2500, 4000, 1000, 6000]
+    seeds = [11, 12, 13, 14]
+    got = engine.batch_run(dps, n_perm, seeds, lanes=2)
+    for dp, n, s, g in zip(dps, n_perm, seeds, got):
+        a = dp.run(n, seed=s)
+        assert g.unpermuted == a.unpermuted
+        assert np.array_equal(g.minp, a.minp)
+    for dp in dps:
+        dp.close()
+
+
+def test_memory_admission_and_errors(engine):
+    from dual_threshold_optimization_gb300._lib import lib
+    p = synth.copula_pair(8000, 0.2, seed=90)
+    dp = engine.pair(p.ranks1, p.feat1, p.ranks2, p.feat2, p.n_features, p.population)
+    need = lib().dto_run_device_bytes(dp.handle, 5000)
+    assert need > 0
+    # a budget of one request: the requests run one after another, and one
+    # larger than the budget still runs (alone)
+    with engine.server(lanes=3, mem_budget=need) as srv:
+        jobs = [srv.submit(dp, 5000, seed=s) for s in (1, 2, 3)]
+        big = srv.submit(dp, 20000, seed=4)
+        peak = 0
+        while not all(j.done() for j in jobs + [big]):
+            peak = max(peak, srv.stats()["running"])
+            time.sleep(0.0005)
+        res = [j.wait() for j in jobs]
+        rb = big.wait()
+        assert peak <= 1
+        with pytest.raises(DtoError):
+            srv.submit(dp, 10, precision=7)
+    for s, r in zip((1, 2, 3), res):
+        assert np.array_equal(r.minp, dp.run(5000, seed=s).minp)
+    assert np.array_equal(rb.minp, dp.run(20000, seed=4).minp)
+    dp.close()
