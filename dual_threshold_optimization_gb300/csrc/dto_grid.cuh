@@ -590,7 +590,7 @@ __global__ void __launch_bounds__(kGridWarps * 32, 1) grid_kernel(const GridArgs
 
 template <int C>
 cudaError_t launch_grid_impl(const GridArgs& a, int ctas, size_t smem, cudaStream_t s) {
-  cudaError_t e = cudaFuncSetAttribute(grid_kernel<C>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  cudaError_t e = raise_smem_limit((const void*)grid_kernel<C>, smem);
   if (e != cudaSuccess) return e;
   grid_kernel<C><<<ctas, kGridWarps * 32, smem, s>>>(a);
   return cudaGetLastError();

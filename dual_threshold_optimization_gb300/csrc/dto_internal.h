@@ -157,6 +157,12 @@ struct TableGridArgs {
   int hitcap;
 };
 
+// Raises a kernel's dynamic shared-memory limit to at least `bytes` on the
+// current device.  The limit only ever grows, so launches from several host
+// threads (executor lanes) never see it lowered between their own set and
+// launch.
+cudaError_t raise_smem_limit(const void* kernel, size_t bytes);
+
 size_t grid_smem_bytes(int C, int n1, long long Npop, int smemF);
 size_t table_smem_bytes(int C, int n1);
 size_t table_entries(int C, int n1);

@@ -21,6 +21,9 @@
 // One level of Rao-Sandelius bucketing followed by uniform shuffles of the
 // buckets gives an exactly uniform permutation.
 #include <algorithm>
+#include <map>
+#include <mutex>
+#include <utility>
 
 #include "dto_grid.cuh"
 #include "dto_internal.h"
@@ -291,11 +294,25 @@ cudaError_t launch_table_grid(const TableGridArgs& a, int C, int ctas, cudaStrea
   }
 }
 
+cudaError_t raise_smem_limit(const void* kernel, size_t bytes) {
+  static std::mutex mu;
+  static std::map<std::pair<int, const void*>, size_t> limit;
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  std::lock_guard<std::mutex> g(mu);
+  size_t& cur = limit[std::make_pair(dev, kernel)];
+  if (bytes <= cur) return cudaSuccess;
+  e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  if (e == cudaSuccess) cur = bytes;
+  return e;
+}
+
 cudaError_t launch_perm(const PermArgs& a, int count, cudaStream_t s) {
   if (count <= 0) return cudaSuccess;
   size_t smem = (size_t)kBuckets * 4 + (a.L <= kPermWordsMaxL ? (size_t)a.L * 4 : 0) +
                 (((size_t)a.L * 2 + 15) & ~(size_t)15);
-  cudaError_t e = cudaFuncSetAttribute(perm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  cudaError_t e = raise_smem_limit((const void*)perm_kernel, smem);
   if (e != cudaSuccess) return e;
   perm_kernel<<<count, kPermThreads, smem, s>>>(a);
   return cudaGetLastError();
@@ -304,7 +321,7 @@ cudaError_t launch_perm(const PermArgs& a, int count, cudaStream_t s) {
 cudaError_t launch_compose(const ComposeArgs& a, int count, cudaStream_t s) {
   if (count <= 0) return cudaSuccess;
   size_t smem = a.idx2 ? (((size_t)a.N2 * 2 + 15) & ~(size_t)15) : 16;
-  cudaError_t e = cudaFuncSetAttribute(compose_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  cudaError_t e = raise_smem_limit((const void*)compose_kernel, smem);
   if (e != cudaSuccess) return e;
   compose_kernel<<<count, 1024, smem, s>>>(a);
   return cudaGetLastError();

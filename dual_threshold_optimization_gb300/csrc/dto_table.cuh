@@ -547,8 +547,7 @@ __global__ void __launch_bounds__(kTableWarps * 32, kTableCtasPerSm) table_grid_
 
 template <int C, bool Packed>
 cudaError_t launch_table_grid_kernel(const TableGridArgs& a, int ctas, size_t smem, cudaStream_t s) {
-  cudaError_t e =
-      cudaFuncSetAttribute(table_grid_kernel<C, Packed>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  cudaError_t e = raise_smem_limit((const void*)table_grid_kernel<C, Packed>, smem);
   if (e != cudaSuccess) return e;
   table_grid_kernel<C, Packed><<<ctas, kTableWarps * 32, smem, s>>>(a);
   return cudaGetLastError();
