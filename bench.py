@@ -42,6 +42,10 @@ METRIC = "perms/s on 1 GB300 at N=20k (FP32-screen vs plain FP64, same argmin); 
 N_FEATURES = 20000
 RHO = 0.2
 PERMS_PER_STEP = 100000
+# DRAM bytes per task of the level-0 table sweep at N = 20,000 (ncu capture
+# summarised in profiles/table_grid_level0_n20k.md): labels read once, hit
+# buffer written and re-read.
+SWEEP0_DRAM_BYTES_PER_TASK = 72800.0
 WORKLOAD = ("single pair, N=20000 features, list 2 Gaussian copula rho=0.2 to list 1, no ties, "
             "100000 on-device Philox permutations per step + the unpermuted task, "
             "FP32 screen + FP64 refine")
@@ -312,19 +316,32 @@ def run_gpu(args):
             torch.distributed.destroy_process_group()
         return 0
 
-    # ---- roofline of the grid kernel ----
+    # ---- roofline of the dominant kernel: the level-0 table sweep ----
     cells = dp.n1 * dp.n2
-    grid_s = sum(grid_ms) * 1e-3
-    tasks = args.steps * (P + 1)
-    achieved_tflops = 8.0 * cells * tasks / grid_s / 1e12
     peaks = measured_peaks(torch, "cuda")
     fp32_peak = peaks.get("fp32_tflops")
-    roofline = {"bound": "fp32", "achieved": achieved_tflops, "peak": fp32_peak, "unit": "TFLOP/s",
-                "frac": (achieved_tflops / fp32_peak) if fp32_peak else None,
-                "traffic": args.traffic,
-                "kernel": "threshold-pair search: table_grid_kernel<20> ladder + exhaustive grid_kernel<20> fallback",
-                "work_per_task": "8 ops x %d cells" % cells,
+    s0_ms = sum(s_["sweep0_ms"] for s_ in summaries)
+    s0_tasks = sum(s_["sweep0_tasks"] for s_ in summaries)
+    s0_launches = sum(s_["sweep0_launches"] for s_ in summaries)
+    achieved = 8.0 * cells * s0_tasks / (s0_ms * 1e-3) / 1e12 if s0_ms > 0 else None
+    grid_s = sum(grid_ms) * 1e-3
+    whole = 8.0 * cells * args.steps * (P + 1) / grid_s / 1e12
+    traffic = args.traffic
+    if traffic is None and s0_launches and P == PERMS_PER_STEP:
+        traffic = SWEEP0_DRAM_BYTES_PER_TASK * s0_tasks / s0_launches
+    roofline = {"bound": "fp32", "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
+                "frac": (achieved / fp32_peak) if (fp32_peak and achieved) else None,
+                "traffic": traffic,
+                "kernel": "table_grid_kernel<%d, packed> level-0 sweep (main stream)" % (20 if cells == 589 * 589 else 0),
+                "work_per_task": "8 FP32-class ops x %d cells (the nine-term log-pmf sum per cell)" % cells,
+                "launch_ms": s0_ms / s0_launches if s0_launches else None,
+                "tasks_per_launch": s0_tasks / s0_launches if s0_launches else None,
                 "peak_source": "measured: cuBLAS SGEMM 8192^3 without TF32 on this GPU (FP32 pipe)",
+                "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one level-0 launch "
+                                  "(profiles/table_grid_level0_n20k.md), scaled to this launch's tasks",
+                "whole_search": {"achieved": whole, "frac": whole / fp32_peak if fp32_peak else None,
+                                 "note": "all search kernels of a step (table levels, exhaustive "
+                                         "fallback, first batch), CUDA-event times summed over streams"},
                 "grid_ms_per_step": statistics.mean(grid_ms),
                 "perm_ms_per_step": statistics.mean(s_["perm_ms"] for s_ in summaries)}
 

@@ -59,7 +59,8 @@ class DtoSummary(C.Structure):
                 ("logp_err_bound_fp64", C.c_double), ("n_fallback", C.c_int64),
                 ("n_refined", C.c_int64), ("n_stage2", C.c_int64),
                 ("device_ms", C.c_double), ("grid_ms", C.c_double), ("perm_ms", C.c_double),
-                ("n_launches", C.c_int64), ("h2d_bytes", C.c_int64), ("d2h_bytes", C.c_int64)]
+                ("n_launches", C.c_int64), ("h2d_bytes", C.c_int64), ("d2h_bytes", C.c_int64),
+                ("sweep0_ms", C.c_double), ("sweep0_launches", C.c_int64), ("sweep0_tasks", C.c_int64)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}

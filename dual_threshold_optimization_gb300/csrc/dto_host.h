@@ -51,8 +51,8 @@ struct Lane {
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   cudaEvent_t evk[4] = {nullptr, nullptr, nullptr, nullptr};  // perm start/end, grid start/end
   // per-run accounting
-  double acc_grid_ms = 0.0, acc_perm_ms = 0.0;
-  long long acc_launches = 0, acc_h2d = 0, acc_d2h = 0;
+  double acc_grid_ms = 0.0, acc_perm_ms = 0.0, acc_sweep0_ms = 0.0;
+  long long acc_launches = 0, acc_h2d = 0, acc_d2h = 0, acc_sweep0_launches = 0, acc_sweep0_tasks = 0;
   // scratch, grown on demand
   void* dX = nullptr;
   size_t xBytes = 0;

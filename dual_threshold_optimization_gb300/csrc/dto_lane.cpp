@@ -409,8 +409,8 @@ int lane_run_range(Lane* L, dto_pair* P, uint32_t perm_first, int64_t n_perm, ui
   struct Guard { void*& p; ~Guard() { if (p) cudaFree(p); } } guard{dIdx};
   TaskResult* dRes = (TaskResult*)L->dRes;
   TaskResult* hRes = (TaskResult*)L->hRes;
-  L->acc_grid_ms = L->acc_perm_ms = 0.0;
-  L->acc_launches = L->acc_h2d = L->acc_d2h = 0;
+  L->acc_grid_ms = L->acc_perm_ms = L->acc_sweep0_ms = 0.0;
+  L->acc_launches = L->acc_h2d = L->acc_d2h = L->acc_sweep0_launches = L->acc_sweep0_tasks = 0;
   LCK(cudaMemsetAsync(L->dRefined, 0, 3 * sizeof(unsigned long long), L->stream));
   LCK(cudaMemsetAsync(L->dGuess, 0, 2048, L->stream));
   LCK(cudaEventRecord(L->ev0, L->stream));
@@ -556,7 +556,12 @@ int lane_run_range(Lane* L, dto_pair* P, uint32_t perm_first, int64_t n_perm, ui
       LCK(cudaEventSynchronize(sl.ev[7]));
       float ms = 0.f;
       if (cudaEventElapsedTime(&ms, sl.ev[0], sl.ev[1]) == cudaSuccess) L->acc_perm_ms += ms;
-      if (cudaEventElapsedTime(&ms, sl.ev[2], sl.ev[6]) == cudaSuccess) L->acc_grid_ms += ms;
+      if (cudaEventElapsedTime(&ms, sl.ev[2], sl.ev[6]) == cudaSuccess) {
+        L->acc_grid_ms += ms;
+        L->acc_sweep0_ms += ms;
+        L->acc_sweep0_launches += 1;
+        L->acc_sweep0_tasks += sl.cnt;
+      }
       if (cudaEventElapsedTime(&ms, sl.ev[4], sl.ev[5]) == cudaSuccess) L->acc_grid_ms += ms;
       take((const TaskResult*)sl.hRes, sl.b0, sl.cnt);
       L->acc_d2h += (long long)sl.cnt * (long long)sizeof(TaskResult);
@@ -629,6 +634,9 @@ int lane_run_range(Lane* L, dto_pair* P, uint32_t perm_first, int64_t n_perm, ui
     s.n_launches = L->acc_launches;
     s.h2d_bytes = L->acc_h2d;
     s.d2h_bytes = L->acc_d2h + 16;
+    s.sweep0_ms = L->acc_sweep0_ms;
+    s.sweep0_launches = L->acc_sweep0_launches;
+    s.sweep0_tasks = L->acc_sweep0_tasks;
   }
   return DTO_OK;
 }

@@ -80,6 +80,9 @@ typedef struct {
     int64_t n_launches;            /* kernels launched */
     int64_t h2d_bytes;             /* host-to-device bytes copied by this call */
     int64_t d2h_bytes;             /* device-to-host bytes copied by this call */
+    double sweep0_ms;              /* CUDA-event time of the level-0 table sweeps (main stream) */
+    int64_t sweep0_launches;       /* their launches */
+    int64_t sweep0_tasks;          /* permutations they took */
 } dto_summary;
 
 DTO_API int dto_version(void);
