@@ -146,6 +146,7 @@ struct TableGridArgs {
   int tau;                // the guess the table was built for
   const uint16_t* kthr;   // [n1][table_cq(C) / 8][32][8]
   int packed;             // 16-bit overlap sweep (every overlap <= 0x7FFF)
+  int smemF;              // the ln m! table is copied to shared memory
   TaskResult* out;
   int* work;
   unsigned long long* n_refined;  // [3]
@@ -164,7 +165,7 @@ struct TableGridArgs {
 cudaError_t raise_smem_limit(const void* kernel, size_t bytes);
 
 size_t grid_smem_bytes(int C, int n1, long long Npop, int smemF);
-size_t table_smem_bytes(int C, int n1);
+size_t table_smem_bytes(int C, int n1, int n2, long long Npop, int smemF);
 size_t table_entries(int C, int n1);
 cudaError_t launch_table_build(const TableArgs& a, int nsm, cudaStream_t s);
 cudaError_t launch_table_grid(const TableGridArgs& a, int C, int ctas, cudaStream_t s);

@@ -267,8 +267,10 @@ cudaError_t launch_grid(const GridArgs& a, int ctas, cudaStream_t s) {
   }
 }
 
-size_t table_smem_bytes(int C, int n1) {
-  return (size_t)((n1 + 1 + 3) & ~3) * 4 + (size_t)kTableWarps * table_warp_ints(C) * 4;
+size_t table_smem_bytes(int C, int n1, int n2, long long Npop, int smemF) {
+  const size_t f = smemF ? (size_t)((Npop + 1 + 3) & ~3LL) * 4 : 0;
+  return f + (size_t)((n1 + 1 + 3) & ~3) * 4 + (size_t)((n2 + 3) & ~3) * 4 +
+         (size_t)kTableWarps * table_warp_ints(C) * 4;
 }
 
 size_t table_entries(int C, int n1) { return (size_t)n1 * 32 * table_cq(C); }
@@ -282,7 +284,7 @@ cudaError_t launch_table_build(const TableArgs& a, int nsm, cudaStream_t s) {
 }
 
 cudaError_t launch_table_grid(const TableGridArgs& a, int C, int ctas, cudaStream_t s) {
-  size_t smem = table_smem_bytes(C, a.P.n1);
+  size_t smem = table_smem_bytes(C, a.P.n1, a.P.n2, a.P.Npop, a.smemF);
   switch (C) {
 #define DTO_CASE(CC) \
   case CC:           \

@@ -256,6 +256,7 @@ int table_levels(Lane* L, dto_pair* P, const int16_t* X, long long xstride, int 
     a.tau = L->kthr_tau[level];
     a.kthr = L->dKthr[level];
     a.packed = P->ncommon <= kPackedMaxCommon ? 1 : 0;
+    a.smemF = table_smem_bytes(P->C, P->dev.n1, P->dev.n2, P->npop, 1) <= L->ctx->smem_optin ? 1 : 0;
     a.out = dOut;
     a.work = cnts + level;
     a.n_refined = L->dRefined;

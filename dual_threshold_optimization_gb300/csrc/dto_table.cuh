@@ -124,8 +124,17 @@ __device__ __forceinline__ TableWarpMem table_warp_mem(int* base, int C) {
   return m;
 }
 
+// Pair tables one CTA reads in the resolve paths: row sizes K (rowstart),
+// column sizes n and the fixed-point ln m! table, in shared memory when the
+// table fits (generic pointers: shared or global).
+struct TabGrid {
+  const int* row;
+  const int* ncnt;
+  const uint32_t* F;
+};
+
 // Stage 3 on the survivors the current B admits.
-static __device__ __noinline__ void table_refine(const TableGridArgs& A, const int* sRow, const TableWarpMem& m,
+static __device__ __noinline__ void table_refine(const TableGridArgs& A, const TabGrid& g, const TableWarpMem& m,
                                           int lane) {
   __syncwarp();
   WarpTask st = *m.st;
@@ -134,7 +143,7 @@ static __device__ __noinline__ void table_refine(const TableGridArgs& A, const i
   for (int q = lane; q < st.nsurv; q += 32) {
     if (m.survLo[q] <= st.B + 1) {
       int ci = m.survCell[q] >> 16, cj = m.survCell[q] & 0xffff;
-      double p = sf64(A.P.LF, A.P.Npop, sRow[ci + 1], __ldg(A.P.ncnt + cj), m.survK[q]);
+      double p = sf64(A.P.LF, A.P.Npop, g.row[ci + 1], g.ncnt[cj], m.survK[q]);
       best_take(lb, p, m.survK[q], ci, cj);
       ++done;
     }
@@ -159,13 +168,13 @@ static __device__ __noinline__ void table_refine(const TableGridArgs& A, const i
 // the reference's tie-break and writes its result.  Tasks share the FP64
 // instructions this way: on GB300 an FP64 warp instruction costs the same
 // whether one lane or all 32 are active.
-static __device__ __noinline__ void table_pending_flush(const TableGridArgs& A, const int* sRow,
+static __device__ __noinline__ void table_pending_flush(const TableGridArgs& A, const TabGrid& g,
                                                         const TableWarpMem& m, int lane) {
   __syncwarp();
   const int np = m.st->npend;
   for (int q = lane; q < np; q += 32) {
     const int ci = m.pendCell[q] >> 16, cj = m.pendCell[q] & 0xffff;
-    m.pendP[q] = sf64(A.P.LF, A.P.Npop, sRow[ci + 1], __ldg(A.P.ncnt + cj), m.pendK[q]);
+    m.pendP[q] = sf64(A.P.LF, A.P.Npop, g.row[ci + 1], g.ncnt[cj], m.pendK[q]);
   }
   __syncwarp();
   for (int q = lane; q < np; q += 32) {
@@ -187,12 +196,12 @@ static __device__ __noinline__ void table_pending_flush(const TableGridArgs& A, 
 
 // Queue the task's survivors that the final B admits, without duplicates
 // (a cell can reach stage 2 twice: as a seed and as a hit).
-static __device__ __noinline__ void table_defer(const TableGridArgs& A, const int* sRow, const TableWarpMem& m,
+static __device__ __noinline__ void table_defer(const TableGridArgs& A, const TabGrid& g, const TableWarpMem& m,
                                                 int lane, int task) {
   __syncwarp();
   const int B = m.st->B;
   const int ns = m.st->nsurv;
-  if (m.st->npend + ns > kPend) table_pending_flush(A, sRow, m, lane);
+  if (m.st->npend + ns > kPend) table_pending_flush(A, g, m, lane);
   int npend = m.st->npend;
   for (int q0 = 0; q0 < ns; q0 += 32) {
     const int q = q0 + lane;
@@ -223,12 +232,12 @@ static __device__ __noinline__ void table_defer(const TableGridArgs& A, const in
 }
 
 // Stage 2 on the candidate buffer.
-static __device__ __noinline__ void table_flush(const TableGridArgs& A, const int* sRow, const TableWarpMem& m,
+static __device__ __noinline__ void table_flush(const TableGridArgs& A, const TabGrid& g, const TableWarpMem& m,
                                          int lane) {
   __syncwarp();
   const int N = (int)A.P.Npop;
-  const uint32_t* F = A.P.F;
-  const uint32_t FN = __ldg(F + N);
+  const uint32_t* F = g.F;
+  const uint32_t FN = F[N];
   const double scale = ldexp(1.0, A.P.fshift);
   const int Bfloor = (int)floor(-700.0 * scale);
   const int ncand = m.st->ncand;
@@ -241,7 +250,7 @@ static __device__ __noinline__ void table_flush(const TableGridArgs& A, const in
     if (q < ncand) {
       c = m.cand[q];
       int ci = c.x >> 16, cj = c.x & 0xffff;
-      iv = eval32_filtered(F, N, FN, sRow[ci + 1], __ldg(A.P.ncnt + cj), c.y, scale, B);
+      iv = eval32_filtered(F, N, FN, g.row[ci + 1], g.ncnt[cj], c.y, scale, B);
     }
     int h = iv.hi;
 #pragma unroll
@@ -257,7 +266,7 @@ static __device__ __noinline__ void table_flush(const TableGridArgs& A, const in
     if (nsurv + nk > kTableSurvCap) {
       __syncwarp();
       if (lane == 0) m.st->B = B;
-      table_refine(A, sRow, m, lane);
+      table_refine(A, g, m, lane);
       nsurv = 0;
     }
     if (keep) {
@@ -282,8 +291,8 @@ static __device__ __noinline__ void table_flush(const TableGridArgs& A, const in
 
 // Fixed-point lower bound of ln p for one cell from its counts alone.
 __device__ __forceinline__ int cell_lb(const uint32_t* F, int N, uint32_t FN, int K, int n, int k) {
-  const uint32_t Arow = __ldg(F + K) + __ldg(F + N - K) - FN;
-  const uint32_t Bcol = __ldg(F + n) + __ldg(F + N - n);
+  const uint32_t Arow = F[K] + F[N - K] - FN;
+  const uint32_t Bcol = F[n] + F[N - n];
   return lb_fix(F, K, N - K, Arow, (float)K, n, Bcol, (float)n * (1.0f / (float)N), k);
 }
 
@@ -293,17 +302,17 @@ __device__ __forceinline__ int cell_lb(const uint32_t* F, int N, uint32_t FN, in
 // partial-sum filter) in batches, B tightening as it goes.  The claim of
 // dto_grid.cuh applies unchanged: the FP64 argmin is among the hits and is
 // never filtered out.
-static __device__ __noinline__ void table_resolve(const TableGridArgs& A, const int* sRow,
+static __device__ __noinline__ void table_resolve(const TableGridArgs& A, const TabGrid& g,
                                                   const TableWarpMem& m, int lane, const int2* hb, int nh) {
   const int N = (int)A.P.Npop;
-  const uint32_t* F = A.P.F;
-  const uint32_t FN = __ldg(F + N);
+  const uint32_t* F = g.F;
+  const uint32_t FN = F[N];
   // seed: each lane's lowest-bound hit
   int bestLB = 0x7fffffff;
   int2 best = make_int2(0, 0);
   for (int q = lane; q < nh; q += 32) {
     const int2 h = hb[q];
-    const int lb = cell_lb(F, N, FN, sRow[(h.x >> 16) + 1], __ldg(A.P.ncnt + (h.x & 0xffff)), h.y);
+    const int lb = cell_lb(F, N, FN, g.row[(h.x >> 16) + 1], g.ncnt[h.x & 0xffff], h.y);
     if (lb < bestLB) {
       bestLB = lb;
       best = h;
@@ -317,7 +326,7 @@ static __device__ __noinline__ void table_resolve(const TableGridArgs& A, const 
     __syncwarp();
     if (lane == 0) m.st->ncand = __popc(msk);
     __syncwarp();
-    table_flush(A, sRow, m, lane);
+    table_flush(A, g, m, lane);
   }
   // every hit within the bound
   for (int q0 = 0; q0 < nh; q0 += 32) {
@@ -326,7 +335,7 @@ static __device__ __noinline__ void table_resolve(const TableGridArgs& A, const 
     bool keep = false;
     if (q < nh) {
       h = hb[q];
-      keep = cell_lb(F, N, FN, sRow[(h.x >> 16) + 1], __ldg(A.P.ncnt + (h.x & 0xffff)), h.y) <=
+      keep = cell_lb(F, N, FN, g.row[(h.x >> 16) + 1], g.ncnt[h.x & 0xffff], h.y) <=
              m.st->B + kScreenSlack + 1;
     }
     const unsigned msk = __ballot_sync(kFull, keep);
@@ -337,10 +346,10 @@ static __device__ __noinline__ void table_resolve(const TableGridArgs& A, const 
       __syncwarp();
       if (lane == 0) m.st->ncand = base + __popc(msk);
       __syncwarp();
-      if (m.st->ncand > kCandCap - 32) table_flush(A, sRow, m, lane);
+      if (m.st->ncand > kCandCap - 32) table_flush(A, g, m, lane);
     }
   }
-  if (m.st->ncand > 0) table_flush(A, sRow, m, lane);
+  if (m.st->ncand > 0) table_flush(A, g, m, lane);
 }
 
 template <int C, bool Packed>
@@ -356,11 +365,18 @@ __global__ void __launch_bounds__(kTableWarps * 32, kTableCtasPerSm) table_grid_
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int n1 = A.P.n1;
 
-  int* sRow = reinterpret_cast<int*>(smem_raw);
-  int* sWarp = sRow + ((n1 + 1 + 3) & ~3);
+  const int Npop = (int)A.P.Npop;
+  uint32_t* sF = reinterpret_cast<uint32_t*>(smem_raw);
+  int* sRow = reinterpret_cast<int*>(sF + (A.smemF ? ((Npop + 1 + 3) & ~3) : 0));
+  int* sNcnt = sRow + ((n1 + 1 + 3) & ~3);
+  int* sWarp = sNcnt + ((A.P.n2 + 3) & ~3);
   const TableWarpMem m = table_warp_mem(sWarp + warp * table_warp_ints(C), C);
   uint32_t* cw = reinterpret_cast<uint32_t*>(m.cnt);  // packed counters (16-byte aligned)
   for (int q = threadIdx.x; q <= n1; q += blockDim.x) sRow[q] = __ldg(A.P.rowstart + q);
+  for (int q = threadIdx.x; q < A.P.n2; q += blockDim.x) sNcnt[q] = __ldg(A.P.ncnt + q);
+  if (A.smemF)
+    for (int q = threadIdx.x; q <= Npop; q += blockDim.x) sF[q] = __ldg(A.P.F + q);
+  const TabGrid g{sRow, sNcnt, A.smemF ? sF : A.P.F};
   if (lane == 0) {
     m.st->n32 = 0;
     m.st->n64 = 0;
@@ -507,7 +523,7 @@ __global__ void __launch_bounds__(kTableWarps * 32, kTableCtasPerSm) table_grid_
       __syncwarp();
       if (m.st->nhits > A.hitcap - 32 * C) {
         // the buffer could overflow on the next row: resolve what it holds
-        table_resolve(A, sRow, m, lane, hb, m.st->nhits);
+        table_resolve(A, g, m, lane, hb, m.st->nhits);
         anyhits = true;
         __syncwarp();
         if (lane == 0) m.st->nhits = 0;
@@ -520,13 +536,13 @@ __global__ void __launch_bounds__(kTableWarps * 32, kTableCtasPerSm) table_grid_
     }
     __syncwarp();
     const int nh = m.st->nhits;
-    if (nh > 0) table_resolve(A, sRow, m, lane, hb, nh);
+    if (nh > 0) table_resolve(A, g, m, lane, hb, nh);
     if ((nh > 0 || anyhits) && m.st->B_valid) {
       if (isinf(m.st->bp)) {
         // no FP64 tail evaluated yet for this task: queue its survivors
-        table_defer(A, sRow, m, lane, b);
+        table_defer(A, g, m, lane, b);
       } else {
-        table_refine(A, sRow, m, lane);
+        table_refine(A, g, m, lane);
         if (lane == 0) A.out[b] = TaskResult{m.st->bp, m.st->bi, m.st->bj, m.st->bk, 0};
       }
     } else {
@@ -537,7 +553,7 @@ __global__ void __launch_bounds__(kTableWarps * 32, kTableCtasPerSm) table_grid_
     }
     __syncwarp();
   }
-  if (m.st->npend > 0) table_pending_flush(A, sRow, m, lane);
+  if (m.st->npend > 0) table_pending_flush(A, g, m, lane);
   if (lane == 0 && A.n_refined) {
     atomicAdd(A.n_refined, m.st->n64);
     atomicAdd(A.n_refined + 1, m.st->n32);
