@@ -433,7 +433,10 @@ int dto_optimize(dto_ctx* ctx, dto_pair* P, int permute, uint64_t seed, uint32_t
   if (rc) return rc;
   CK(cudaMemcpyAsync(L->hRes, L->dRes, sizeof(TaskResult), cudaMemcpyDeviceToHost, L->stream));
   CK(cudaStreamSynchronize(L->stream));
-  fill_result(P, ((TaskResult*)L->hRes)[0], permute ? 1 : 0, out);
+  const TaskResult r = ((TaskResult*)L->hRes)[0];
+  if (r.i < 0 || r.i >= (int)P->T1.size() || r.j < 0 || r.j >= (int)P->T2.size())
+    return set_err(ctx, DTO_ERR_CUDA, "dto_optimize: the search returned no grid cell");
+  fill_result(P, r, permute ? 1 : 0, out);
   return DTO_OK;
 }
 

@@ -118,6 +118,18 @@ struct ComposeArgs {
 #endif
 constexpr int kTableWarps = DTO_TABLE_WARPS;
 constexpr int kTableCtasPerSm = DTO_TABLE_MINB;
+// Tasks one warp of the table screen sweeps side by side (sharing the
+// table-row loads and the loop control, interleaving their dependent
+// instruction chains).  Two measured slower than one at N = 20,000 (1.72 M
+// against 2.04 M permutations/s: the two tasks' state does not fit 128
+// registers without spilling), so one is the default.  Each task has
+// kTableHitCap hit slots.
+#ifndef DTO_TABLE_TASKS
+#define DTO_TABLE_TASKS 1
+#endif
+constexpr int kTableTasks = DTO_TABLE_TASKS;
+static_assert(kTableTasks == 1 || kTableTasks == 2, "one or two tasks per warp");
+constexpr int kTableHitCap = 8192;
 
 // The packed table sweep holds overlaps in 16-bit halves and tests
 // k >= kthr as the sign bit of k + (0x8000 - kthr): it needs every overlap,

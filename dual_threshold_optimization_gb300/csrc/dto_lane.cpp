@@ -172,7 +172,7 @@ long long run_device_bytes(const dto_ctx* ctx, const dto_pair* P, int64_t n_perm
   long long b = first * xs * 2 + (long long)(batch + 1) * (long long)sizeof(TaskResult);  // first batch
   if (n_perm > 2048) {
     b += 2 * batch * (xs * 2 + (long long)sizeof(TaskResult) + 12);                          // two slots
-    b += 2LL * kTableCtasPerSm * ctx->nsm * kTableWarps * 8192 * 8;                           // hit buffers
+    b += 2LL * kTableCtasPerSm * ctx->nsm * kTableWarps * kTableHitCap * kTableTasks * 8;    // hit buffers
     b += 3LL * (long long)table_entries(P->C, P->dev.n1) * 2;                                 // table ladder
   }
   if (test_mode || !P->same_set) b += 2 * batch * L12 * 4;  // index scratch
@@ -242,7 +242,7 @@ int ensure_table(Lane* L, dto_pair* P, int level, int tau) {
 int table_levels(Lane* L, dto_pair* P, const int16_t* X, long long xstride, int ntask, TaskResult* dOut,
                  int lev_begin, int lev_end, int* fall, int* cnts, cudaStream_t stream, int hb) {
   const int cap = std::max(ntask, 1);
-  const int hitcap = 8192;
+  const int hitcap = kTableHitCap * kTableTasks;
   int rc = lane_grow(L, &L->dHits[hb], &L->hitBytes[hb], (size_t)kTableCtasPerSm * L->ctx->nsm * kTableWarps * hitcap * 8);
   if (rc) return rc;
   if (lev_begin == 0) LCK(cudaMemsetAsync(cnts, 0, 12 * sizeof(int), stream));
@@ -424,13 +424,24 @@ int lane_run_range(Lane* L, dto_pair* P, uint32_t perm_first, int64_t n_perm, ui
   // remaining batches.
   const long long first_batch = 1024;
   const bool use_table = (mode == kModeScreen) && n_perm > 2 * first_batch;
-  auto take = [&](const TaskResult* hr, long long b0, int cnt) {
+  // every task's result must name a grid cell: a result that does not is a
+  // device-side failure and is reported instead of read
+  const int nt1 = (int)P->T1.size(), nt2 = (int)P->T2.size();
+  auto valid = [&](const TaskResult& r) { return r.i >= 0 && r.i < nt1 && r.j >= 0 && r.j < nt2; };
+  auto take = [&](const TaskResult* hr, long long b0, int cnt) -> int {
     for (int q = 0; q < cnt; ++q) {
       const TaskResult& r = hr[q];
+      if (!valid(r)) {
+        char msg[160];
+        std::snprintf(msg, sizeof(msg), "permutation %lld: the search returned no grid cell",
+                      (long long)perm_first + b0 + q);
+        return lane_err(L, DTO_ERR_CUDA, msg);
+      }
       minp[(size_t)(b0 + q)] = r.p;
       if (out_minp) out_minp[b0 + q] = r.p;
       if (out_perm) fill_result(P, r, 1, &out_perm[b0 + q]);
     }
+    return DTO_OK;
   };
   auto upload_idx = [&](void** buf, size_t* cap, long long b0, int cnt, const int32_t** dI) -> int {
     *dI = nullptr;
@@ -468,7 +479,9 @@ int lane_run_range(Lane* L, dto_pair* P, uint32_t perm_first, int64_t n_perm, ui
       if (cnt > 0 && cudaEventElapsedTime(&ms, L->evk[0], L->evk[1]) == cudaSuccess) L->acc_perm_ms += ms;
       if (cudaEventElapsedTime(&ms, L->evk[2], L->evk[3]) == cudaSuccess) L->acc_grid_ms += ms;
       if (row0) unperm = hRes[0];
-      take(hRes + row0, b0, cnt);
+      if (row0 && !valid(hRes[0])) return lane_err(L, DTO_ERR_CUDA, "unpermuted task: the search returned no grid cell");
+      rc = take(hRes + row0, b0, cnt);
+      if (rc) return rc;
     }
   } else {
     // Slots left busy by a call that returned early hold nothing of this call.
@@ -533,7 +546,9 @@ int lane_run_range(Lane* L, dto_pair* P, uint32_t perm_first, int64_t n_perm, ui
       if (cudaEventElapsedTime(&ms, L->evk[2], L->evk[3]) == cudaSuccess) L->acc_grid_ms += ms;
     }
     unperm = hRes[0];
-    take(hRes + 1, 0, cnt0);
+    if (!valid(hRes[0])) return lane_err(L, DTO_ERR_CUDA, "unpermuted task: the search returned no grid cell");
+    rc = take(hRes + 1, 0, cnt0);
+    if (rc) return rc;
     std::vector<double> v(minp.begin(), minp.begin() + cnt0);
     std::sort(v.begin(), v.end());
     const double p90 = std::max(v[(size_t)(kLevel0Quantile * (double)(v.size() - 1))], 1e-300);
@@ -564,7 +579,8 @@ int lane_run_range(Lane* L, dto_pair* P, uint32_t perm_first, int64_t n_perm, ui
         L->acc_sweep0_tasks += sl.cnt;
       }
       if (cudaEventElapsedTime(&ms, sl.ev[4], sl.ev[5]) == cudaSuccess) L->acc_grid_ms += ms;
-      take((const TaskResult*)sl.hRes, sl.b0, sl.cnt);
+      const int trc = take((const TaskResult*)sl.hRes, sl.b0, sl.cnt);
+      if (trc) return trc;
       L->acc_d2h += (long long)sl.cnt * (long long)sizeof(TaskResult);
       sl.busy = false;
       return DTO_OK;

@@ -75,8 +75,9 @@ static __global__ void table_build_kernel(const TableArgs A) {
 constexpr int kTableSurvCap = 64;
 constexpr int kPend = 64;  // deferred FP64 evaluations per warp (several tasks)
 
-// Per-warp state of the current task, in shared memory: the hot sweep never
-// touches it; only the (rare) hit path and the task end do.
+// Per-task state in shared memory: the hot sweep never touches it; only the
+// hit path and the task end do.  n32, n64 and npend count for the whole warp
+// and live in the warp's first WarpTask (TableWarpMem::q).
 struct WarpTask {
   int B;        // running bound (fixed-point ln p)
   int B_valid;  // some cell's stage-2 upper bound reached B
@@ -89,9 +90,15 @@ struct WarpTask {
   int pad2;
 };
 
+// Shared memory of one warp: per task the column counters, the lane totals,
+// a WarpTask and the survivors (they outlive a chunked resolve, so each task
+// keeps its own); then the candidate and deferred-FP64 buffers, which hold
+// one task's entries at a time (candidates) or are tagged by task (FP64).
+__host__ __device__ constexpr int table_task_ints(int C) {
+  return grid_cnt_ints(C) + 32 + (int)(sizeof(WarpTask) / 4) + 3 * kTableSurvCap;
+}
 __host__ __device__ constexpr int table_warp_ints(int C) {
-  return grid_cnt_ints(C) + 32 + 2 * kCandCap + 3 * kTableSurvCap + (int)(sizeof(WarpTask) / 4) +
-         5 * kPend;
+  return kTableTasks * table_task_ints(C) + 2 * kCandCap + 5 * kPend;
 }
 
 struct TableWarpMem {
@@ -101,23 +108,27 @@ struct TableWarpMem {
   int* survCell;
   int* survK;
   int* survLo;
-  WarpTask* st;
+  WarpTask* st;   // this task
+  WarpTask* q;    // the warp's counters (n32, n64, npend)
   double* pendP;  // deferred FP64 queue: p, task, packed cell, overlap
   int* pendTask;
   int* pendCell;
   int* pendK;
 };
 
-__device__ __forceinline__ TableWarpMem table_warp_mem(int* base, int C) {
+__device__ __forceinline__ TableWarpMem table_warp_mem(int* base, int C, int t) {
   TableWarpMem m;
-  m.cnt = base;
-  m.tot = base + grid_cnt_ints(C);
-  m.cand = reinterpret_cast<int2*>(m.tot + 32);
-  m.survCell = reinterpret_cast<int*>(m.cand + kCandCap);
+  int* tb = base + t * table_task_ints(C);
+  m.cnt = tb;
+  m.tot = tb + grid_cnt_ints(C);
+  m.st = reinterpret_cast<WarpTask*>(m.tot + 32);
+  m.q = reinterpret_cast<WarpTask*>(base + grid_cnt_ints(C) + 32);
+  m.survCell = reinterpret_cast<int*>(m.st + 1);
   m.survK = m.survCell + kTableSurvCap;
   m.survLo = m.survK + kTableSurvCap;
-  m.st = reinterpret_cast<WarpTask*>(m.survLo + kTableSurvCap);
-  m.pendP = reinterpret_cast<double*>(m.st + 1);
+  int* sh = base + kTableTasks * table_task_ints(C);
+  m.cand = reinterpret_cast<int2*>(sh);
+  m.pendP = reinterpret_cast<double*>(m.cand + kCandCap);
   m.pendTask = reinterpret_cast<int*>(m.pendP + kPend);
   m.pendCell = m.pendTask + kPend;
   m.pendK = m.pendCell + kPend;
@@ -158,7 +169,7 @@ static __device__ __noinline__ void table_refine(const TableGridArgs& A, const T
     m.st->bi = lb.i;
     m.st->bj = lb.j;
     m.st->nsurv = 0;
-    m.st->n64 += (unsigned long long)done;
+    m.q->n64 += (unsigned long long)done;
   }
   __syncwarp();
 }
@@ -171,7 +182,7 @@ static __device__ __noinline__ void table_refine(const TableGridArgs& A, const T
 static __device__ __noinline__ void table_pending_flush(const TableGridArgs& A, const TabGrid& g,
                                                         const TableWarpMem& m, int lane) {
   __syncwarp();
-  const int np = m.st->npend;
+  const int np = m.q->npend;
   for (int q = lane; q < np; q += 32) {
     const int ci = m.pendCell[q] >> 16, cj = m.pendCell[q] & 0xffff;
     m.pendP[q] = sf64(A.P.LF, A.P.Npop, g.row[ci + 1], g.ncnt[cj], m.pendK[q]);
@@ -188,8 +199,8 @@ static __device__ __noinline__ void table_pending_flush(const TableGridArgs& A, 
   }
   __syncwarp();
   if (lane == 0) {
-    m.st->n64 += (unsigned long long)np;
-    m.st->npend = 0;
+    m.q->n64 += (unsigned long long)np;
+    m.q->npend = 0;
   }
   __syncwarp();
 }
@@ -201,8 +212,8 @@ static __device__ __noinline__ void table_defer(const TableGridArgs& A, const Ta
   __syncwarp();
   const int B = m.st->B;
   const int ns = m.st->nsurv;
-  if (m.st->npend + ns > kPend) table_pending_flush(A, g, m, lane);
-  int npend = m.st->npend;
+  if (m.q->npend + ns > kPend) table_pending_flush(A, g, m, lane);
+  int npend = m.q->npend;
   for (int q0 = 0; q0 < ns; q0 += 32) {
     const int q = q0 + lane;
     bool keep = q < ns && m.survLo[q] <= B + 1;
@@ -225,7 +236,7 @@ static __device__ __noinline__ void table_defer(const TableGridArgs& A, const Ta
   }
   __syncwarp();
   if (lane == 0) {
-    m.st->npend = npend;
+    m.q->npend = npend;
     m.st->nsurv = 0;
   }
   __syncwarp();
@@ -284,7 +295,7 @@ static __device__ __noinline__ void table_flush(const TableGridArgs& A, const Ta
     m.st->B = B;
     m.st->B_valid = B_valid;
     m.st->ncand = 0;
-    m.st->n32 += (unsigned long long)ncand;
+    m.q->n32 += (unsigned long long)ncand;
   }
   __syncwarp();
 }
@@ -354,6 +365,7 @@ static __device__ __noinline__ void table_resolve(const TableGridArgs& A, const 
 
 template <int C, bool Packed>
 __global__ void __launch_bounds__(kTableWarps * 32, kTableCtasPerSm) table_grid_kernel(const TableGridArgs A) {
+  constexpr int T = kTableTasks;
   constexpr int Cp = C | 1;
   constexpr int Cq = table_cq(C);
   constexpr int NQ = Cq / 8;  // 16-byte table chunks per lane per row
@@ -370,193 +382,248 @@ __global__ void __launch_bounds__(kTableWarps * 32, kTableCtasPerSm) table_grid_
   int* sRow = reinterpret_cast<int*>(sF + (A.smemF ? ((Npop + 1 + 3) & ~3) : 0));
   int* sNcnt = sRow + ((n1 + 1 + 3) & ~3);
   int* sWarp = sNcnt + ((A.P.n2 + 3) & ~3);
-  const TableWarpMem m = table_warp_mem(sWarp + warp * table_warp_ints(C), C);
-  uint32_t* cw = reinterpret_cast<uint32_t*>(m.cnt);  // packed counters (16-byte aligned)
+  // per task t: counters at wb + t * TTI, lane totals GCI further, then its WarpTask
+  int* const wb = sWarp + warp * table_warp_ints(C);
+  constexpr int TTI = table_task_ints(C), GCI = grid_cnt_ints(C);
+  auto cnt_of = [&](int t) { return wb + t * TTI; };
+  auto tot_of = [&](int t) { return wb + t * TTI + GCI; };
+  auto st_of = [&](int t) { return reinterpret_cast<WarpTask*>(wb + t * TTI + GCI + 32); };
   for (int q = threadIdx.x; q <= n1; q += blockDim.x) sRow[q] = __ldg(A.P.rowstart + q);
   for (int q = threadIdx.x; q < A.P.n2; q += blockDim.x) sNcnt[q] = __ldg(A.P.ncnt + q);
   if (A.smemF)
     for (int q = threadIdx.x; q <= Npop; q += blockDim.x) sF[q] = __ldg(A.P.F + q);
   const TabGrid g{sRow, sNcnt, A.smemF ? sF : A.P.F};
   if (lane == 0) {
-    m.st->n32 = 0;
-    m.st->n64 = 0;
-    m.st->npend = 0;
+    st_of(0)->n32 = 0;
+    st_of(0)->n64 = 0;
+    st_of(0)->npend = 0;
   }
   __syncthreads();
   const uint4* ktab = reinterpret_cast<const uint4*>(A.kthr);
-  int2* hb = A.hitbuf + (size_t)(blockIdx.x * kTableWarps + warp) * A.hitcap;
+  // the warp's hit buffer, split between its tasks
+  const int hcap = A.hitcap / T;
+  int2* hbw = A.hitbuf + (size_t)(blockIdx.x * kTableWarps + warp) * A.hitcap;
   unsigned long long nfall = 0;
 
   const int ntask = A.ntask_dev ? *((volatile const int*)A.ntask_dev) : A.ntask;
   for (;;) {
-    int b = 0;
-    if (lane == 0) b = atomicAdd(A.work, 1);
-    b = __shfl_sync(kFull, b, 0);
-    if (b >= ntask) break;
-    if (A.task_list) b = A.task_list[b];
-    const int16_t* x = A.X + (long long)b * A.xstride;
-    if (lane == 0) {
-      m.st->B = A.tau;
-      m.st->B_valid = 0;
-      m.st->ncand = 0;
-      m.st->nsurv = 0;
-      m.st->nhits = 0;
-      Best z = best_init();
-      m.st->bp = z.p;
-      m.st->bk = z.k;
-      m.st->bi = z.i;
-      m.st->bj = z.j;
+    int b0 = 0;
+    if (lane == 0) b0 = atomicAdd(A.work, T);
+    b0 = __shfl_sync(kFull, b0, 0);
+    if (b0 >= ntask) break;
+    // tasks b0 .. b0+T-1 (those below ntask); a missing task sweeps nothing
+    int bt[T];
+    bool live[T];
+    const int* x32[T];
+#pragma unroll
+    for (int t = 0; t < T; ++t) {
+      live[t] = b0 + t < ntask;
+      bt[t] = live[t] ? (A.task_list ? A.task_list[b0 + t] : b0 + t) : -1;
+      x32[t] = reinterpret_cast<const int*>(A.X + (long long)(live[t] ? bt[t] : 0) * A.xstride);
+      if (lane == 0) {
+        WarpTask* st = st_of(t);
+        st->B = A.tau;
+        st->B_valid = 0;
+        st->ncand = 0;
+        st->nsurv = 0;
+        st->nhits = 0;
+        Best z = best_init();
+        st->bp = z.p;
+        st->bk = z.k;
+        st->bi = z.i;
+        st->bj = z.j;
+      }
+      for (int q = lane; q < 32 * Cp; q += 32) cnt_of(t)[q] = 0;
+      tot_of(t)[lane] = 0;
     }
-    for (int q = lane; q < 32 * Cp; q += 32) m.cnt[q] = 0;
-    m.tot[lane] = 0;
     __syncwarp();
     // Labels are read as 32-bit words (two labels each); a row's words are
-    // prefetched one row ahead, 64 words (128 labels) per warp.  X rows start
-    // 16-byte aligned and are padded to a multiple of 8 labels.
-    const int* x32 = reinterpret_cast<const int*>(x);
+    // prefetched one row ahead, 64 words (128 labels) per warp and task.  X
+    // rows start 16-byte aligned and are padded to a multiple of 8 labels.
     int s = sRow[0], e = sRow[1];
-    int w0, w1;
-    {
-      const int q0 = (s >> 1) + lane;
-      w0 = (2 * q0 < e) ? __ldg(x32 + q0) : -1;
-      w1 = (2 * (q0 + 32) < e) ? __ldg(x32 + q0 + 32) : -1;
-    }
-    bool anyhits = false;
-    uint4 kt[NQ], ktn[NQ];
+    int w0[T], w1[T];
 #pragma unroll
-    for (int u = 0; u < NQ; ++u) kt[u] = __ldg(ktab + (size_t)u * 32 + lane);
+    for (int t = 0; t < T; ++t) {
+      const int q0 = (s >> 1) + lane;
+      w0[t] = (live[t] && 2 * q0 < e) ? __ldg(x32[t] + q0) : -1;
+      w1[t] = (live[t] && 2 * (q0 + 32) < e) ? __ldg(x32[t] + q0 + 32) : -1;
+    }
+    bool anyhits[T];
+#pragma unroll
+    for (int t = 0; t < T; ++t) anyhits[t] = false;
+    uint4 kt[NQ];
     // a label is the counter slot lane * Cp + t of its column lane * C + t
-    auto add_lab = [&](int lab) {
+    auto add_lab = [&](int t, int lab) {
       const int l = lab / Cp;
       if (Packed) {
-        const int t = lab - l * Cp;
-        atomicAdd(&cw[l * Wp + (t >> 1)], 1u << ((t & 1) << 4));
+        const int tc = lab - l * Cp;
+        atomicAdd(reinterpret_cast<uint32_t*>(cnt_of(t)) + l * Wp + (tc >> 1), 1u << ((tc & 1) << 4));
       } else {
-        atomicAdd(&m.cnt[lab], 1);
+        atomicAdd(&cnt_of(t)[lab], 1);
       }
-      atomicAdd(&m.tot[l], 1);
+      atomicAdd(&tot_of(t)[l], 1);
     };
-    auto add_word = [&](int w, int q, int rs, int re) {
+    auto add_word = [&](int t, int w, int q, int rs, int re) {
       const int p = 2 * q;
       const int lab0 = (int)(short)(w & 0xffff), lab1 = w >> 16;  // sign-extended labels
-      if (p >= rs && p < re && lab0 >= 0) add_lab(lab0);
-      if (p + 1 >= rs && p + 1 < re && lab1 >= 0) add_lab(lab1);
+      if (p >= rs && p < re && lab0 >= 0) add_lab(t, lab0);
+      if (p + 1 >= rs && p + 1 < re && lab1 >= 0) add_lab(t, lab1);
     };
-    auto push_hit = [&](int i, int t, int k) {
-      const int pos = atomicAdd(&m.st->nhits, 1);
-      if (pos < A.hitcap) hb[pos] = make_int2((i << 16) | (lane * C + t), k);
+    auto push_hit = [&](int t, int i, int tcol, int k) {
+      const int pos = atomicAdd(&st_of(t)->nhits, 1);
+      if (pos < hcap) hbw[t * hcap + pos] = make_int2((i << 16) | (lane * C + tcol), k);
     };
     for (int i = 0; i < n1; ++i) {
-      const int c0 = w0, c1 = w1;
+      int c0[T], c1[T];
       const int sN = e;
       const int eN = (i + 2 <= n1) ? sRow[i + 2] : e;
-      {
-        const int q0 = (sN >> 1) + lane;
-        w0 = (2 * q0 < eN) ? __ldg(x32 + q0) : -1;
-        w1 = (2 * (q0 + 32) < eN) ? __ldg(x32 + q0 + 32) : -1;
-      }
-      if (i + 1 < n1) {
 #pragma unroll
-        for (int u = 0; u < NQ; ++u) ktn[u] = __ldg(ktab + ((size_t)(i + 1) * NQ + u) * 32 + lane);
+      for (int t = 0; t < T; ++t) {
+        c0[t] = w0[t];
+        c1[t] = w1[t];
+        const int q0 = (sN >> 1) + lane;
+        w0[t] = (live[t] && 2 * q0 < eN) ? __ldg(x32[t] + q0) : -1;
+        w1[t] = (live[t] && 2 * (q0 + 32) < eN) ? __ldg(x32[t] + q0 + 32) : -1;
       }
-      {
+      // this row's table chunks: consumed after the label updates and the scan
+#pragma unroll
+      for (int u = 0; u < NQ; ++u) kt[u] = __ldg(ktab + ((size_t)i * NQ + u) * 32 + lane);
+#pragma unroll
+      for (int t = 0; t < T; ++t) {
         const int q0 = (s >> 1) + lane;
-        add_word(c0, q0, s, e);
-        add_word(c1, q0 + 32, s, e);
-        for (int q = q0 + 64; 2 * q < e; q += 32) add_word(__ldg(x32 + q), q, s, e);
+        add_word(t, c0[t], q0, s, e);
+        add_word(t, c1[t], q0 + 32, s, e);
+        if (live[t])
+          for (int q = q0 + 64; 2 * q < e; q += 32) add_word(t, __ldg(x32[t] + q), q, s, e);
       }
       __syncwarp();
-      const int mine = m.tot[lane];
-      int incl = mine;
+      int excl[T];
 #pragma unroll
-      for (int d = 1; d < 32; d <<= 1) {
-        int y = __shfl_up_sync(kFull, incl, d);
-        if (lane >= d) incl += y;
+      for (int t = 0; t < T; ++t) {
+        const int mine = tot_of(t)[lane];
+        int incl = mine;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+          int y = __shfl_up_sync(kFull, incl, d);
+          if (lane >= d) incl += y;
+        }
+        excl[t] = incl - mine;  // overlap before this lane's first column
       }
       if (Packed) {
         // y[w] = (overlap of column 2w+1) << 16 | (overlap of column 2w);
         // R carries the running overlap in both halves
-        uint32_t R = (uint32_t)(incl - mine) * 0x10001u;
-        uint32_t y[NW];
-        uint32_t acc = 0;
+        uint32_t acc[T];
+        uint32_t R[T];
+#pragma unroll
+        for (int t = 0; t < T; ++t) {
+          R[t] = (uint32_t)excl[t] * 0x10001u;
+          acc[t] = 0;
+        }
 #pragma unroll
         for (int u = 0; u < NQ; ++u) {
-          const uint4 c4 = *reinterpret_cast<const uint4*>(cw + lane * Wp + 4 * u);
-          const uint32_t cv[4] = {c4.x, c4.y, c4.z, c4.w};
+          uint4 c4[T];
+#pragma unroll
+          for (int t = 0; t < T; ++t)
+            c4[t] = *reinterpret_cast<const uint4*>(reinterpret_cast<const uint32_t*>(cnt_of(t)) + lane * Wp + 4 * u);
           const uint32_t tv[4] = {kt[u].x, kt[u].y, kt[u].z, kt[u].w};
 #pragma unroll
           for (int c = 0; c < 4; ++c) {
             if (4 * u + c < NW) {
-              const uint32_t v = cv[c] * 0x10001u + R;
-              y[4 * u + c] = v;
-              R = __byte_perm(v, 0, 0x3232);
-              acc |= v + tv[c];
+#pragma unroll
+              for (int t = 0; t < T; ++t) {
+                const uint32_t cv = (c == 0) ? c4[t].x : (c == 1) ? c4[t].y : (c == 2) ? c4[t].z : c4[t].w;
+                const uint32_t v = cv * 0x10001u + R[t];
+                R[t] = __byte_perm(v, 0, 0x3232);
+                acc[t] |= v + tv[c];
+              }
             }
           }
         }
-        if (acc & 0x80008000u) {
 #pragma unroll
-          for (int u = 0; u < NQ; ++u) {
-            const uint32_t tv[4] = {kt[u].x, kt[u].y, kt[u].z, kt[u].w};
+        for (int t = 0; t < T; ++t) {
+          if (acc[t] & 0x80008000u) {
+            // a hit in this lane's columns: redo the chain and record the cells
+            uint32_t Rh = (uint32_t)excl[t] * 0x10001u;
 #pragma unroll
-            for (int c = 0; c < 4; ++c) {
-              if (4 * u + c < NW) {
-                const int w = 4 * u + c;
-                const uint32_t d = y[w] + tv[c];
-                if (d & 0x8000u) push_hit(i, 2 * w, (int)(y[w] & 0xFFFFu));
-                if (d & 0x80000000u) push_hit(i, 2 * w + 1, (int)(y[w] >> 16));
+            for (int u = 0; u < NQ; ++u) {
+              const uint4 c4 = *reinterpret_cast<const uint4*>(reinterpret_cast<const uint32_t*>(cnt_of(t)) + lane * Wp + 4 * u);
+              const uint32_t cvs[4] = {c4.x, c4.y, c4.z, c4.w};
+              const uint32_t tv[4] = {kt[u].x, kt[u].y, kt[u].z, kt[u].w};
+#pragma unroll
+              for (int c = 0; c < 4; ++c) {
+                if (4 * u + c < NW) {
+                  const int w = 4 * u + c;
+                  const uint32_t v = cvs[c] * 0x10001u + Rh;
+                  Rh = __byte_perm(v, 0, 0x3232);
+                  const uint32_t d = v + tv[c];
+                  if (d & 0x8000u) push_hit(t, i, 2 * w, (int)(v & 0xFFFFu));
+                  if (d & 0x80000000u) push_hit(t, i, 2 * w + 1, (int)(v >> 16));
+                }
               }
             }
           }
         }
       } else {
-        int k = incl - mine;  // overlap before this lane's first column
 #pragma unroll
-        for (int t = 0; t < C; ++t) {
-          k += m.cnt[lane * Cp + t];
-          const uint4 v = kt[t / 8];
-          const uint32_t w = ((t % 8) / 2 == 0) ? v.x : ((t % 8) / 2 == 1) ? v.y : ((t % 8) / 2 == 2) ? v.z : v.w;
-          const int thr = (t & 1) ? (int)(w >> 16) : (int)(w & 0xFFFFu);
-          if (k >= thr) push_hit(i, t, k);  // columns past n2 hold 0xFFFF, above any overlap
+        for (int t = 0; t < T; ++t) {
+          int k = excl[t];
+#pragma unroll
+          for (int tc = 0; tc < C; ++tc) {
+            k += cnt_of(t)[lane * Cp + tc];
+            const uint4 v = kt[tc / 8];
+            const uint32_t w = ((tc % 8) / 2 == 0) ? v.x : ((tc % 8) / 2 == 1) ? v.y : ((tc % 8) / 2 == 2) ? v.z : v.w;
+            const int thr = (tc & 1) ? (int)(w >> 16) : (int)(w & 0xFFFFu);
+            if (k >= thr) push_hit(t, i, tc, k);  // columns past n2 hold 0xFFFF, above any overlap
+          }
         }
       }
+      // the next row's counter updates wait for every lane's reads of this row
       __syncwarp();
-      if (m.st->nhits > A.hitcap - 32 * C) {
-        // the buffer could overflow on the next row: resolve what it holds
-        table_resolve(A, g, m, lane, hb, m.st->nhits);
-        anyhits = true;
-        __syncwarp();
-        if (lane == 0) m.st->nhits = 0;
-        __syncwarp();
-      }
+      // every fourth row: could a task's buffer overflow within the next four
+      // rows?  Then resolve what it holds (hcap leaves room for four full rows).
+      if ((i & 3) == 3) {
 #pragma unroll
-      for (int u = 0; u < NQ; ++u) kt[u] = ktn[u];
+        for (int t = 0; t < T; ++t) {
+          if (st_of(t)->nhits > hcap - 4 * 32 * C) {
+            table_resolve(A, g, table_warp_mem(wb, C, t), lane, hbw + t * hcap, st_of(t)->nhits);
+            anyhits[t] = true;
+            __syncwarp();
+            if (lane == 0) st_of(t)->nhits = 0;
+            __syncwarp();
+          }
+        }
+      }
       s = sN;
       e = eN;
     }
     __syncwarp();
-    const int nh = m.st->nhits;
-    if (nh > 0) table_resolve(A, g, m, lane, hb, nh);
-    if ((nh > 0 || anyhits) && m.st->B_valid) {
-      if (isinf(m.st->bp)) {
-        // no FP64 tail evaluated yet for this task: queue its survivors
-        table_defer(A, g, m, lane, b);
+#pragma unroll
+    for (int t = 0; t < T; ++t) {
+      if (!live[t]) continue;
+      const TableWarpMem mt = table_warp_mem(wb, C, t);
+      const int nh = mt.st->nhits;
+      if (nh > 0) table_resolve(A, g, mt, lane, hbw + t * hcap, nh);
+      if ((nh > 0 || anyhits[t]) && mt.st->B_valid) {
+        if (isinf(mt.st->bp)) {
+          // no FP64 tail evaluated yet for this task: queue its survivors
+          table_defer(A, g, mt, lane, bt[t]);
+        } else {
+          table_refine(A, g, mt, lane);
+          if (lane == 0) A.out[bt[t]] = TaskResult{mt.st->bp, mt.st->bi, mt.st->bj, mt.st->bk, 0};
+        }
       } else {
-        table_refine(A, g, m, lane);
-        if (lane == 0) A.out[b] = TaskResult{m.st->bp, m.st->bi, m.st->bj, m.st->bk, 0};
+        // no cell reaches the guess: the next level (or the exhaustive
+        // screen) takes the task
+        if (lane == 0) A.fallback[atomicAdd(A.nfallback, 1)] = bt[t];
+        ++nfall;
       }
-    } else {
-      // no cell reaches the guess: the next level (or the exhaustive
-      // screen) takes the task
-      if (lane == 0) A.fallback[atomicAdd(A.nfallback, 1)] = b;
-      ++nfall;
+      __syncwarp();
     }
-    __syncwarp();
   }
-  if (m.st->npend > 0) table_pending_flush(A, g, m, lane);
+  if (st_of(0)->npend > 0) table_pending_flush(A, g, table_warp_mem(wb, C, 0), lane);
   if (lane == 0 && A.n_refined) {
-    atomicAdd(A.n_refined, m.st->n64);
-    atomicAdd(A.n_refined + 1, m.st->n32);
+    atomicAdd(A.n_refined, st_of(0)->n64);
+    atomicAdd(A.n_refined + 1, st_of(0)->n32);
     atomicAdd(A.n_refined + 2, nfall);
   }
 }
