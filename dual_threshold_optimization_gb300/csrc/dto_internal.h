@@ -24,6 +24,16 @@ static_assert(kBuckets % kPermThreads == 0 && kPermThreads % 32 == 0 && kPermThr
 // Longest list whose Philox words the permutation kernel keeps in shared
 // memory (4 + 2 bytes an element + the counters: 208 KB at 32,768).
 constexpr int kPermWordsMaxL = 32768;
+// Shared-memory budget of the permutation kernel: the label table Ylab is
+// staged there (random 2-byte gathers hit shared-memory banks instead of L1
+// sectors) when it fits beside the counters, the words and the indices.
+constexpr size_t kPermSmemBudget = 227 * 1024;
+__host__ __device__ constexpr size_t perm_base_smem(int L) {
+  return (size_t)kBuckets * 4 + (L <= kPermWordsMaxL ? (size_t)L * 4 : 0) + (((size_t)L * 2 + 15) & ~(size_t)15);
+}
+__host__ __device__ constexpr bool perm_stage_ylab(int L) {
+  return perm_base_smem(L) + (((size_t)L * 2 + 15) & ~(size_t)15) <= kPermSmemBudget;
+}
 constexpr int kMaxListLen = 65534;   // positions are uint16; overlaps stay below the 0xFFFF "never" mark
 constexpr int kScreenSlack = 5;      // fixed-point units added to the screen threshold
 constexpr int kSurvCap = 256;        // per-warp survivors of the FP32 stage

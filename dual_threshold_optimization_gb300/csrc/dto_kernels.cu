@@ -77,7 +77,8 @@ __device__ __forceinline__ uint32_t bucket_of(uint4 w, int q) {
 // lengths of interest, so the per-bucket canonical sort and Fisher-Yates are
 // a few operations per element.
 template <bool kWords>
-__device__ __forceinline__ void perm_body(const PermArgs& A, int* cnt, uint16_t* sA, uint32_t* sW) {
+__device__ __forceinline__ void perm_body(const PermArgs& A, int* cnt, uint16_t* sA, uint32_t* sW,
+                                          int16_t* sY) {
   __shared__ int warpTot[kPermThreads / 32];
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int L = A.L;
@@ -95,6 +96,8 @@ __device__ __forceinline__ void perm_body(const PermArgs& A, int* cnt, uint16_t*
   };
 
   for (int b = tid; b < kBuckets; b += kPermThreads) cnt[b] = 0;
+  if (sY)
+    for (int q = tid; q < L; q += kPermThreads) sY[q] = __ldg(A.Ylab + q);
   __syncthreads();
   const int groups = (L + 3) >> 2;
   for (int g = tid; g < groups; g += kPermThreads) {
@@ -199,7 +202,10 @@ __device__ __forceinline__ void perm_body(const PermArgs& A, int* cnt, uint16_t*
   __syncthreads();
   if (A.X) {
     int16_t* xo = A.X + (long long)blockIdx.x * A.xstride;
-    for (int p = tid; p < L; p += kPermThreads) xo[p] = __ldg(A.Ylab + sA[p]);
+    if (sY)
+      for (int p = tid; p < L; p += kPermThreads) xo[p] = sY[sA[p]];
+    else
+      for (int p = tid; p < L; p += kPermThreads) xo[p] = __ldg(A.Ylab + sA[p]);
   }
   if (A.sigma) {
     int* so = A.sigma + (long long)blockIdx.x * A.sstride;
@@ -210,11 +216,14 @@ __device__ __forceinline__ void perm_body(const PermArgs& A, int* cnt, uint16_t*
 __global__ void __launch_bounds__(kPermThreads) perm_kernel(const PermArgs A) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   int* cnt = reinterpret_cast<int*>(smem_raw);
+  int16_t* sY = (A.X && perm_stage_ylab(A.L))
+                    ? reinterpret_cast<int16_t*>(smem_raw + perm_base_smem(A.L))
+                    : nullptr;
   if (A.L <= kPermWordsMaxL) {
     uint32_t* sW = reinterpret_cast<uint32_t*>(cnt + kBuckets);
-    perm_body<true>(A, cnt, reinterpret_cast<uint16_t*>(sW + A.L), sW);
+    perm_body<true>(A, cnt, reinterpret_cast<uint16_t*>(sW + A.L), sW, sY);
   } else {
-    perm_body<false>(A, cnt, reinterpret_cast<uint16_t*>(cnt + kBuckets), nullptr);
+    perm_body<false>(A, cnt, reinterpret_cast<uint16_t*>(cnt + kBuckets), nullptr, sY);
   }
 }
 
@@ -312,8 +321,7 @@ cudaError_t raise_smem_limit(const void* kernel, size_t bytes) {
 
 cudaError_t launch_perm(const PermArgs& a, int count, cudaStream_t s) {
   if (count <= 0) return cudaSuccess;
-  size_t smem = (size_t)kBuckets * 4 + (a.L <= kPermWordsMaxL ? (size_t)a.L * 4 : 0) +
-                (((size_t)a.L * 2 + 15) & ~(size_t)15);
+  size_t smem = perm_base_smem(a.L) + ((a.X && perm_stage_ylab(a.L)) ? (((size_t)a.L * 2 + 15) & ~(size_t)15) : 0);
   cudaError_t e = raise_smem_limit((const void*)perm_kernel, smem);
   if (e != cudaSuccess) return e;
   perm_kernel<<<count, kPermThreads, smem, s>>>(a);
