@@ -353,14 +353,35 @@ __global__ void __launch_bounds__(kGridWarps * 32, 1) grid_kernel(const GridArgs
   const uint32_t FN = F[N];
   unsigned long long n32 = 0, n64 = 0, nfall = 0;  // stage-2, FP64 evaluations, fallbacks
 
+  // Cooperative screen: the CTA's warps share one task.  Every warp sweeps
+  // all rows (the counters need every label) but evaluates only the cells of
+  // rows i with i % kGridWarps == warp, and the bound B is shared through
+  // shared memory; the warps' optima are reduced at the end.  This cuts the
+  // latency of hard tasks (a flat landscape sends most cells to stage 2).
+  static_assert(kGridWarps <= 32, "one lane per warp in the cooperative reduction");
+  const bool coop = A.coop != 0 && A.mode == kModeScreen;
+  __shared__ int sTask, sB;
+  __shared__ double sBestP[kGridWarps];
+  __shared__ int sBestK[kGridWarps], sBestI[kGridWarps], sBestJ[kGridWarps];
   const int ntask = A.ntask_dev ? *((volatile const int*)A.ntask_dev) : A.ntask;
   for (;;) {
     int b = 0;
-    if (lane == 0) b = atomicAdd(A.work, 1);
-    b = __shfl_sync(kFull, b, 0);
+    if (coop) {
+      __syncthreads();  // the previous task is finished by every warp
+      if (threadIdx.x == 0) {
+        sTask = atomicAdd(A.work, 1);
+        sB = kScreenSlack;
+      }
+      __syncthreads();
+      b = sTask;
+    } else {
+      if (lane == 0) b = atomicAdd(A.work, 1);
+      b = __shfl_sync(kFull, b, 0);
+    }
     if (b >= ntask) break;
     if (A.task_list) b = A.task_list[b];
     const int16_t* x = A.X + (long long)b * A.xstride;
+    auto my_row = [&](int i) { return !coop || i % kGridWarps == warp; };
 
     if (A.mode == kModeFull64 || A.mode == kModeDump) {
       Best best = best_init();
@@ -455,6 +476,11 @@ __global__ void __launch_bounds__(kGridWarps * 32, 1) grid_kernel(const GridArgs
           B = max(h, Bfloor);
           B_valid = true;
         }
+        if (coop) {
+          // any warp's bound is attained by a cell of this task: take the least
+          if (lane == 0) atomicMin(&sB, B);
+          B = min(B, *((volatile int*)&sB));
+        }
         bool keep = (q < ncand) && iv.lo <= B + 1;
         unsigned m = __ballot_sync(kFull, keep);
         int nk = __popc(m);
@@ -478,6 +504,7 @@ __global__ void __launch_bounds__(kGridWarps * 32, 1) grid_kernel(const GridArgs
     // One sweep: cells with LB <= B + slack go to stage 2 (B only decreases).
     auto candidate_sweep = [&]() {
       sweep<C>(x, sRow, n1, cnt, lane, [&](int i, const int (&O)[C], int excl) {
+        if (!my_row(i)) return;
         const int K = sRow[i + 1];
         const int NK = N - K;
         const uint32_t Arow = F[K] + F[NK] - FN;
@@ -531,7 +558,7 @@ __global__ void __launch_bounds__(kGridWarps * 32, 1) grid_kernel(const GridArgs
     // so ties at 0) are kept too.
     bool done = false;
     int guess = kNoGuess;
-    if (A.guess_hist != nullptr) {
+    if (A.guess_hist != nullptr && !coop) {
       int gq = bound_guess_bin(A.guess_hist, lane);
       if (gq >= 0) guess = max((int)floor(-0.25 * (double)gq * scale), Bfloor);
     }
@@ -550,6 +577,7 @@ __global__ void __launch_bounds__(kGridWarps * 32, 1) grid_kernel(const GridArgs
       // bound seeds B
       int bestLB = 0x7fffffff, bestCell = -1, bestK = 0;
       sweep<C>(x, sRow, n1, cnt, lane, [&](int i, const int (&O)[C], int excl) {
+        if (!my_row(i)) return;
         const int K = sRow[i + 1];
         const int NK = N - K;
         const uint32_t Arow = F[K] + F[NK] - FN;
@@ -574,10 +602,35 @@ __global__ void __launch_bounds__(kGridWarps * 32, 1) grid_kernel(const GridArgs
 #pragma unroll
       for (int d = 16; d > 0; d >>= 1) B = min(B, __shfl_xor_sync(kFull, B, d));
       B = max(B, Bfloor);
+      if (coop) {
+        if (lane == 0) atomicMin(&sB, B);
+        __syncthreads();
+        B = sB;
+      }
       B_valid = true;
       candidate_sweep();
     }
+    if (coop) {
+      __syncthreads();  // every warp's stage 2 is done: sB is the task's bound
+      B = min(B, sB);
+    }
     refine_survivors();
+    if (coop) {
+      if (lane == 0) {
+        sBestP[warp] = best64.p;
+        sBestK[warp] = best64.k;
+        sBestI[warp] = best64.i;
+        sBestJ[warp] = best64.j;
+      }
+      __syncthreads();
+      if (warp == 0) {
+        Best bb = best_init();
+        if (lane < kGridWarps) bb = Best{sBestP[lane], sBestK[lane], sBestI[lane], sBestJ[lane]};
+        warp_best(bb);
+        if (lane == 0) A.out[b] = TaskResult{bb.p, bb.i, bb.j, bb.k, 0};
+      }
+      continue;
+    }
     if (A.guess_hist != nullptr && lane == 0) bound_record(A.guess_hist, B, scale);
     if (lane == 0) A.out[b] = TaskResult{best64.p, best64.i, best64.j, best64.k, 0};
   }

@@ -148,7 +148,7 @@ void fill_result(const dto_pair* P, const TaskResult& r, int permuted, dto_resul
 // One task per launch through the exhaustive screen (or FP64 / dump modes).
 int lane_grid_tasks(Lane* L, dto_pair* P, const int16_t* dX, long long xstride, int ntask, int mode,
                     TaskResult* dOut, int* dumpK = nullptr, double* dumpP = nullptr, bool guess = false,
-                    cudaStream_t stream = nullptr);
+                    cudaStream_t stream = nullptr, bool coop = false);
 // Labels of `count` permutations from perm id `first` (or of uploaded index
 // rows dIdx) into L->dX from row `row0`.
 int lane_make_labels(Lane* L, dto_pair* P, uint64_t seed, uint32_t first, int count, const int32_t* dIdx,

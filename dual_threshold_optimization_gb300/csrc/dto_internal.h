@@ -80,6 +80,7 @@ struct GridArgs {
   int ntask;
   int mode;
   int smemF;             // 1: the fixed-point table is staged in shared memory
+  int coop;              // screen mode: the CTA's warps share each task
   TaskResult* out;       // [ntask]
   int* work;             // task counter (zeroed before the launch)
   unsigned long long* n_refined;  // [3]: FP64 tails, FP32 tails, speculative sweeps rejected

@@ -24,6 +24,16 @@ namespace dto {
 #define DTO_L0_QUANTILE 0.90
 #endif
 constexpr double kLevel0Quantile = DTO_L0_QUANTILE;
+// Permutations of the first batch, whose minimum p-values set the ladder.
+#ifndef DTO_FIRST_BATCH
+#define DTO_FIRST_BATCH 1024
+#endif
+constexpr long long kFirstBatch = DTO_FIRST_BATCH;
+// The first batch's screen with a CTA per task (see grid_kernel).
+#ifndef DTO_FIRST_COOP
+#define DTO_FIRST_COOP 1
+#endif
+constexpr bool kFirstBatchCoop = DTO_FIRST_COOP != 0;
 
 int set_err(dto_ctx* ctx, int code, const std::string& msg) {
   if (ctx) ctx->err = msg;
@@ -180,7 +190,7 @@ long long run_device_bytes(const dto_ctx* ctx, const dto_pair* P, int64_t n_perm
 }
 
 int lane_grid_tasks(Lane* L, dto_pair* P, const int16_t* dX, long long xstride, int ntask, int mode,
-                    TaskResult* dOut, int* dumpK, double* dumpP, bool guess, cudaStream_t stream) {
+                    TaskResult* dOut, int* dumpK, double* dumpP, bool guess, cudaStream_t stream, bool coop) {
   if (!stream) stream = L->stream;
   GridArgs a{};
   a.P = P->dev;
@@ -197,8 +207,9 @@ int lane_grid_tasks(Lane* L, dto_pair* P, const int16_t* dX, long long xstride, 
   a.guess_hist = (guess && mode == kModeScreen) ? L->dGuess : nullptr;
   a.dump_k = dumpK;
   a.dump_p = dumpP;
+  a.coop = (coop && mode == kModeScreen) ? 1 : 0;
   LCK(cudaMemsetAsync(L->dWork, 0, sizeof(int), stream));
-  int ctas = std::min(L->ctx->nsm, (ntask + kGridWarps - 1) / kGridWarps);
+  int ctas = std::min(L->ctx->nsm, a.coop ? ntask : (ntask + kGridWarps - 1) / kGridWarps);
   ctas = std::max(ctas, 1);
   LCK(cudaEventRecord(L->evk[2], stream));
   LCK(launch_grid(a, ctas, stream));
@@ -289,6 +300,7 @@ int table_exhaustive(Lane* L, dto_pair* P, const int16_t* X, long long xstride, 
   g.ntask = ntask;
   g.mode = kModeScreen;
   g.smemF = grid_smem_bytes(P->C, P->dev.n1, P->npop, 1) <= L->ctx->smem_optin ? 1 : 0;
+  g.coop = 1;  // the few tasks left here are the hard ones: a CTA each
   g.out = dOut;
   g.work = cnts + nlev;
   g.n_refined = L->dRefined;
@@ -422,7 +434,7 @@ int lane_run_range(Lane* L, dto_pair* P, uint32_t perm_first, int64_t n_perm, ui
   // batch holds first_batch permutations; its 90th and 99th percentiles and
   // maximum of the minimum p set the three-level table ladder of the
   // remaining batches.
-  const long long first_batch = 1024;
+  const long long first_batch = kFirstBatch;
   const bool use_table = (mode == kModeScreen) && n_perm > 2 * first_batch;
   // every task's result must name a grid cell: a result that does not is a
   // device-side failure and is reported instead of read
@@ -500,7 +512,8 @@ int lane_run_range(Lane* L, dto_pair* P, uint32_t perm_first, int64_t n_perm, ui
     LCK(cudaMemcpyAsync(L->dX, P->dYlab, (size_t)P->N1 * 2, cudaMemcpyDeviceToDevice, L->stream));
     LCK(cudaEventRecord(L->evSide, L->stream));
     LCK(cudaStreamWaitEvent(L->side, L->evSide, 0));
-    rc = lane_grid_tasks(L, P, (const int16_t*)L->dX, xs, cnt0 + 1, mode, dRes, nullptr, nullptr, true, L->side);
+    rc = lane_grid_tasks(L, P, (const int16_t*)L->dX, xs, cnt0 + 1, mode, dRes, nullptr, nullptr, true, L->side,
+                         kFirstBatchCoop);
     if (rc) return rc;
     LCK(cudaMemcpyAsync(hRes, dRes, (size_t)(cnt0 + 1) * sizeof(TaskResult), cudaMemcpyDeviceToHost, L->side));
     L->acc_d2h += (long long)(cnt0 + 1) * (long long)sizeof(TaskResult);
