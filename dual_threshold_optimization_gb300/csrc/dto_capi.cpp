@@ -164,7 +164,9 @@ int dto_ctx_create(int device, dto_ctx** out) {
     return e == cudaErrorMemoryAllocation ? DTO_ERR_OOM : DTO_ERR_CUDA;
   }
   ctx->nsm = prop.multiProcessorCount;
-  ctx->smem_optin = prop.sharedMemPerBlockOptin;
+  // dynamic shared memory a kernel may take: the per-block limit less 1 KB
+  // for the kernels' static shared arrays
+  ctx->smem_optin = prop.sharedMemPerBlockOptin - 1024;
   const int rc = lane_create(ctx, &ctx->lane0, &ctx->err);
   if (rc) {
     delete ctx;

@@ -45,6 +45,10 @@ struct Lane {
   dto_ctx* ctx = nullptr;
   std::string* err = nullptr;  // where this lane's error messages go
   std::string own_err;
+  // first batch with a CTA per task: lowest latency for a run alone; lanes
+  // that share the GPU with other runs take the warp-per-task screen, whose
+  // throughput is higher
+  bool coop_first = true;
   cudaStream_t stream = nullptr;
   cudaStream_t side = nullptr;  // first batch, later table levels and fallbacks
   cudaEvent_t evSide = nullptr;
@@ -80,7 +84,7 @@ struct Lane {
 struct dto_ctx {
   int device = 0;
   int nsm = 0;
-  size_t smem_optin = 0;
+  size_t smem_optin = 0;  // dynamic shared-memory budget of one block
   std::string err;
   std::mutex mu;       // serialises the context-level calls (default lane, pair creation)
   std::mutex lf_mu;    // guards the log-factorial table

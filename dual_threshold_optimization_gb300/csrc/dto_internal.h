@@ -27,7 +27,7 @@ constexpr int kPermWordsMaxL = 32768;
 // Shared-memory budget of the permutation kernel: the label table Ylab is
 // staged there (random 2-byte gathers hit shared-memory banks instead of L1
 // sectors) when it fits beside the counters, the words and the indices.
-constexpr size_t kPermSmemBudget = 227 * 1024;
+constexpr size_t kPermSmemBudget = 226 * 1024;  // 227 KB per block, less the static arrays
 __host__ __device__ constexpr size_t perm_base_smem(int L) {
   return (size_t)kBuckets * 4 + (L <= kPermWordsMaxL ? (size_t)L * 4 : 0) + (((size_t)L * 2 + 15) & ~(size_t)15);
 }

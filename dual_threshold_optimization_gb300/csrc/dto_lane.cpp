@@ -513,7 +513,7 @@ int lane_run_range(Lane* L, dto_pair* P, uint32_t perm_first, int64_t n_perm, ui
     LCK(cudaEventRecord(L->evSide, L->stream));
     LCK(cudaStreamWaitEvent(L->side, L->evSide, 0));
     rc = lane_grid_tasks(L, P, (const int16_t*)L->dX, xs, cnt0 + 1, mode, dRes, nullptr, nullptr, true, L->side,
-                         kFirstBatchCoop);
+                         kFirstBatchCoop && L->coop_first);
     if (rc) return rc;
     LCK(cudaMemcpyAsync(hRes, dRes, (size_t)(cnt0 + 1) * sizeof(TaskResult), cudaMemcpyDeviceToHost, L->side));
     L->acc_d2h += (long long)(cnt0 + 1) * (long long)sizeof(TaskResult);

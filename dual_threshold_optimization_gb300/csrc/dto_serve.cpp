@@ -136,6 +136,7 @@ int dto_serve_create(dto_ctx* ctx, int lanes, int64_t mem_budget, dto_server** o
       delete s;
       return rc;
     }
+    L->coop_first = false;  // requests share the GPU: throughput first
     s->lanes.push_back(L);
   }
   for (int w = 0; w < lanes; ++w) s->workers.emplace_back(worker, s, w);

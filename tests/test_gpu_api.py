@@ -98,3 +98,18 @@ def test_run_range_splits_reproduce_one_run():
     a = dp.run(120, seed=5, first=1)
     b = dp.run(180, seed=5, first=121)
     assert np.array_equal(np.concatenate([a.minp, b.minp]), whole.minp)
+
+
+@pytest.mark.parametrize("N", [26870, 26890, 27000, 32760, 32780])
+def test_shared_memory_limits_at_list_lengths(engine, N):
+    # list lengths around the permutation kernel's shared-memory switches
+    # (label staging, kept words): the launches fit and agree with the spec
+    from oracle import oracle as O
+    from dual_threshold_optimization_gb300 import synth
+    p = synth.copula_pair(N, 0.1, seed=91)
+    dp = engine.pair(p.ranks1, p.feat1, p.ranks2, p.feat2, p.n_features, p.population)
+    i1, _ = dp.export_permutations(5, 1, 1)
+    assert np.array_equal(O.shuffle(5, 0, 1, 1, N), i1[0])
+    r = dp.run(40, seed=5)
+    assert np.all(np.isfinite(r.minp)) and r.unpermuted["pvalue"] <= 1.0
+    dp.close()
