@@ -71,7 +71,13 @@ struct Lane {
   unsigned* dGuess = nullptr;  // bound histogram shared by the batches of one run
   void* dHits[2] = {nullptr, nullptr};  // per-warp hit buffers of the table screen, one per stream
   size_t hitBytes[2] = {0, 0};
-  BatchSlot slot[2];  // double-buffered batches of the table-screen pipeline
+  // Batches of the table-screen pipeline in flight.  A slot is reused only
+  // once the side stream has finished its batch; with three, the main stream
+  // draws the next batch's labels while the side stream still resolves the
+  // batch before last (its later levels get SMs only as the level-0 sweep
+  // on the main stream lets go of them).
+  static constexpr int kSlots = 3;
+  BatchSlot slot[kSlots];
   // table screens (the ladder) of the pair this lane last ran
   uint16_t* dKthr[3] = {nullptr, nullptr, nullptr};
   size_t kthrBytes[3] = {0, 0, 0};

@@ -519,12 +519,12 @@ int lane_run_range(Lane* L, dto_pair* P, uint32_t perm_first, int64_t n_perm, ui
     L->acc_d2h += (long long)(cnt0 + 1) * (long long)sizeof(TaskResult);
     LCK(cudaEventRecord(L->evSide, L->side));
     // Labels of the pipelined batches b = 0, 1, ... (permutations
-    // first_batch + b * batch on), slot b & 1; the first two are drawn now.
+    // first_batch + b * batch on), slot b % kSlots; the first two are drawn now.
     const long long pipe_from = first_batch;
     const long long npipe = (n_perm - pipe_from + batch - 1) / batch;
     bool drawn[2] = {false, false};
     auto draw = [&](long long it) -> int {
-      BatchSlot& sl = L->slot[it & 1];
+      BatchSlot& sl = L->slot[it % Lane::kSlots];
       const long long b0 = pipe_from + it * batch;
       const int cnt = (int)std::min(batch, n_perm - b0);
       if (!sl.ev[0])
@@ -578,9 +578,9 @@ int lane_run_range(Lane* L, dto_pair* P, uint32_t perm_first, int64_t n_perm, ui
     rc = ensure_table(L, P, 2, t2);
     if (rc) return rc;
     const int nlev = 3;
-    // Two batches in flight: while batch b's later table levels, exhaustive
-    // fallback and result copy run on the side stream, batch b+1's labels and
-    // level-0 table sweep run on the main stream.
+    // Batches in flight: while batch b's later table levels, exhaustive
+    // fallback and result copy run on the side stream, the next batches'
+    // labels and level-0 table sweeps run on the main stream.
     auto harvest = [&](BatchSlot& sl) -> int {
       LCK(cudaEventSynchronize(sl.ev[7]));
       float ms = 0.f;
@@ -599,7 +599,7 @@ int lane_run_range(Lane* L, dto_pair* P, uint32_t perm_first, int64_t n_perm, ui
       return DTO_OK;
     };
     for (long long it = 0; it < npipe; ++it) {
-      BatchSlot& sl = L->slot[it & 1];
+      BatchSlot& sl = L->slot[it % Lane::kSlots];
       if (sl.busy) {
         rc = harvest(sl);
         if (rc) return rc;

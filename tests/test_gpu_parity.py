@@ -185,12 +185,12 @@ def test_table_screen_equals_fp64_many_permutations(engine):
 
 @pytest.mark.parametrize("kind", ["same_set", "general"])
 def test_pipelined_batches_equal_short_runs(engine, kind):
-    # a run long enough for three label batches after the first one (two
-    # batches in flight, one slot reused) must give every permutation the
+    # a run long enough for several label batches after the first one
+    # (batches in flight, slots reused) must give every permutation the
     # optimum that short runs of the same permutation ids give
     if kind == "same_set":
         p = synth.copula_pair(20000, 0.2, seed=57)
-        P = 60000  # 1,024 + 26,843 + 26,843 + 5,290 at 40,000 label bytes a permutation
+        P = 110000  # 1,024 + 26,843 x 4 + 1,604 at 40,000 label bytes a permutation: slots reused
     else:
         p = synth.small_pair(20000, 0.2, seed=58, subset1=19000, subset2=19500)
         P = 15000  # 1,024 + 6,972 + 6,972 + 32 at 1 GiB of two-list index scratch
