@@ -125,6 +125,12 @@ struct dto_pair {
   int16_t* dLab2 = nullptr;
   int* dMap12 = nullptr;
   dto::PairDev dev{};
+  // The table ladder (fixed-point bounds of levels 0..2) from the last long
+  // run of this pair: a property of the pair's null distribution, so a later
+  // run starts its pipeline with it instead of measuring a first batch.
+  std::mutex ladder_mu;
+  bool ladder_ok = false;
+  int ladder_tau[3] = {0, 0, 0};
 };
 
 namespace dto {

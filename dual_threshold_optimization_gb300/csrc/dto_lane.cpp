@@ -394,6 +394,23 @@ int make_labels_launch(Lane* L, dto_pair* P, uint64_t seed, uint32_t first, int 
   return DTO_OK;
 }
 
+// Bounds of the three table levels from a sample of minimum p-values: the
+// 90th percentile (level 0), the 99th (level 1), one nat above the maximum
+// (level 2), as fixed-point ln p, each above the one before.
+void ladder_of(std::vector<double> v, int fshift, int tau[3]) {
+  auto q = [&](double f) {
+    const size_t k = (size_t)(f * (double)(v.size() - 1));
+    std::nth_element(v.begin(), v.begin() + (long)k, v.end());
+    return std::max(v[k], 1e-300);
+  };
+  const double p90 = q(kLevel0Quantile);
+  const double p99 = q(0.99);
+  const double pmax = std::max(*std::max_element(v.begin(), v.end()), 1e-300);
+  tau[0] = fixed_log(p90, fshift);
+  tau[1] = std::max(fixed_log(p99, fshift), tau[0] + 1);
+  tau[2] = std::max((int)std::min(0.0, std::floor((std::log(pmax) + 1.0) * std::ldexp(1.0, fshift))), tau[1] + 1);
+}
+
 int lane_run_range(Lane* L, dto_pair* P, uint32_t perm_first, int64_t n_perm, uint64_t seed,
                    const int32_t* perm_idx, int precision, dto_result* out_unpermuted, double* out_minp,
                    dto_result* out_perm, dto_summary* out_summary) {
@@ -499,28 +516,45 @@ int lane_run_range(Lane* L, dto_pair* P, uint32_t perm_first, int64_t n_perm, ui
     // Slots left busy by a call that returned early hold nothing of this call.
     LCK(cudaStreamSynchronize(L->side));
     for (BatchSlot& sl : L->slot) sl.busy = false;
-    // Batch 0 (task 0 + first_batch permutations) runs through the exhaustive
-    // screen on the side stream.  Its slowest tasks (the permutations with
-    // the largest minimum p) take several times a typical task; meanwhile the
-    // main stream draws the labels of the first two pipelined batches.
-    const int cnt0 = (int)first_batch;
-    const int32_t* dI0 = nullptr;
-    rc = upload_idx(&dIdx, &idxBytes, 0, cnt0, &dI0);
-    if (rc) return rc;
-    rc = lane_make_labels(L, P, seed, perm_first, cnt0, dI0, 1);
-    if (rc) return rc;
+    // The ladder: from an earlier run of this pair when there was one (task 0
+    // then runs alone on the side stream and every permutation goes through
+    // the pipeline), else from this run's first batch: task 0 and first_batch
+    // permutations through the exhaustive screen on the side stream.  The
+    // first batch's slowest tasks (the permutations with the largest minimum
+    // p) take several times a typical task; meanwhile the main stream draws
+    // the labels of the first two pipelined batches.
+    int tau[3] = {0, 0, 0};
+    bool warm = false;
+    {
+      std::lock_guard<std::mutex> g(P->ladder_mu);
+      if (P->ladder_ok) {
+        warm = true;
+        for (int l = 0; l < 3; ++l) tau[l] = P->ladder_tau[l];
+      }
+    }
+    const int cnt0 = warm ? 0 : (int)first_batch;
+    if (warm) {
+      rc = lane_grow(L, &L->dX, &L->xBytes, (size_t)xs * 2);
+      if (rc) return rc;
+    } else {
+      const int32_t* dI0 = nullptr;
+      rc = upload_idx(&dIdx, &idxBytes, 0, cnt0, &dI0);
+      if (rc) return rc;
+      rc = lane_make_labels(L, P, seed, perm_first, cnt0, dI0, 1);
+      if (rc) return rc;
+    }
     LCK(cudaMemcpyAsync(L->dX, P->dYlab, (size_t)P->N1 * 2, cudaMemcpyDeviceToDevice, L->stream));
     LCK(cudaEventRecord(L->evSide, L->stream));
     LCK(cudaStreamWaitEvent(L->side, L->evSide, 0));
-    rc = lane_grid_tasks(L, P, (const int16_t*)L->dX, xs, cnt0 + 1, mode, dRes, nullptr, nullptr, true, L->side,
-                         kFirstBatchCoop && L->coop_first);
+    rc = lane_grid_tasks(L, P, (const int16_t*)L->dX, xs, cnt0 + 1, mode, dRes, nullptr, nullptr, !warm, L->side,
+                         warm || (kFirstBatchCoop && L->coop_first));
     if (rc) return rc;
     LCK(cudaMemcpyAsync(hRes, dRes, (size_t)(cnt0 + 1) * sizeof(TaskResult), cudaMemcpyDeviceToHost, L->side));
     L->acc_d2h += (long long)(cnt0 + 1) * (long long)sizeof(TaskResult);
     LCK(cudaEventRecord(L->evSide, L->side));
     // Labels of the pipelined batches b = 0, 1, ... (permutations
-    // first_batch + b * batch on), slot b % kSlots; the first two are drawn now.
-    const long long pipe_from = first_batch;
+    // cnt0 + b * batch on), slot b % kSlots; the first two are drawn now.
+    const long long pipe_from = cnt0;
     const long long npipe = (n_perm - pipe_from + batch - 1) / batch;
     bool drawn[2] = {false, false};
     auto draw = [&](long long it) -> int {
@@ -551,32 +585,24 @@ int lane_run_range(Lane* L, dto_pair* P, uint32_t perm_first, int64_t n_perm, ui
       if (rc) return rc;
       drawn[it] = true;
     }
-    // the first batch's results set the ladder
-    LCK(cudaEventSynchronize(L->evSide));
-    {
+    auto first_done = [&]() -> int {
+      LCK(cudaEventSynchronize(L->evSide));
       float ms = 0.f;
-      if (cudaEventElapsedTime(&ms, L->evk[0], L->evk[1]) == cudaSuccess) L->acc_perm_ms += ms;
+      if (cnt0 > 0 && cudaEventElapsedTime(&ms, L->evk[0], L->evk[1]) == cudaSuccess) L->acc_perm_ms += ms;
       if (cudaEventElapsedTime(&ms, L->evk[2], L->evk[3]) == cudaSuccess) L->acc_grid_ms += ms;
+      if (!valid(hRes[0])) return lane_err(L, DTO_ERR_CUDA, "unpermuted task: the search returned no grid cell");
+      unperm = hRes[0];
+      return take(hRes + 1, 0, cnt0);
+    };
+    if (!warm) {
+      rc = first_done();
+      if (rc) return rc;
+      ladder_of(std::vector<double>(minp.begin(), minp.begin() + cnt0), P->fshift, tau);
     }
-    unperm = hRes[0];
-    if (!valid(hRes[0])) return lane_err(L, DTO_ERR_CUDA, "unpermuted task: the search returned no grid cell");
-    rc = take(hRes + 1, 0, cnt0);
-    if (rc) return rc;
-    std::vector<double> v(minp.begin(), minp.begin() + cnt0);
-    std::sort(v.begin(), v.end());
-    const double p90 = std::max(v[(size_t)(kLevel0Quantile * (double)(v.size() - 1))], 1e-300);
-    const double p99 = std::max(v[(size_t)(0.99 * (double)(v.size() - 1))], 1e-300);
-    const double pmax = std::max(v.back(), 1e-300);
-    const int sc = P->fshift;
-    const int t0 = fixed_log(p90, sc);
-    const int t1 = std::max(fixed_log(p99, sc), t0 + 1);
-    const int t2 = std::max((int)std::min(0.0, std::floor((std::log(pmax) + 1.0) * std::ldexp(1.0, sc))), t1 + 1);
-    rc = ensure_table(L, P, 0, t0);
-    if (rc) return rc;
-    rc = ensure_table(L, P, 1, t1);
-    if (rc) return rc;
-    rc = ensure_table(L, P, 2, t2);
-    if (rc) return rc;
+    for (int l = 0; l < 3; ++l) {
+      rc = ensure_table(L, P, l, tau[l]);
+      if (rc) return rc;
+    }
     const int nlev = 3;
     // Batches in flight: while batch b's later table levels, exhaustive
     // fallback and result copy run on the side stream, the next batches'
@@ -631,6 +657,18 @@ int lane_run_range(Lane* L, dto_pair* P, uint32_t perm_first, int64_t n_perm, ui
         rc = harvest(sl);
         if (rc) return rc;
       }
+    }
+    if (warm) {
+      rc = first_done();
+      if (rc) return rc;
+    }
+    // this run's minimum p-values set the ladder of the pair's next run
+    {
+      int t[3];
+      ladder_of(minp, P->fshift, t);
+      std::lock_guard<std::mutex> g(P->ladder_mu);
+      for (int l = 0; l < 3; ++l) P->ladder_tau[l] = t[l];
+      P->ladder_ok = true;
     }
     // the main stream's timing event follows the side stream's last work
     LCK(cudaEventRecord(L->evSide, L->side));

@@ -234,3 +234,20 @@ def test_philox_permutations_long_lists_match_spec(engine, N):
     for b in range(3):
         assert np.array_equal(O.shuffle(seed, 0, 11 + b, 1, N), i1[b])
     dp.close()
+
+
+def test_warm_ladder_gives_the_same_results(engine):
+    # the first long run of a pair measures its ladder from a first batch; a
+    # later run starts from the ladder the earlier run left: same results
+    p = synth.copula_pair(5000, 0.25, seed=63, frac_tied2=0.05)
+    dp = engine.pair(p.ranks1, p.feat1, p.ranks2, p.feat2, p.n_features, p.population)
+    cold = dp.run(9000, seed=17, want_records=True)
+    warm = dp.run(9000, seed=17, want_records=True)
+    assert warm.unpermuted == cold.unpermuted
+    assert np.array_equal(warm.records, cold.records)
+    assert warm.summary["count_le"] == cold.summary["count_le"]
+    other = engine.pair(p.ranks1, p.feat1, p.ranks2, p.feat2, p.n_features, p.population)
+    shifted = other.run(4000, seed=17, first=5001, want_records=True)  # cold, other ids
+    assert np.array_equal(shifted.records, cold.records[5000:9000])
+    dp.close()
+    other.close()
