@@ -29,6 +29,13 @@ constexpr double kLevel0Quantile = DTO_L0_QUANTILE;
 #define DTO_FIRST_BATCH 1024
 #endif
 constexpr long long kFirstBatch = DTO_FIRST_BATCH;
+// Levels of the table ladder: 3 (90th, 99th percentile, maximum + 1 nat) or
+// 2 (90th percentile, maximum + 1 nat).
+#ifndef DTO_LADDER_LEVELS
+#define DTO_LADDER_LEVELS 3
+#endif
+constexpr int kLadderLevels = DTO_LADDER_LEVELS;
+static_assert(kLadderLevels == 2 || kLadderLevels == 3, "two or three table levels");
 // The first batch's screen with a CTA per task (see grid_kernel).
 #ifndef DTO_FIRST_COOP
 #define DTO_FIRST_COOP 1
@@ -409,6 +416,7 @@ void ladder_of(std::vector<double> v, int fshift, int tau[3]) {
   tau[0] = fixed_log(p90, fshift);
   tau[1] = std::max(fixed_log(p99, fshift), tau[0] + 1);
   tau[2] = std::max((int)std::min(0.0, std::floor((std::log(pmax) + 1.0) * std::ldexp(1.0, fshift))), tau[1] + 1);
+  if (kLadderLevels == 2) tau[1] = tau[2];
 }
 
 int lane_run_range(Lane* L, dto_pair* P, uint32_t perm_first, int64_t n_perm, uint64_t seed,
@@ -599,11 +607,11 @@ int lane_run_range(Lane* L, dto_pair* P, uint32_t perm_first, int64_t n_perm, ui
       if (rc) return rc;
       ladder_of(std::vector<double>(minp.begin(), minp.begin() + cnt0), P->fshift, tau);
     }
-    for (int l = 0; l < 3; ++l) {
+    for (int l = 0; l < kLadderLevels; ++l) {
       rc = ensure_table(L, P, l, tau[l]);
       if (rc) return rc;
     }
-    const int nlev = 3;
+    const int nlev = kLadderLevels;
     // Batches in flight: while batch b's later table levels, exhaustive
     // fallback and result copy run on the side stream, the next batches'
     // labels and level-0 table sweeps run on the main stream.
