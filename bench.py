@@ -373,6 +373,8 @@ def run_gpu(args):
         "data": "synthetic (seeded Gaussian-copula lists)",
         "config": {"workload": WORKLOAD, "n_features": N_FEATURES, "rho": RHO, "permutations": P,
                    "grid": [dp.n1, dp.n2],
+                   "ladder": "value: the pair keeps the table ladder its warm-up runs measured; "
+                             "e2e: a new pair each step, so its first run measures the ladder",
                    "l2": "inputs larger than L2: each step streams %d MB of permutation labels"
                          % (P * N_FEATURES * 2 // 1000000)},
         "latency_ms": {"p50": statistics.median(step_ms),

@@ -19,7 +19,8 @@
 
 namespace dto {
 
-// Quantile of the first batch's minimum p-values that sets the level-0 table.
+// Quantile of a sample of minimum p-values (a run's first batch, or the
+// pair's previous run) that sets the level-0 table.
 #ifndef DTO_L0_QUANTILE
 #define DTO_L0_QUANTILE 0.90
 #endif
@@ -188,7 +189,7 @@ long long run_device_bytes(const dto_ctx* ctx, const dto_pair* P, int64_t n_perm
   const long long first = std::min<long long>(batch, 1025);
   long long b = first * xs * 2 + (long long)(batch + 1) * (long long)sizeof(TaskResult);  // first batch
   if (n_perm > 2048) {
-    b += 2 * batch * (xs * 2 + (long long)sizeof(TaskResult) + 12);                          // two slots
+    b += Lane::kSlots * batch * (xs * 2 + (long long)sizeof(TaskResult) + 12);                // batch slots
     b += 2LL * kTableCtasPerSm * ctx->nsm * kTableWarps * kTableHitCap * kTableTasks * 8;    // hit buffers
     b += 3LL * (long long)table_entries(P->C, P->dev.n1) * 2;                                 // table ladder
   }
@@ -250,13 +251,12 @@ int ensure_table(Lane* L, dto_pair* P, int level, int tau) {
   return DTO_OK;
 }
 
-// Tasks [0, ntask) of X through the table ladder: level l takes the tasks
-// that level l-1 could not settle (their minimum lies above its bound), and
-// the exhaustive screen takes what the last level leaves.  The lists and
-// their counts stay on the device.  `fall` holds nlev lists of cap entries,
-// `cnts` 8 task counters then 4 list counts.  The levels run on the context's
-// stream; the exhaustive screen runs on `xstream` after `evTab` (which may be
-// the same stream).
+// Levels [lev_begin, lev_end) of the table ladder over tasks [0, ntask) of X,
+// on `stream` with hit buffer `hb`: level l takes the tasks that level l-1
+// could not settle (their minimum lies above its bound); table_exhaustive
+// takes what the last level leaves.  The lists and their counts stay on the
+// device: `fall` holds one list of ntask entries per level, `cnts` 8 task
+// counters then 4 list counts (zeroed by the launch of level 0).
 int table_levels(Lane* L, dto_pair* P, const int16_t* X, long long xstride, int ntask, TaskResult* dOut,
                  int lev_begin, int lev_end, int* fall, int* cnts, cudaStream_t stream, int hb) {
   const int cap = std::max(ntask, 1);
@@ -401,7 +401,7 @@ int make_labels_launch(Lane* L, dto_pair* P, uint64_t seed, uint32_t first, int 
   return DTO_OK;
 }
 
-// Bounds of the three table levels from a sample of minimum p-values: the
+// Bounds of the table levels from a sample of minimum p-values: the
 // 90th percentile (level 0), the 99th (level 1), one nat above the maximum
 // (level 2), as fixed-point ln p, each above the one before.
 void ladder_of(std::vector<double> v, int fshift, int tau[3]) {
@@ -454,11 +454,9 @@ int lane_run_range(Lane* L, dto_pair* P, uint32_t perm_first, int64_t n_perm, ui
   LCK(cudaEventRecord(L->ev0, L->stream));
   std::vector<double> minp((size_t)n_perm);
   TaskResult unperm{};
-  // The unpermuted task (task 0) rides in row 0 of the first batch, through
-  // the exhaustive screen.  With the table screen (long runs), the first
-  // batch holds first_batch permutations; its 90th and 99th percentiles and
-  // maximum of the minimum p set the three-level table ladder of the
-  // remaining batches.
+  // Short runs (and FP64 runs) go through the exhaustive screen in batches,
+  // the unpermuted task (task 0) in row 0 of the first.  Long runs go through
+  // the table ladder (below).
   const long long first_batch = kFirstBatch;
   const bool use_table = (mode == kModeScreen) && n_perm > 2 * first_batch;
   // every task's result must name a grid cell: a result that does not is a
