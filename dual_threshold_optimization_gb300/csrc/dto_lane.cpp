@@ -42,6 +42,10 @@ static_assert(kLadderLevels == 2 || kLadderLevels == 3, "two or three table leve
 #define DTO_FIRST_COOP 1
 #endif
 constexpr bool kFirstBatchCoop = DTO_FIRST_COOP != 0;
+#ifndef DTO_SIDE_PRIORITY
+#define DTO_SIDE_PRIORITY 0
+#endif
+constexpr bool kSidePriority = DTO_SIDE_PRIORITY != 0;
 
 int set_err(dto_ctx* ctx, int code, const std::string& msg) {
   if (ctx) ctx->err = msg;
@@ -98,7 +102,16 @@ int lane_create(dto_ctx* ctx, Lane** out, std::string* err_sink) {
   };
   cudaError_t e;
   if ((e = cudaStreamCreateWithFlags(&L->stream, cudaStreamNonBlocking)) != cudaSuccess) return fail(e, "stream");
-  if ((e = cudaStreamCreateWithFlags(&L->side, cudaStreamNonBlocking)) != cudaSuccess) return fail(e, "stream");
+  // The side stream runs the later table levels and the fallbacks of a batch
+  // while the main stream sweeps the next one.  With DTO_SIDE_PRIORITY its
+  // CTAs go first whenever SMs free up (the level-0 sweep is a persistent
+  // kernel that keeps its SMs until its queue drains); measured neutral at
+  // N = 20,000 (the side levels finish sooner, the next labels later), so off.
+  int prio_least = 0, prio_greatest = 0;
+  if ((e = cudaDeviceGetStreamPriorityRange(&prio_least, &prio_greatest)) != cudaSuccess) return fail(e, "stream");
+  if ((e = cudaStreamCreateWithPriority(&L->side, cudaStreamNonBlocking, kSidePriority ? prio_greatest : prio_least)) !=
+      cudaSuccess)
+    return fail(e, "stream");
   if ((e = cudaEventCreateWithFlags(&L->evSide, cudaEventDisableTiming)) != cudaSuccess) return fail(e, "event");
   if ((e = cudaEventCreate(&L->ev0)) != cudaSuccess) return fail(e, "event");
   if ((e = cudaEventCreate(&L->ev1)) != cudaSuccess) return fail(e, "event");
