@@ -190,10 +190,10 @@ def test_pipelined_batches_equal_short_runs(engine, kind):
     # optimum that short runs of the same permutation ids give
     if kind == "same_set":
         p = synth.copula_pair(20000, 0.2, seed=57)
-        P = 110000  # 1,024 + 26,843 x 4 + 1,604 at 40,000 label bytes a permutation: slots reused
+        P = 110000  # 512 + 26,843 x 4 + 2,116 at 40,000 label bytes a permutation: slots reused
     else:
         p = synth.small_pair(20000, 0.2, seed=58, subset1=19000, subset2=19500)
-        P = 15000  # 1,024 + 6,972 + 6,972 + 32 at 1 GiB of two-list index scratch
+        P = 15000  # 512 + 6,972 + 6,972 + 544 at 1 GiB of two-list index scratch
     dp = engine.pair(p.ranks1, p.feat1, p.ranks2, p.feat2, p.n_features, p.population)
     long_run = dp.run(P, seed=99, precision="screen", want_records=True)
     step = 2000  # at most 2,048: the exhaustive screen alone
