@@ -483,7 +483,9 @@ __global__ void __launch_bounds__(kTableWarps * 32, kTableCtasPerSm) table_grid_
         c1[t] = w1[t];
         const int q0 = (sN >> 1) + lane;
         w0[t] = (live[t] && 2 * q0 < eN) ? __ldg(x32[t] + q0) : -1;
-        w1[t] = (live[t] && 2 * (q0 + 32) < eN) ? __ldg(x32[t] + q0 + 32) : -1;
+        // the second 64 labels, only for rows that long (uniform branch)
+        w1[t] = -1;
+        if (eN > 2 * (sN >> 1) + 64 && live[t] && 2 * (q0 + 32) < eN) w1[t] = __ldg(x32[t] + q0 + 32);
       }
       // this row's table chunks: consumed after the label updates and the scan
 #pragma unroll
@@ -492,9 +494,11 @@ __global__ void __launch_bounds__(kTableWarps * 32, kTableCtasPerSm) table_grid_
       for (int t = 0; t < T; ++t) {
         const int q0 = (s >> 1) + lane;
         add_word(t, c0[t], q0, s, e);
-        add_word(t, c1[t], q0 + 32, s, e);
-        if (live[t])
-          for (int q = q0 + 64; 2 * q < e; q += 32) add_word(t, __ldg(x32[t] + q), q, s, e);
+        if (e > 2 * (s >> 1) + 64) {  // a row of more than 64 labels (uniform)
+          add_word(t, c1[t], q0 + 32, s, e);
+          if (live[t])
+            for (int q = q0 + 64; 2 * q < e; q += 32) add_word(t, __ldg(x32[t] + q), q, s, e);
+        }
       }
       __syncwarp();
       int excl[T];
