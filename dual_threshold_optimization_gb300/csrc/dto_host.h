@@ -78,11 +78,14 @@ struct Lane {
   // on the main stream lets go of them).
   static constexpr int kSlots = 3;
   BatchSlot slot[kSlots];
-  // table screens (the ladder) of the pair this lane last ran
-  uint16_t* dKthr[3] = {nullptr, nullptr, nullptr};
-  size_t kthrBytes[3] = {0, 0, 0};
-  unsigned long long kthr_pair[3] = {0, 0, 0};  // pair serial the table was built for (0: none)
-  int kthr_tau[3] = {0, 0, 0};
+  // table screens of the pair this lane last ran: the ladder's levels 0..2,
+  // then the tighter tables 3..5 a level-0 sweep switches to once a task's
+  // bound is known
+  static constexpr int kTables = 6;
+  uint16_t* dKthr[kTables] = {};
+  size_t kthrBytes[kTables] = {};
+  unsigned long long kthr_pair[kTables] = {};  // pair serial the table was built for (0: none)
+  int kthr_tau[kTables] = {};
 };
 
 }  // namespace dto
@@ -130,7 +133,7 @@ struct dto_pair {
   // run starts its pipeline with it instead of measuring a first batch.
   std::mutex ladder_mu;
   bool ladder_ok = false;
-  int ladder_tau[3] = {0, 0, 0};
+  int ladder_tau[6] = {0, 0, 0, 0, 0, 0};
 };
 
 namespace dto {

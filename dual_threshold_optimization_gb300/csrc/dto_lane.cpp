@@ -39,6 +39,12 @@ constexpr long long kFirstBatch = DTO_FIRST_BATCH;
 #endif
 constexpr int kLadderLevels = DTO_LADDER_LEVELS;
 static_assert(kLadderLevels == 2 || kLadderLevels == 3, "two or three table levels");
+// Tighter tables a level-0 sweep may switch to (0 to 3).
+#ifndef DTO_TIGHT_TABLES
+#define DTO_TIGHT_TABLES 3
+#endif
+constexpr int kTightTables = DTO_TIGHT_TABLES;
+static_assert(kTightTables >= 0 && kTightTables <= 3, "at most three tighter tables");
 // The first batch's screen with a CTA per task (see grid_kernel).
 #ifndef DTO_FIRST_COOP
 #define DTO_FIRST_COOP 1
@@ -139,7 +145,7 @@ void lane_destroy(Lane* L) {
   cudaFree(L->dGuess);
   cudaFree(L->dHits[0]);
   cudaFree(L->dHits[1]);
-  for (int l = 0; l < 3; ++l) cudaFree(L->dKthr[l]);
+  for (int l = 0; l < Lane::kTables; ++l) cudaFree(L->dKthr[l]);
   for (BatchSlot& sl : L->slot) {
     cudaFree(sl.dX);
     cudaFree(sl.dRes);
@@ -206,7 +212,7 @@ long long run_device_bytes(const dto_ctx* ctx, const dto_pair* P, int64_t n_perm
   if (n_perm > 2048) {
     b += Lane::kSlots * batch * (xs * 2 + (long long)sizeof(TaskResult) + 12);                // batch slots
     b += 2LL * kTableCtasPerSm * ctx->nsm * kTableWarps * kTableHitCap * kTableTasks * 8;    // hit buffers
-    b += 3LL * (long long)table_entries(P->C, P->dev.n1) * 2;                                 // table ladder
+    b += (long long)Lane::kTables * (long long)table_entries(P->C, P->dev.n1) * 2;           // tables
   }
   if (test_mode || !P->same_set) b += 2 * batch * L12 * 4;  // index scratch
   return b;
@@ -288,6 +294,11 @@ int table_levels(Lane* L, dto_pair* P, const int16_t* X, long long xstride, int 
     a.ntask = ntask;
     a.tau = L->kthr_tau[level];
     a.kthr = L->dKthr[level];
+    a.ntight = level == 0 ? kTightTables : 0;
+    for (int q = 0; q < a.ntight; ++q) {
+      a.tight[q] = L->dKthr[3 + q];
+      a.tight_tau[q] = L->kthr_tau[3 + q];
+    }
     a.packed = P->ncommon <= kPackedMaxCommon ? 1 : 0;
     a.smemF = table_smem_bytes(P->C, P->dev.n1, P->dev.n2, P->npop, 1) <= L->ctx->smem_optin ? 1 : 0;
     a.out = dOut;
@@ -419,7 +430,7 @@ int make_labels_launch(Lane* L, dto_pair* P, uint64_t seed, uint32_t first, int 
 // Bounds of the table levels from a sample of minimum p-values: the
 // 90th percentile (level 0), the 99th (level 1), one nat above the maximum
 // (level 2), as fixed-point ln p, each above the one before.
-void ladder_of(std::vector<double> v, int fshift, int tau[3]) {
+void ladder_of(std::vector<double> v, int fshift, int tau[6]) {
   auto q = [&](double f) {
     const size_t k = (size_t)(f * (double)(v.size() - 1));
     std::nth_element(v.begin(), v.begin() + (long)k, v.end());
@@ -432,6 +443,13 @@ void ladder_of(std::vector<double> v, int fshift, int tau[3]) {
   tau[1] = std::max(fixed_log(p99, fshift), tau[0] + 1);
   tau[2] = std::max((int)std::min(0.0, std::floor((std::log(pmax) + 1.0) * std::ldexp(1.0, fshift))), tau[1] + 1);
   if (kLadderLevels == 2) tau[1] = tau[2];
+  // the tighter tables of the level-0 sweep: 50th, 10th and 1st percentiles
+  const double ptight[3] = {q(0.5), q(0.1), q(0.01)};
+  int prev = tau[0];
+  for (int t = 0; t < 3; ++t) {
+    tau[3 + t] = std::min(fixed_log(ptight[t], fshift), prev - 1);
+    prev = tau[3 + t];
+  }
 }
 
 int lane_run_range(Lane* L, dto_pair* P, uint32_t perm_first, int64_t n_perm, uint64_t seed,
@@ -544,13 +562,13 @@ int lane_run_range(Lane* L, dto_pair* P, uint32_t perm_first, int64_t n_perm, ui
     // first batch's slowest tasks (the permutations with the largest minimum
     // p) take several times a typical task; meanwhile the main stream draws
     // the labels of the first two pipelined batches.
-    int tau[3] = {0, 0, 0};
+    int tau[6] = {0, 0, 0, 0, 0, 0};
     bool warm = false;
     {
       std::lock_guard<std::mutex> g(P->ladder_mu);
       if (P->ladder_ok) {
         warm = true;
-        for (int l = 0; l < 3; ++l) tau[l] = P->ladder_tau[l];
+        for (int l = 0; l < 6; ++l) tau[l] = P->ladder_tau[l];
       }
     }
     const int cnt0 = warm ? 0 : (int)first_batch;
@@ -624,6 +642,10 @@ int lane_run_range(Lane* L, dto_pair* P, uint32_t perm_first, int64_t n_perm, ui
       rc = ensure_table(L, P, l, tau[l]);
       if (rc) return rc;
     }
+    for (int l = 0; l < kTightTables; ++l) {
+      rc = ensure_table(L, P, 3 + l, tau[3 + l]);
+      if (rc) return rc;
+    }
     const int nlev = kLadderLevels;
     // Batches in flight: while batch b's later table levels, exhaustive
     // fallback and result copy run on the side stream, the next batches'
@@ -685,10 +707,10 @@ int lane_run_range(Lane* L, dto_pair* P, uint32_t perm_first, int64_t n_perm, ui
     }
     // this run's minimum p-values set the ladder of the pair's next run
     {
-      int t[3];
+      int t[6];
       ladder_of(minp, P->fshift, t);
       std::lock_guard<std::mutex> g(P->ladder_mu);
-      for (int l = 0; l < 3; ++l) P->ladder_tau[l] = t[l];
+      for (int l = 0; l < 6; ++l) P->ladder_tau[l] = t[l];
       P->ladder_ok = true;
     }
     // the main stream's timing event follows the side stream's last work

@@ -73,6 +73,11 @@ static __global__ void table_build_kernel(const TableArgs A) {
 }
 
 constexpr int kTableSurvCap = 64;
+// Hits after which a level-0 sweep resolves early to switch to a tighter table.
+#ifndef DTO_EARLY_HITS
+#define DTO_EARLY_HITS 512
+#endif
+constexpr int kEarlyHits = DTO_EARLY_HITS;
 constexpr int kPend = 64;  // deferred FP64 evaluations per warp (several tasks)
 
 // Per-task state in shared memory: the hot sweep never touches it; only the
@@ -452,6 +457,9 @@ __global__ void __launch_bounds__(kTableWarps * 32, kTableCtasPerSm) table_grid_
 #pragma unroll
     for (int t = 0; t < T; ++t) anyhits[t] = false;
     uint4 kt[NQ];
+    // the table this task's rows are compared with (level's own, or tighter)
+    const uint4* ktab_cur = ktab;
+    int cur_tight = -1;
     // a label is the counter slot lane * Cp + t of its column lane * C + t
     auto add_lab = [&](int t, int lab) {
       const int l = lab / Cp;
@@ -489,7 +497,7 @@ __global__ void __launch_bounds__(kTableWarps * 32, kTableCtasPerSm) table_grid_
       }
       // this row's table chunks: consumed after the label updates and the scan
 #pragma unroll
-      for (int u = 0; u < NQ; ++u) kt[u] = __ldg(ktab + ((size_t)i * NQ + u) * 32 + lane);
+      for (int u = 0; u < NQ; ++u) kt[u] = __ldg(ktab_cur + ((size_t)i * NQ + u) * 32 + lane);
 #pragma unroll
       for (int t = 0; t < T; ++t) {
         const int q0 = (s >> 1) + lane;
@@ -584,15 +592,30 @@ __global__ void __launch_bounds__(kTableWarps * 32, kTableCtasPerSm) table_grid_
       // the next row's counter updates wait for every lane's reads of this row
       __syncwarp();
       // every fourth row: could a task's buffer overflow within the next four
-      // rows?  Then resolve what it holds (hcap leaves room for four full rows).
+      // rows (hcap leaves room for four full rows)?  Or, at level 0, has a
+      // task gathered kEarlyHits hits while a tighter table is left?  Then
+      // resolve what it holds; the bound B it sets lets the remaining rows be
+      // compared with the tightest table whose bound is still >= B: every
+      // cell with ln p <= B (the final B is lower still) stays a hit.
       if ((i & 3) == 3) {
 #pragma unroll
         for (int t = 0; t < T; ++t) {
-          if (st_of(t)->nhits > hcap - 4 * 32 * C) {
-            table_resolve(A, g, table_warp_mem(wb, C, t), lane, hbw + t * hcap, st_of(t)->nhits);
+          const int nh = st_of(t)->nhits;
+          if (nh > hcap - 4 * 32 * C || (T == 1 && cur_tight + 1 < A.ntight && nh >= kEarlyHits)) {
+            table_resolve(A, g, table_warp_mem(wb, C, t), lane, hbw + t * hcap, nh);
             anyhits[t] = true;
             __syncwarp();
             if (lane == 0) st_of(t)->nhits = 0;
+            if (T == 1 && st_of(t)->B_valid) {
+              const int B = st_of(t)->B;
+              for (int q = A.ntight - 1; q > cur_tight; --q) {
+                if (A.tight_tau[q] >= B) {
+                  cur_tight = q;
+                  ktab_cur = reinterpret_cast<const uint4*>(A.tight[q]);
+                  break;
+                }
+              }
+            }
             __syncwarp();
           }
         }
