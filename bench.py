@@ -45,7 +45,7 @@ PERMS_PER_STEP = 100000
 # DRAM bytes per task of the level-0 table sweep at N = 20,000 (ncu capture
 # summarised in profiles/table_grid_level0_n20k.md): labels read once, hit
 # buffer written and re-read.
-SWEEP0_DRAM_BYTES_PER_TASK = 55400.0
+SWEEP0_DRAM_BYTES_PER_TASK = 51900.0
 WORKLOAD = ("single pair, N=20000 features, list 2 Gaussian copula rho=0.2 to list 1, no ties, "
             "100000 on-device Philox permutations per step + the unpermuted task, "
             "FP32 screen + FP64 refine")
