@@ -35,7 +35,10 @@ struct BatchSlot {
   void* dIdx = nullptr;
   size_t idxBytes = 0;
   int* dCnt = nullptr;  // [0, 8): task counters, [8, 12): fallback counts
-  cudaEvent_t ev[8] = {};  // perm start/end, tables start, -, exhaustive start/end, tables done, batch done
+  cudaEvent_t ev[8] = {};  // perm start/end, tables start, side drained, exhaustive start/end, tables done, batch done
+  // the stream of this slot's later table levels, fallbacks and result copy:
+  // the side work of different batches overlaps (each is latency-bound)
+  cudaStream_t side = nullptr;
   bool busy = false;
   long long b0 = 0;
   int cnt = 0;
@@ -69,8 +72,10 @@ struct Lane {
   int* dWork = nullptr;
   unsigned long long* dRefined = nullptr;
   unsigned* dGuess = nullptr;  // bound histogram shared by the batches of one run
-  void* dHits[2] = {nullptr, nullptr};  // per-warp hit buffers of the table screen, one per stream
-  size_t hitBytes[2] = {0, 0};
+  // per-warp hit buffers of the table screen: [0] the main stream's, [1 + s]
+  // slot s's side stream's
+  void* dHits[4] = {};
+  size_t hitBytes[4] = {};
   // Batches of the table-screen pipeline in flight.  A slot is reused only
   // once the side stream has finished its batch; with three, the main stream
   // draws the next batch's labels while the side stream still resolves the

@@ -143,10 +143,13 @@ void lane_destroy(Lane* L) {
   cudaFree(L->dWork);
   cudaFree(L->dRefined);
   cudaFree(L->dGuess);
-  cudaFree(L->dHits[0]);
-  cudaFree(L->dHits[1]);
+  for (void* h : L->dHits) cudaFree(h);
   for (int l = 0; l < Lane::kTables; ++l) cudaFree(L->dKthr[l]);
   for (BatchSlot& sl : L->slot) {
+    if (sl.side) {
+      cudaStreamSynchronize(sl.side);
+      cudaStreamDestroy(sl.side);
+    }
     cudaFree(sl.dX);
     cudaFree(sl.dRes);
     cudaFreeHost(sl.hRes);
@@ -211,7 +214,7 @@ long long run_device_bytes(const dto_ctx* ctx, const dto_pair* P, int64_t n_perm
   long long b = first * xs * 2 + (long long)(batch + 1) * (long long)sizeof(TaskResult);  // first batch
   if (n_perm > 2048) {
     b += Lane::kSlots * batch * (xs * 2 + (long long)sizeof(TaskResult) + 12);                // batch slots
-    b += 2LL * kTableCtasPerSm * ctx->nsm * kTableWarps * kTableHitCap * kTableTasks * 8;    // hit buffers
+    b += 4LL * kTableCtasPerSm * ctx->nsm * kTableWarps * kTableHitCap * kTableTasks * 8;    // hit buffers
     b += (long long)Lane::kTables * (long long)table_entries(P->C, P->dev.n1) * 2;           // tables
   }
   if (test_mode || !P->same_set) b += 2 * batch * L12 * 4;  // index scratch
@@ -554,7 +557,10 @@ int lane_run_range(Lane* L, dto_pair* P, uint32_t perm_first, int64_t n_perm, ui
   } else {
     // Slots left busy by a call that returned early hold nothing of this call.
     LCK(cudaStreamSynchronize(L->side));
-    for (BatchSlot& sl : L->slot) sl.busy = false;
+    for (BatchSlot& sl : L->slot) {
+      if (sl.side) LCK(cudaStreamSynchronize(sl.side));
+      sl.busy = false;
+    }
     // The ladder: from an earlier run of this pair when there was one (task 0
     // then runs alone on the side stream and every permutation goes through
     // the pipeline), else from this run's first batch: task 0 and first_batch
@@ -602,6 +608,7 @@ int lane_run_range(Lane* L, dto_pair* P, uint32_t perm_first, int64_t n_perm, ui
       const int cnt = (int)std::min(batch, n_perm - b0);
       if (!sl.ev[0])
         for (cudaEvent_t& e : sl.ev) LCK(cudaEventCreate(&e));
+      if (!sl.side) LCK(cudaStreamCreateWithFlags(&sl.side, cudaStreamNonBlocking));
       if (!sl.dCnt) LCK(cudaMalloc(&sl.dCnt, 256));
       int r = lane_grow(L, &sl.dX, &sl.xBytes, (size_t)cnt * xs * 2);
       if (!r) r = lane_grow(L, &sl.dRes, &sl.resBytes, (size_t)cnt * sizeof(TaskResult));
@@ -684,15 +691,16 @@ int lane_run_range(Lane* L, dto_pair* P, uint32_t perm_first, int64_t n_perm, ui
       rc = table_levels(L, P, X, xs, cnt, dR, 0, 1, (int*)sl.dFall, sl.dCnt, L->stream, 0);
       if (rc) return rc;
       LCK(cudaEventRecord(sl.ev[6], L->stream));
-      LCK(cudaStreamWaitEvent(L->side, sl.ev[6], 0));
-      LCK(cudaEventRecord(sl.ev[4], L->side));
-      rc = table_levels(L, P, X, xs, cnt, dR, 1, nlev, (int*)sl.dFall, sl.dCnt, L->side, 1);
+      const int si = (int)(it % Lane::kSlots);
+      LCK(cudaStreamWaitEvent(sl.side, sl.ev[6], 0));
+      LCK(cudaEventRecord(sl.ev[4], sl.side));
+      rc = table_levels(L, P, X, xs, cnt, dR, 1, nlev, (int*)sl.dFall, sl.dCnt, sl.side, 1 + si);
       if (rc) return rc;
-      rc = table_exhaustive(L, P, X, xs, cnt, dR, nlev, (const int*)sl.dFall, sl.dCnt, L->side);
+      rc = table_exhaustive(L, P, X, xs, cnt, dR, nlev, (const int*)sl.dFall, sl.dCnt, sl.side);
       if (rc) return rc;
-      LCK(cudaEventRecord(sl.ev[5], L->side));
-      LCK(cudaMemcpyAsync(sl.hRes, dR, (size_t)cnt * sizeof(TaskResult), cudaMemcpyDeviceToHost, L->side));
-      LCK(cudaEventRecord(sl.ev[7], L->side));
+      LCK(cudaEventRecord(sl.ev[5], sl.side));
+      LCK(cudaMemcpyAsync(sl.hRes, dR, (size_t)cnt * sizeof(TaskResult), cudaMemcpyDeviceToHost, sl.side));
+      LCK(cudaEventRecord(sl.ev[7], sl.side));
       sl.busy = true;
     }
     for (BatchSlot& sl : L->slot) {
@@ -713,9 +721,14 @@ int lane_run_range(Lane* L, dto_pair* P, uint32_t perm_first, int64_t n_perm, ui
       for (int l = 0; l < 6; ++l) P->ladder_tau[l] = t[l];
       P->ladder_ok = true;
     }
-    // the main stream's timing event follows the side stream's last work
+    // the main stream's timing event follows the side streams' last work
     LCK(cudaEventRecord(L->evSide, L->side));
     LCK(cudaStreamWaitEvent(L->stream, L->evSide, 0));
+    for (BatchSlot& sl : L->slot) {
+      if (!sl.side) continue;
+      LCK(cudaEventRecord(sl.ev[3], sl.side));
+      LCK(cudaStreamWaitEvent(L->stream, sl.ev[3], 0));
+    }
   }
   fill_result(P, unperm, 0, out_unpermuted);
   const double p_obs = unperm.p;
