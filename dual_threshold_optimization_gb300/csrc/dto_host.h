@@ -44,6 +44,8 @@ struct BatchSlot {
   int cnt = 0;
 };
 
+constexpr int kSlotsMax = 4;
+
 struct Lane {
   dto_ctx* ctx = nullptr;
   std::string* err = nullptr;  // where this lane's error messages go
@@ -74,14 +76,18 @@ struct Lane {
   unsigned* dGuess = nullptr;  // bound histogram shared by the batches of one run
   // per-warp hit buffers of the table screen: [0] the main stream's, [1 + s]
   // slot s's side stream's
-  void* dHits[4] = {};
-  size_t hitBytes[4] = {};
+  void* dHits[1 + kSlotsMax] = {};
+  size_t hitBytes[1 + kSlotsMax] = {};
   // Batches of the table-screen pipeline in flight.  A slot is reused only
   // once the side stream has finished its batch; with three, the main stream
   // draws the next batch's labels while the side stream still resolves the
   // batch before last (its later levels get SMs only as the level-0 sweep
   // on the main stream lets go of them).
-  static constexpr int kSlots = 3;
+#ifndef DTO_SLOTS
+#define DTO_SLOTS 3
+#endif
+  static constexpr int kSlots = DTO_SLOTS;
+  static_assert(kSlots >= 2 && kSlots <= kSlotsMax, "two to four batch slots");
   BatchSlot slot[kSlots];
   // table screens of the pair this lane last ran: the ladder's levels 0..2,
   // then the tighter tables 3..5 a level-0 sweep switches to once a task's

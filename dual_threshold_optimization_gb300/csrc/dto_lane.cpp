@@ -214,7 +214,7 @@ long long run_device_bytes(const dto_ctx* ctx, const dto_pair* P, int64_t n_perm
   long long b = first * xs * 2 + (long long)(batch + 1) * (long long)sizeof(TaskResult);  // first batch
   if (n_perm > 2048) {
     b += Lane::kSlots * batch * (xs * 2 + (long long)sizeof(TaskResult) + 12);                // batch slots
-    b += 4LL * kTableCtasPerSm * ctx->nsm * kTableWarps * kTableHitCap * kTableTasks * 8;    // hit buffers
+    b += (1LL + Lane::kSlots) * kTableCtasPerSm * ctx->nsm * kTableWarps * kTableHitCap * kTableTasks * 8;  // hits
     b += (long long)Lane::kTables * (long long)table_entries(P->C, P->dev.n1) * 2;           // tables
   }
   if (test_mode || !P->same_set) b += 2 * batch * L12 * 4;  // index scratch
