@@ -28,8 +28,10 @@ constexpr int kPermWordsMaxL = 32768;
 // staged there (random 2-byte gathers hit shared-memory banks instead of L1
 // sectors) when it fits beside the counters, the words and the indices.
 constexpr size_t kPermSmemBudget = 226 * 1024;  // 227 KB per block, less the static arrays
+__host__ __device__ constexpr size_t perm_bound_words(int L) { return ((size_t)L + 32 + 31) / 32; }
 __host__ __device__ constexpr size_t perm_base_smem(int L) {
-  return (size_t)kBuckets * 4 + (L <= kPermWordsMaxL ? (size_t)L * 4 : 0) + (((size_t)L * 2 + 15) & ~(size_t)15);
+  return (size_t)kBuckets * 4 + (L <= kPermWordsMaxL ? (size_t)L * 4 : 0) + (((size_t)L * 2 + 15) & ~(size_t)15) +
+         perm_bound_words(L) * 4;
 }
 __host__ __device__ constexpr bool perm_stage_ylab(int L) {
   return perm_base_smem(L) + (((size_t)L * 2 + 15) & ~(size_t)15) <= kPermSmemBudget;
@@ -102,6 +104,12 @@ struct PermArgs {
   long long xstride;
   int* sigma;            // nullable: write sigma [count][sstride]
   long long sstride;
+  // With labels (X): the grid rows' position ranges, rowstart[0..n1].  Only
+  // the multiset of labels inside each row reaches the search, so a bucket
+  // whose positions lie inside one row keeps the order the scatter left
+  // (nullable: every bucket shuffled as the specification says).
+  const int* rowstart;
+  int n1;
 };
 
 struct ComposeArgs {

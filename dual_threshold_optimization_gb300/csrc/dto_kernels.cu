@@ -78,7 +78,7 @@ __device__ __forceinline__ uint32_t bucket_of(uint4 w, int q) {
 // a few operations per element.
 template <bool kWords>
 __device__ __forceinline__ void perm_body(const PermArgs& A, int* cnt, uint16_t* sA, uint32_t* sW,
-                                          int16_t* sY) {
+                                          int16_t* sY, uint32_t* sBound) {
   __shared__ int warpTot[kPermThreads / 32];
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int L = A.L;
@@ -98,7 +98,17 @@ __device__ __forceinline__ void perm_body(const PermArgs& A, int* cnt, uint16_t*
   for (int b = tid; b < kBuckets; b += kPermThreads) cnt[b] = 0;
   if (sY)
     for (int q = tid; q < L; q += kPermThreads) sY[q] = __ldg(A.Ylab + q);
+  // row-start bitmap of the label path: bit p set when a grid row starts at
+  // position p (positions past the last row form one more range)
+  const bool rows = A.X && A.rowstart;
+  if (rows)
+    for (int q = tid; q < (int)perm_bound_words(L); q += kPermThreads) sBound[q] = 0;
   __syncthreads();
+  if (rows)
+    for (int r = tid; r <= A.n1; r += kPermThreads) {
+      const int p = __ldg(A.rowstart + r);
+      atomicOr(&sBound[p >> 5], 1u << (p & 31));
+    }
   const int groups = (L + 3) >> 2;
   for (int g = tid; g < groups; g += kPermThreads) {
     uint4 w = philox4x32_10(make_uint4((uint32_t)g, perm, A.pair_id, tagB), k0, k1);
@@ -172,6 +182,19 @@ __device__ __forceinline__ void perm_body(const PermArgs& A, int* cnt, uint16_t*
     const int s0 = b == 0 ? 0 : cnt[b - 1];
     const int sz = cnt[b] - s0;
     if (sz < 2) continue;
+    if (rows) {
+      // labels only: the search sees each row's multiset of labels, and a
+      // bucket inside one row gives the same multisets in any order (the
+      // sort and the Fisher-Yates pass only decide which of its elements
+      // fall on which side of a row start)
+      bool inside = true;
+      for (int p = s0 + 1; p < s0 + sz; ++p)
+        if (sBound[p >> 5] & (1u << (p & 31))) {
+          inside = false;
+          break;
+        }
+      if (inside) continue;
+    }
     uint16_t* a = sA + s0;
     // canonical (increasing) order inside the bucket
     for (int i = 1; i < sz; ++i) {
@@ -216,14 +239,16 @@ __device__ __forceinline__ void perm_body(const PermArgs& A, int* cnt, uint16_t*
 __global__ void __launch_bounds__(kPermThreads) perm_kernel(const PermArgs A) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   int* cnt = reinterpret_cast<int*>(smem_raw);
+  uint32_t* sBound = reinterpret_cast<uint32_t*>(cnt + kBuckets);
+  unsigned char* rest = reinterpret_cast<unsigned char*>(sBound + perm_bound_words(A.L));
   int16_t* sY = (A.X && perm_stage_ylab(A.L))
                     ? reinterpret_cast<int16_t*>(smem_raw + perm_base_smem(A.L))
                     : nullptr;
   if (A.L <= kPermWordsMaxL) {
-    uint32_t* sW = reinterpret_cast<uint32_t*>(cnt + kBuckets);
-    perm_body<true>(A, cnt, reinterpret_cast<uint16_t*>(sW + A.L), sW, sY);
+    uint32_t* sW = reinterpret_cast<uint32_t*>(rest);
+    perm_body<true>(A, cnt, reinterpret_cast<uint16_t*>(sW + A.L), sW, sY, sBound);
   } else {
-    perm_body<false>(A, cnt, reinterpret_cast<uint16_t*>(cnt + kBuckets), nullptr, sY);
+    perm_body<false>(A, cnt, reinterpret_cast<uint16_t*>(rest), nullptr, sY, sBound);
   }
 }
 

@@ -398,6 +398,8 @@ int make_labels_launch(Lane* L, dto_pair* P, uint64_t seed, uint32_t first, int 
     a.list_tag = 1;
     a.Ylab = P->dYlab;
     a.X = X;
+    a.rowstart = P->dRow;
+    a.n1 = P->dev.n1;
     LCK(launch_perm(a, count, L->stream));
     L->acc_launches += 1;
     return DTO_OK;
