@@ -22,7 +22,8 @@ constexpr int kBuckets = 1 << kBucketBits;  // Rao-Sandelius buckets
 static_assert(kBuckets % kPermThreads == 0 && kPermThreads % 32 == 0 && kPermThreads <= 1024,
               "perm_kernel: buckets must split evenly over its warps");
 // Longest list whose Philox words the permutation kernel keeps in shared
-// memory (4 + 2 bytes an element + the counters: 208 KB at 32,768).
+// memory (4 + 2 bytes an element + the counters and the bucket list: 220 KB
+// at 32,768).
 constexpr int kPermWordsMaxL = 32768;
 // Shared-memory budget of the permutation kernel: the label table Ylab is
 // staged there (random 2-byte gathers hit shared-memory banks instead of L1
@@ -30,8 +31,8 @@ constexpr int kPermWordsMaxL = 32768;
 constexpr size_t kPermSmemBudget = 226 * 1024;  // 227 KB per block, less the static arrays
 __host__ __device__ constexpr size_t perm_bound_words(int L) { return ((size_t)L + 32 + 31) / 32; }
 __host__ __device__ constexpr size_t perm_base_smem(int L) {
-  return (size_t)kBuckets * 4 + (L <= kPermWordsMaxL ? (size_t)L * 4 : 0) + (((size_t)L * 2 + 15) & ~(size_t)15) +
-         perm_bound_words(L) * 4;
+  return (size_t)kBuckets * 4 + (size_t)kBuckets * 2 + (L <= kPermWordsMaxL ? (size_t)L * 4 : 0) +
+         (((size_t)L * 2 + 15) & ~(size_t)15) + perm_bound_words(L) * 4;
 }
 __host__ __device__ constexpr bool perm_stage_ylab(int L) {
   return perm_base_smem(L) + (((size_t)L * 2 + 15) & ~(size_t)15) <= kPermSmemBudget;

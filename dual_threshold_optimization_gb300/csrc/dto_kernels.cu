@@ -78,8 +78,9 @@ __device__ __forceinline__ uint32_t bucket_of(uint4 w, int q) {
 // a few operations per element.
 template <bool kWords>
 __device__ __forceinline__ void perm_body(const PermArgs& A, int* cnt, uint16_t* sA, uint32_t* sW,
-                                          int16_t* sY, uint32_t* sBound) {
+                                          int16_t* sY, uint32_t* sBound, uint16_t* sList) {
   __shared__ int warpTot[kPermThreads / 32];
+  __shared__ int nList;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int L = A.L;
   const uint32_t perm = A.perm_base + blockIdx.x;
@@ -96,6 +97,7 @@ __device__ __forceinline__ void perm_body(const PermArgs& A, int* cnt, uint16_t*
   };
 
   for (int b = tid; b < kBuckets; b += kPermThreads) cnt[b] = 0;
+  if (tid == 0) nList = 0;
   if (sY)
     for (int q = tid; q < L; q += kPermThreads) sY[q] = __ldg(A.Ylab + q);
   // row-start bitmap of the label path: bit p set when a grid row starts at
@@ -177,7 +179,8 @@ __device__ __forceinline__ void perm_body(const PermArgs& A, int* cnt, uint16_t*
     }
   }
   __syncthreads();
-  // cnt[b] now holds the end of bucket b
+  // cnt[b] now holds the end of bucket b.  The buckets to shuffle go to a
+  // list first, so that the threads share the shuffles evenly.
   for (int b = tid; b < kBuckets; b += kPermThreads) {
     const int s0 = b == 0 ? 0 : cnt[b - 1];
     const int sz = cnt[b] - s0;
@@ -195,6 +198,13 @@ __device__ __forceinline__ void perm_body(const PermArgs& A, int* cnt, uint16_t*
         }
       if (inside) continue;
     }
+    sList[atomicAdd(&nList, 1)] = (uint16_t)b;
+  }
+  __syncthreads();
+  for (int w = tid; w < nList; w += kPermThreads) {
+    const int b = sList[w];
+    const int s0 = b == 0 ? 0 : cnt[b - 1];
+    const int sz = cnt[b] - s0;
     uint16_t* a = sA + s0;
     // canonical (increasing) order inside the bucket
     for (int i = 1; i < sz; ++i) {
@@ -239,16 +249,17 @@ __device__ __forceinline__ void perm_body(const PermArgs& A, int* cnt, uint16_t*
 __global__ void __launch_bounds__(kPermThreads) perm_kernel(const PermArgs A) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   int* cnt = reinterpret_cast<int*>(smem_raw);
-  uint32_t* sBound = reinterpret_cast<uint32_t*>(cnt + kBuckets);
+  uint16_t* sList = reinterpret_cast<uint16_t*>(cnt + kBuckets);
+  uint32_t* sBound = reinterpret_cast<uint32_t*>(sList + kBuckets);
   unsigned char* rest = reinterpret_cast<unsigned char*>(sBound + perm_bound_words(A.L));
   int16_t* sY = (A.X && perm_stage_ylab(A.L))
                     ? reinterpret_cast<int16_t*>(smem_raw + perm_base_smem(A.L))
                     : nullptr;
   if (A.L <= kPermWordsMaxL) {
     uint32_t* sW = reinterpret_cast<uint32_t*>(rest);
-    perm_body<true>(A, cnt, reinterpret_cast<uint16_t*>(sW + A.L), sW, sY, sBound);
+    perm_body<true>(A, cnt, reinterpret_cast<uint16_t*>(sW + A.L), sW, sY, sBound, sList);
   } else {
-    perm_body<false>(A, cnt, reinterpret_cast<uint16_t*>(rest), nullptr, sY, sBound);
+    perm_body<false>(A, cnt, reinterpret_cast<uint16_t*>(rest), nullptr, sY, sBound, sList);
   }
 }
 
