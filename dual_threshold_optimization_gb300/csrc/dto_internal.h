@@ -10,32 +10,34 @@ namespace dto {
 #endif
 constexpr int kGridWarps = DTO_GRID_WARPS;  // warps per CTA of the grid kernel (one task per warp)
 constexpr int kCandCap = 64;         // per-warp candidate buffer of the screen
-#ifndef DTO_PERM_THREADS
-#define DTO_PERM_THREADS 1024
-#endif
 #ifndef DTO_BUCKET_BITS
 #define DTO_BUCKET_BITS 12
 #endif
-constexpr int kPermThreads = DTO_PERM_THREADS;  // threads per CTA of the permutation kernel
 constexpr int kBucketBits = DTO_BUCKET_BITS;
 constexpr int kBuckets = 1 << kBucketBits;  // Rao-Sandelius buckets
-static_assert(kBuckets % kPermThreads == 0 && kPermThreads % 32 == 0 && kPermThreads <= 1024,
-              "perm_kernel: buckets must split evenly over its warps");
-// Longest list whose Philox words the permutation kernel keeps in shared
+static_assert(kBuckets % 1024 == 0, "perm_kernel: buckets must split evenly over its warps");
+// Longest list whose Philox words the permutation kernel may keep in shared
 // memory (4 + 2 bytes an element + the counters and the bucket list: 220 KB
 // at 32,768).
-constexpr int kPermWordsMaxL = 32768;
-// Shared-memory budget of the permutation kernel: the label table Ylab is
+#ifndef DTO_PERM_WORDS_MAXL
+#define DTO_PERM_WORDS_MAXL 32768
+#endif
+constexpr int kPermWordsMaxL = DTO_PERM_WORDS_MAXL;
+// Shared-memory budget of one permutation CTA.  The label table Ylab is
 // staged there (random 2-byte gathers hit shared-memory banks instead of L1
 // sectors) when it fits beside the counters, the words and the indices.
 constexpr size_t kPermSmemBudget = 226 * 1024;  // 227 KB per block, less the static arrays
-__host__ __device__ constexpr size_t perm_bound_words(int L) { return ((size_t)L + 32 + 31) / 32; }
-__host__ __device__ constexpr size_t perm_base_smem(int L) {
-  return (size_t)kBuckets * 4 + (size_t)kBuckets * 2 + (L <= kPermWordsMaxL ? (size_t)L * 4 : 0) +
-         (((size_t)L * 2 + 15) & ~(size_t)15) + perm_bound_words(L) * 4;
+__host__ __device__ constexpr size_t perm_round16(size_t b) { return (b + 15) & ~(size_t)15; }
+// row-start bitmap words (positions 0..L+32), a multiple of four
+__host__ __device__ constexpr size_t perm_bound_words(int L) { return (((size_t)L + 32 + 127) / 128) * 4; }
+// counters | bucket list | row-start bitmap | indices | words (when kept);
+// every region starts on a 16-byte boundary, the staged labels follow
+__host__ __device__ constexpr size_t perm_base_smem(int L, bool words) {
+  return (size_t)kBuckets * 4 + (size_t)kBuckets * 2 + perm_bound_words(L) * 4 + perm_round16((size_t)L * 2) +
+         (words ? perm_round16((size_t)L * 4) : 0);
 }
-__host__ __device__ constexpr bool perm_stage_ylab(int L) {
-  return perm_base_smem(L) + (((size_t)L * 2 + 15) & ~(size_t)15) <= kPermSmemBudget;
+__host__ __device__ constexpr bool perm_stage_ylab(int L, bool words) {
+  return perm_base_smem(L, words) + perm_round16((size_t)L * 2) <= kPermSmemBudget;
 }
 constexpr int kMaxListLen = 65534;   // positions are uint16; overlaps stay below the 0xFFFF "never" mark
 constexpr int kScreenSlack = 5;      // fixed-point units added to the screen threshold
@@ -111,6 +113,9 @@ struct PermArgs {
   // (nullable: every bucket shuffled as the specification says).
   const int* rowstart;
   int n1;
+  // set by launch_perm: the words are kept in shared memory / the labels
+  // staged there
+  int words, stage;
 };
 
 struct ComposeArgs {

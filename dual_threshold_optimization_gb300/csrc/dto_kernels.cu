@@ -69,14 +69,15 @@ __device__ __forceinline__ uint32_t bucket_of(uint4 w, int q) {
 }
 
 // One CTA per permutation.  Shared memory: the bucket counters (int32,
-// kBuckets; after the scatter they hold each bucket's end), the shuffled
-// element indices (uint16, L) and, for L <= kPermWordsMaxL, every element's
-// Philox word (uint32, L), so that the scatter and the shuffle draws reuse
-// the words of the counting pass; longer lists recompute a word where it is
-// needed.  kBuckets = 4096 keeps buckets at a few elements for the list
+// kBuckets; after the scatter they hold each bucket's end), the list of
+// buckets to shuffle, the row-start bitmap, the shuffled element indices
+// (uint16, L), where the launch keeps them every element's Philox word
+// (uint32, L), so that the scatter and the shuffle draws reuse the words of
+// the counting pass (otherwise a word is recomputed where it is needed),
+// and where it fits the label table.  kBuckets = 4096 keeps buckets at a few elements for the list
 // lengths of interest, so the per-bucket canonical sort and Fisher-Yates are
 // a few operations per element.
-template <bool kWords>
+template <bool kWords, int kPermThreads>
 __device__ __forceinline__ void perm_body(const PermArgs& A, int* cnt, uint16_t* sA, uint32_t* sW,
                                           int16_t* sY, uint32_t* sBound, uint16_t* sList) {
   __shared__ int warpTot[kPermThreads / 32];
@@ -98,8 +99,22 @@ __device__ __forceinline__ void perm_body(const PermArgs& A, int* cnt, uint16_t*
 
   for (int b = tid; b < kBuckets; b += kPermThreads) cnt[b] = 0;
   if (tid == 0) nList = 0;
-  if (sY)
+  // the label table goes to shared memory by asynchronous 16-byte copies
+  // that land while the words are drawn (waited for before the gather)
+  const bool asyncY = sY && (reinterpret_cast<uintptr_t>(A.Ylab) & 15) == 0;
+  if (asyncY) {
+    const char* src = reinterpret_cast<const char*>(A.Ylab);
+    const uint32_t dst = (uint32_t)__cvta_generic_to_shared(sY);
+    const int bytes = 2 * L;
+    for (int o = 16 * tid; o < bytes; o += 16 * kPermThreads) {
+      const int n = min(16, bytes - o);
+      asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(dst + o), "l"(src + o), "r"(n)
+                   : "memory");
+    }
+    asm volatile("cp.async.commit_group;\n" ::: "memory");
+  } else if (sY) {
     for (int q = tid; q < L; q += kPermThreads) sY[q] = __ldg(A.Ylab + q);
+  }
   // row-start bitmap of the label path: bit p set when a grid row starts at
   // position p (positions past the last row form one more range)
   const bool rows = A.X && A.rowstart;
@@ -190,12 +205,17 @@ __device__ __forceinline__ void perm_body(const PermArgs& A, int* cnt, uint16_t*
       // bucket inside one row gives the same multisets in any order (the
       // sort and the Fisher-Yates pass only decide which of its elements
       // fall on which side of a row start)
+      const int lo = s0 + 1, hi = s0 + sz - 1;  // no row may start at lo..hi
       bool inside = true;
-      for (int p = s0 + 1; p < s0 + sz; ++p)
-        if (sBound[p >> 5] & (1u << (p & 31))) {
+      for (int w = lo >> 5; w <= (hi >> 5); ++w) {
+        uint32_t bits = sBound[w];
+        if (w == (lo >> 5)) bits &= 0xFFFFFFFFu << (lo & 31);
+        if (w == (hi >> 5)) bits &= 0xFFFFFFFFu >> (31 - (hi & 31));
+        if (bits) {
           inside = false;
           break;
         }
+      }
       if (inside) continue;
     }
     sList[atomicAdd(&nList, 1)] = (uint16_t)b;
@@ -232,13 +252,32 @@ __device__ __forceinline__ void perm_body(const PermArgs& A, int* cnt, uint16_t*
       a[j] = tmp;
     }
   }
+  if (asyncY) asm volatile("cp.async.wait_all;\n" ::: "memory");
   __syncthreads();
   if (A.X) {
     int16_t* xo = A.X + (long long)blockIdx.x * A.xstride;
-    if (sY)
+    if ((reinterpret_cast<uintptr_t>(xo) & 15) == 0 && (A.xstride & 7) == 0) {
+      // eight labels per 16-byte store; the row's padding past L gets -1
+      const int chunks = (L + 7) >> 3;
+      for (int c = tid; c < chunks; c += kPermThreads) {
+        const uint4 ix = reinterpret_cast<const uint4*>(sA)[c];
+        const uint32_t iw[4] = {ix.x, ix.y, ix.z, ix.w};
+        uint32_t ow[4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+          const int p = 8 * c + 2 * k;
+          const int i0 = iw[k] & 0xFFFF, i1 = iw[k] >> 16;
+          const int16_t v0 = p < L ? (sY ? sY[i0] : __ldg(A.Ylab + i0)) : (int16_t)-1;
+          const int16_t v1 = p + 1 < L ? (sY ? sY[i1] : __ldg(A.Ylab + i1)) : (int16_t)-1;
+          ow[k] = (uint32_t)(uint16_t)v0 | ((uint32_t)(uint16_t)v1 << 16);
+        }
+        reinterpret_cast<uint4*>(xo)[c] = make_uint4(ow[0], ow[1], ow[2], ow[3]);
+      }
+    } else if (sY) {
       for (int p = tid; p < L; p += kPermThreads) xo[p] = sY[sA[p]];
-    else
+    } else {
       for (int p = tid; p < L; p += kPermThreads) xo[p] = __ldg(A.Ylab + sA[p]);
+    }
   }
   if (A.sigma) {
     int* so = A.sigma + (long long)blockIdx.x * A.sstride;
@@ -246,20 +285,19 @@ __device__ __forceinline__ void perm_body(const PermArgs& A, int* cnt, uint16_t*
   }
 }
 
+template <int kPermThreads>
 __global__ void __launch_bounds__(kPermThreads) perm_kernel(const PermArgs A) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   int* cnt = reinterpret_cast<int*>(smem_raw);
   uint16_t* sList = reinterpret_cast<uint16_t*>(cnt + kBuckets);
   uint32_t* sBound = reinterpret_cast<uint32_t*>(sList + kBuckets);
-  unsigned char* rest = reinterpret_cast<unsigned char*>(sBound + perm_bound_words(A.L));
-  int16_t* sY = (A.X && perm_stage_ylab(A.L))
-                    ? reinterpret_cast<int16_t*>(smem_raw + perm_base_smem(A.L))
-                    : nullptr;
-  if (A.L <= kPermWordsMaxL) {
-    uint32_t* sW = reinterpret_cast<uint32_t*>(rest);
-    perm_body<true>(A, cnt, reinterpret_cast<uint16_t*>(sW + A.L), sW, sY, sBound, sList);
+  uint16_t* sA = reinterpret_cast<uint16_t*>(sBound + perm_bound_words(A.L));
+  int16_t* sY = A.stage ? reinterpret_cast<int16_t*>(smem_raw + perm_base_smem(A.L, A.words)) : nullptr;
+  if (A.words) {
+    uint32_t* sW = reinterpret_cast<uint32_t*>(reinterpret_cast<unsigned char*>(sA) + perm_round16((size_t)A.L * 2));
+    perm_body<true, kPermThreads>(A, cnt, sA, sW, sY, sBound, sList);
   } else {
-    perm_body<false>(A, cnt, reinterpret_cast<uint16_t*>(rest), nullptr, sY, sBound, sList);
+    perm_body<false, kPermThreads>(A, cnt, sA, nullptr, sY, sBound, sList);
   }
 }
 
@@ -355,12 +393,49 @@ cudaError_t raise_smem_limit(const void* kernel, size_t bytes) {
   return e;
 }
 
-cudaError_t launch_perm(const PermArgs& a, int count, cudaStream_t s) {
+// Shared-memory layout of a permutation launch.  Keeping the words saves
+// recomputing a Philox block per element in the scatter pass; dropping them
+// is worth it only where that lets a second CTA share the SM (the phases of
+// one CTA, separated by barriers, then overlap with the other's).  `ctas`
+// gives the resident CTAs per SM for a dynamic shared-memory size.
+template <class Ctas>
+void perm_layout(int L, bool labels, Ctas ctas, int* words, int* stage, size_t* smem) {
+  auto bytes = [&](bool w, bool* st) {
+    *st = labels && perm_stage_ylab(L, w);
+    return perm_base_smem(L, w) + (*st ? perm_round16((size_t)L * 2) : 0);
+  };
+  bool stW = false, stN = false;
+  const size_t bW = bytes(true, &stW), bN = bytes(false, &stN);
+  const bool keep = L <= kPermWordsMaxL && (ctas(bW) >= 2 || ctas(bN) < 2);
+  *words = keep ? 1 : 0;
+  *stage = (keep ? stW : stN) ? 1 : 0;
+  *smem = keep ? bW : bN;
+}
+
+cudaError_t launch_perm(const PermArgs& a0, int count, cudaStream_t s) {
   if (count <= 0) return cudaSuccess;
-  size_t smem = perm_base_smem(a.L) + ((a.X && perm_stage_ylab(a.L)) ? (((size_t)a.L * 2 + 15) & ~(size_t)15) : 0);
-  cudaError_t e = raise_smem_limit((const void*)perm_kernel, smem);
+  PermArgs a = a0;
+  size_t smem = 0;
+  cudaError_t e = cudaSuccess;
+  // CTAs of 512 threads, two to an SM where the shared memory allows; where
+  // only one fits, CTAs of 1024 threads keep the SM's warps busy
+  auto ctas = [&](size_t bytes) {
+    int n = 0;
+    if (e == cudaSuccess) e = raise_smem_limit((const void*)perm_kernel<512>, bytes);
+    if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, perm_kernel<512>, 512, bytes);
+    return n;
+  };
+  perm_layout(a.L, a.X != nullptr, ctas, &a.words, &a.stage, &smem);
   if (e != cudaSuccess) return e;
-  perm_kernel<<<count, kPermThreads, smem, s>>>(a);
+  const bool pairs = ctas(smem) >= 2;
+  if (e != cudaSuccess) return e;
+  if (pairs) {
+    perm_kernel<512><<<count, 512, smem, s>>>(a);
+  } else {
+    e = raise_smem_limit((const void*)perm_kernel<1024>, smem);
+    if (e != cudaSuccess) return e;
+    perm_kernel<1024><<<count, 1024, smem, s>>>(a);
+  }
   return cudaGetLastError();
 }
 
