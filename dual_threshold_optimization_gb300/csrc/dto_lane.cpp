@@ -54,6 +54,18 @@ constexpr bool kFirstBatchCoop = DTO_FIRST_COOP != 0;
 #define DTO_SIDE_PRIORITY 0
 #endif
 constexpr bool kSidePriority = DTO_SIDE_PRIORITY != 0;
+// Table levels of the last pipelined batch before its exhaustive screen
+// (a CTA per task).  Nothing runs beside that batch's later levels, but the
+// table sweeps still beat the exhaustive screen on its hardest tasks: 3
+// levels measured 36.9 ms per 100,000 permutations at N = 20,000, 2 levels
+// 38.7 ms, 1 level 44.6 ms.
+#ifndef DTO_LAST_LEVELS
+#define DTO_LAST_LEVELS 3
+#endif
+constexpr int kLastLevels = DTO_LAST_LEVELS;
+// How far (in nats of ln p) a run's ladder bounds may lie from the pair's
+// stored ladder before they replace it.
+constexpr double kLadderSlack = 0.1;
 
 int set_err(dto_ctx* ctx, int code, const std::string& msg) {
   if (ctx) ctx->err = msg;
@@ -435,7 +447,13 @@ int make_labels_launch(Lane* L, dto_pair* P, uint64_t seed, uint32_t first, int 
 // Bounds of the table levels from a sample of minimum p-values: the
 // 90th percentile (level 0), the 99th (level 1), one nat above the maximum
 // (level 2), as fixed-point ln p, each above the one before.
-void ladder_of(std::vector<double> v, int fshift, int tau[6]) {
+void ladder_of(const std::vector<double>& all, int fshift, int tau[6]) {
+  // the quantiles from an evenly strided sample of at most 16,384 minima
+  // (the permutations are in random order), the maximum from all of them
+  const size_t stride = (all.size() + 16383) / 16384;
+  std::vector<double> v;
+  v.reserve(all.size() / std::max<size_t>(stride, 1) + 1);
+  for (size_t i = 0; i < all.size(); i += std::max<size_t>(stride, 1)) v.push_back(all[i]);
   auto q = [&](double f) {
     const size_t k = (size_t)(f * (double)(v.size() - 1));
     std::nth_element(v.begin(), v.begin() + (long)k, v.end());
@@ -443,7 +461,7 @@ void ladder_of(std::vector<double> v, int fshift, int tau[6]) {
   };
   const double p90 = q(kLevel0Quantile);
   const double p99 = q(0.99);
-  const double pmax = std::max(*std::max_element(v.begin(), v.end()), 1e-300);
+  const double pmax = std::max(*std::max_element(all.begin(), all.end()), 1e-300);
   tau[0] = fixed_log(p90, fshift);
   tau[1] = std::max(fixed_log(p99, fshift), tau[0] + 1);
   tau[2] = std::max((int)std::min(0.0, std::floor((std::log(pmax) + 1.0) * std::ldexp(1.0, fshift))), tau[1] + 1);
@@ -696,18 +714,26 @@ int lane_run_range(Lane* L, dto_pair* P, uint32_t perm_first, int64_t n_perm, ui
       const int si = (int)(it % Lane::kSlots);
       LCK(cudaStreamWaitEvent(sl.side, sl.ev[6], 0));
       LCK(cudaEventRecord(sl.ev[4], sl.side));
-      rc = table_levels(L, P, X, xs, cnt, dR, 1, nlev, (int*)sl.dFall, sl.dCnt, sl.side, 1 + si);
+      const int nl = it + 1 == npipe ? std::min(nlev, kLastLevels) : nlev;
+      rc = table_levels(L, P, X, xs, cnt, dR, 1, nl, (int*)sl.dFall, sl.dCnt, sl.side, 1 + si);
       if (rc) return rc;
-      rc = table_exhaustive(L, P, X, xs, cnt, dR, nlev, (const int*)sl.dFall, sl.dCnt, sl.side);
+      rc = table_exhaustive(L, P, X, xs, cnt, dR, nl, (const int*)sl.dFall, sl.dCnt, sl.side);
       if (rc) return rc;
       LCK(cudaEventRecord(sl.ev[5], sl.side));
       LCK(cudaMemcpyAsync(sl.hRes, dR, (size_t)cnt * sizeof(TaskResult), cudaMemcpyDeviceToHost, sl.side));
       LCK(cudaEventRecord(sl.ev[7], sl.side));
       sl.busy = true;
     }
-    for (BatchSlot& sl : L->slot) {
-      if (sl.busy) {
-        rc = harvest(sl);
+    // the batches still in flight, oldest first: the host takes each one's
+    // results while the later ones still run
+    {
+      BatchSlot* order[Lane::kSlots];
+      int nb = 0;
+      for (BatchSlot& sl : L->slot)
+        if (sl.busy) order[nb++] = &sl;
+      std::sort(order, order + nb, [](const BatchSlot* a, const BatchSlot* b) { return a->b0 < b->b0; });
+      for (int k = 0; k < nb; ++k) {
+        rc = harvest(*order[k]);
         if (rc) return rc;
       }
     }
@@ -715,12 +741,21 @@ int lane_run_range(Lane* L, dto_pair* P, uint32_t perm_first, int64_t n_perm, ui
       rc = first_done();
       if (rc) return rc;
     }
-    // this run's minimum p-values set the ladder of the pair's next run
+    // this run's minimum p-values set the ladder of the pair's next run.
+    // The bounds are quantiles of the pair's null distribution, so another
+    // seed moves them a little; the ladder is replaced only when a bound has
+    // moved by more than kLadderSlack nats, which spares the next run the
+    // rebuild of the table screens (they are screens: any bounds give the
+    // same results).
     {
       int t[6];
       ladder_of(minp, P->fshift, t);
+      const long long slack = (long long)std::ldexp(kLadderSlack, P->fshift);
       std::lock_guard<std::mutex> g(P->ladder_mu);
-      for (int l = 0; l < 6; ++l) P->ladder_tau[l] = t[l];
+      bool keep = P->ladder_ok;
+      for (int l = 0; l < 6 && keep; ++l) keep = std::llabs((long long)t[l] - P->ladder_tau[l]) <= slack;
+      if (!keep)
+        for (int l = 0; l < 6; ++l) P->ladder_tau[l] = t[l];
       P->ladder_ok = true;
     }
     // the main stream's timing event follows the side streams' last work
