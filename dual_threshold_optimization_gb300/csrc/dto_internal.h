@@ -17,8 +17,7 @@ constexpr int kBucketBits = DTO_BUCKET_BITS;
 constexpr int kBuckets = 1 << kBucketBits;  // Rao-Sandelius buckets
 static_assert(kBuckets % 1024 == 0, "perm_kernel: buckets must split evenly over its warps");
 // Longest list whose Philox words the permutation kernel may keep in shared
-// memory (4 + 2 bytes an element + the counters and the bucket list: 220 KB
-// at 32,768).
+// memory (4 + 2 bytes an element + the counters: 208 KB at 32,768).
 #ifndef DTO_PERM_WORDS_MAXL
 #define DTO_PERM_WORDS_MAXL 32768
 #endif
@@ -28,13 +27,10 @@ constexpr int kPermWordsMaxL = DTO_PERM_WORDS_MAXL;
 // sectors) when it fits beside the counters, the words and the indices.
 constexpr size_t kPermSmemBudget = 226 * 1024;  // 227 KB per block, less the static arrays
 __host__ __device__ constexpr size_t perm_round16(size_t b) { return (b + 15) & ~(size_t)15; }
-// row-start bitmap words (positions 0..L+32), a multiple of four
-__host__ __device__ constexpr size_t perm_bound_words(int L) { return (((size_t)L + 32 + 127) / 128) * 4; }
-// counters | bucket list | row-start bitmap | indices | words (when kept);
-// every region starts on a 16-byte boundary, the staged labels follow
+// counters | indices | words (when kept); every region starts on a 16-byte
+// boundary, the staged labels follow
 __host__ __device__ constexpr size_t perm_base_smem(int L, bool words) {
-  return (size_t)kBuckets * 4 + (size_t)kBuckets * 2 + perm_bound_words(L) * 4 + perm_round16((size_t)L * 2) +
-         (words ? perm_round16((size_t)L * 4) : 0);
+  return (size_t)kBuckets * 4 + perm_round16((size_t)L * 2) + (words ? perm_round16((size_t)L * 4) : 0);
 }
 __host__ __device__ constexpr bool perm_stage_ylab(int L, bool words) {
   return perm_base_smem(L, words) + perm_round16((size_t)L * 2) <= kPermSmemBudget;

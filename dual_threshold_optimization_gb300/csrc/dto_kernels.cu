@@ -69,8 +69,8 @@ __device__ __forceinline__ uint32_t bucket_of(uint4 w, int q) {
 }
 
 // One CTA per permutation.  Shared memory: the bucket counters (int32,
-// kBuckets; after the scatter they hold each bucket's end), the list of
-// buckets to shuffle, the row-start bitmap, the shuffled element indices
+// kBuckets; after the scatter they hold each bucket's end), the shuffled
+// element indices
 // (uint16, L), where the launch keeps them every element's Philox word
 // (uint32, L), so that the scatter and the shuffle draws reuse the words of
 // the counting pass (otherwise a word is recomputed where it is needed),
@@ -79,9 +79,8 @@ __device__ __forceinline__ uint32_t bucket_of(uint4 w, int q) {
 // a few operations per element.
 template <bool kWords, int kPermThreads>
 __device__ __forceinline__ void perm_body(const PermArgs& A, int* cnt, uint16_t* sA, uint32_t* sW,
-                                          int16_t* sY, uint32_t* sBound, uint16_t* sList) {
+                                          int16_t* sY) {
   __shared__ int warpTot[kPermThreads / 32];
-  __shared__ int nList;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int L = A.L;
   const uint32_t perm = A.perm_base + blockIdx.x;
@@ -98,7 +97,6 @@ __device__ __forceinline__ void perm_body(const PermArgs& A, int* cnt, uint16_t*
   };
 
   for (int b = tid; b < kBuckets; b += kPermThreads) cnt[b] = 0;
-  if (tid == 0) nList = 0;
   // the label table goes to shared memory by asynchronous 16-byte copies
   // that land while the words are drawn (waited for before the gather)
   const bool asyncY = sY && (reinterpret_cast<uintptr_t>(A.Ylab) & 15) == 0;
@@ -115,17 +113,15 @@ __device__ __forceinline__ void perm_body(const PermArgs& A, int* cnt, uint16_t*
   } else if (sY) {
     for (int q = tid; q < L; q += kPermThreads) sY[q] = __ldg(A.Ylab + q);
   }
-  // row-start bitmap of the label path: bit p set when a grid row starts at
-  // position p (positions past the last row form one more range)
   const bool rows = A.X && A.rowstart;
-  if (rows)
-    for (int q = tid; q < (int)perm_bound_words(L); q += kPermThreads) sBound[q] = 0;
+  // this thread's first two row starts (and the ones before them), loaded
+  // now so that the loads are done by the time the shuffles need them
+  const int r1 = tid + kPermThreads;
+  const int rsPrev0 = (rows && tid >= 1 && tid <= A.n1) ? __ldg(A.rowstart + tid - 1) : 0;
+  const int rs0 = (rows && tid <= A.n1) ? __ldg(A.rowstart + tid) : 0;
+  const int rsPrev1 = (rows && r1 <= A.n1) ? __ldg(A.rowstart + r1 - 1) : 0;
+  const int rs1 = (rows && r1 <= A.n1) ? __ldg(A.rowstart + r1) : 0;
   __syncthreads();
-  if (rows)
-    for (int r = tid; r <= A.n1; r += kPermThreads) {
-      const int p = __ldg(A.rowstart + r);
-      atomicOr(&sBound[p >> 5], 1u << (p & 31));
-    }
   const int groups = (L + 3) >> 2;
   for (int g = tid; g < groups; g += kPermThreads) {
     uint4 w = philox4x32_10(make_uint4((uint32_t)g, perm, A.pair_id, tagB), k0, k1);
@@ -194,39 +190,10 @@ __device__ __forceinline__ void perm_body(const PermArgs& A, int* cnt, uint16_t*
     }
   }
   __syncthreads();
-  // cnt[b] now holds the end of bucket b.  The buckets to shuffle go to a
-  // list first, so that the threads share the shuffles evenly.
-  for (int b = tid; b < kBuckets; b += kPermThreads) {
-    const int s0 = b == 0 ? 0 : cnt[b - 1];
-    const int sz = cnt[b] - s0;
-    if (sz < 2) continue;
-    if (rows) {
-      // labels only: the search sees each row's multiset of labels, and a
-      // bucket inside one row gives the same multisets in any order (the
-      // sort and the Fisher-Yates pass only decide which of its elements
-      // fall on which side of a row start)
-      const int lo = s0 + 1, hi = s0 + sz - 1;  // no row may start at lo..hi
-      bool inside = true;
-      for (int w = lo >> 5; w <= (hi >> 5); ++w) {
-        uint32_t bits = sBound[w];
-        if (w == (lo >> 5)) bits &= 0xFFFFFFFFu << (lo & 31);
-        if (w == (hi >> 5)) bits &= 0xFFFFFFFFu >> (31 - (hi & 31));
-        if (bits) {
-          inside = false;
-          break;
-        }
-      }
-      if (inside) continue;
-    }
-    sList[atomicAdd(&nList, 1)] = (uint16_t)b;
-  }
-  __syncthreads();
-  for (int w = tid; w < nList; w += kPermThreads) {
-    const int b = sList[w];
-    const int s0 = b == 0 ? 0 : cnt[b - 1];
-    const int sz = cnt[b] - s0;
+  // cnt[b] now holds the end of bucket b.  Canonical (increasing) order
+  // inside bucket b, then the forward Fisher-Yates pass.
+  auto shuffle_bucket = [&](int b, int s0, int sz) {
     uint16_t* a = sA + s0;
-    // canonical (increasing) order inside the bucket
     for (int i = 1; i < sz; ++i) {
       uint16_t key = a[i];
       int j = i - 1;
@@ -250,6 +217,32 @@ __device__ __forceinline__ void perm_body(const PermArgs& A, int* cnt, uint16_t*
       const uint16_t tmp = a[i];
       a[i] = a[j];
       a[j] = tmp;
+    }
+  };
+  if (rows) {
+    // Labels only: the search sees each grid row's multiset of labels, and a
+    // bucket inside one row gives the same multisets in any order (the sort
+    // and the Fisher-Yates pass only decide which of its elements fall on
+    // which side of a row start).  So only the buckets with a row start
+    // strictly inside are shuffled: each row start finds its bucket from the
+    // word of the element the scatter put there, and the lowest row start
+    // inside a bucket takes it.  (Positions past the last row form one more
+    // range.)
+    for (int r = tid, u = 0; r <= A.n1; r += kPermThreads, ++u) {
+      const int p = u == 0 ? rs0 : u == 1 ? rs1 : __ldg(A.rowstart + r);
+      if (p <= 0 || p >= L) continue;
+      const int lo = (int)(word_of(sA[p]) >> kLowBits);  // the bucket holding position p
+      const int s0 = lo == 0 ? 0 : cnt[lo - 1];
+      if (s0 >= p) continue;                                // p starts the bucket
+      const int prev = u == 0 ? rsPrev0 : u == 1 ? rsPrev1 : __ldg(A.rowstart + r - 1);
+      if (r > 0 && prev > s0) continue;  // a lower row start takes it
+      shuffle_bucket(lo, s0, cnt[lo] - s0);
+    }
+  } else {
+    for (int b = tid; b < kBuckets; b += kPermThreads) {
+      const int s0 = b == 0 ? 0 : cnt[b - 1];
+      const int sz = cnt[b] - s0;
+      if (sz >= 2) shuffle_bucket(b, s0, sz);
     }
   }
   if (asyncY) asm volatile("cp.async.wait_all;\n" ::: "memory");
@@ -289,15 +282,13 @@ template <int kPermThreads>
 __global__ void __launch_bounds__(kPermThreads) perm_kernel(const PermArgs A) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   int* cnt = reinterpret_cast<int*>(smem_raw);
-  uint16_t* sList = reinterpret_cast<uint16_t*>(cnt + kBuckets);
-  uint32_t* sBound = reinterpret_cast<uint32_t*>(sList + kBuckets);
-  uint16_t* sA = reinterpret_cast<uint16_t*>(sBound + perm_bound_words(A.L));
+  uint16_t* sA = reinterpret_cast<uint16_t*>(cnt + kBuckets);
   int16_t* sY = A.stage ? reinterpret_cast<int16_t*>(smem_raw + perm_base_smem(A.L, A.words)) : nullptr;
   if (A.words) {
     uint32_t* sW = reinterpret_cast<uint32_t*>(reinterpret_cast<unsigned char*>(sA) + perm_round16((size_t)A.L * 2));
-    perm_body<true, kPermThreads>(A, cnt, sA, sW, sY, sBound, sList);
+    perm_body<true, kPermThreads>(A, cnt, sA, sW, sY);
   } else {
-    perm_body<false, kPermThreads>(A, cnt, sA, nullptr, sY, sBound, sList);
+    perm_body<false, kPermThreads>(A, cnt, sA, nullptr, sY);
   }
 }
 

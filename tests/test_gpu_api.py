@@ -100,7 +100,7 @@ def test_run_range_splits_reproduce_one_run():
     assert np.array_equal(np.concatenate([a.minp, b.minp]), whole.minp)
 
 
-@pytest.mark.parametrize("N", [11180, 11190, 14830, 14840, 22020, 22030, 24440, 24460, 25440, 25470, 32760, 32780])
+@pytest.mark.parametrize("N", [12380, 12390, 16510, 16520, 24760, 24775, 26875, 26890, 32760, 32780, 49530, 49540, 53755, 53770])
 def test_shared_memory_limits_at_list_lengths(engine, N):
     # list lengths around the permutation kernel's shared-memory switches
     # (label staging, kept words): the launches fit and agree with the spec
