@@ -62,7 +62,8 @@ def build(force=False, verbose=False, jobs=None):
                   "DTO_TABLE_WARPS", "DTO_TABLE_MINB", "DTO_TABLE_TASKS", "DTO_FIRST_BATCH",
                   "DTO_FIRST_COOP", "DTO_LADDER_LEVELS", "DTO_SIDE_PRIORITY",
                   "DTO_TIGHT_TABLES", "DTO_EARLY_HITS", "DTO_SLOTS", "DTO_PERM_WORDS_MAXL",
-                  "DTO_LAST_LEVELS", "DTO_BATCH_SHIFT"):
+                  "DTO_LAST_LEVELS", "DTO_BATCH_SHIFT",
+                  "DTO_TIGHT_LEVELS"):
         if os.environ.get(knob):
             flags += ["-D%s=%d" % (knob, int(os.environ[knob]))]
     if os.environ.get("DTO_L0_QUANTILE"):

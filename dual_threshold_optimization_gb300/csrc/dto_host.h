@@ -46,6 +46,11 @@ struct BatchSlot {
 
 constexpr int kSlotsMax = 4;
 
+// The ladder's fixed-point bounds: levels 0..2, then three tighter tables
+// per level.
+constexpr int kLadderTaus = 12;
+constexpr int tight_slot(int level, int q) { return 3 + 3 * level + q; }
+
 struct Lane {
   dto_ctx* ctx = nullptr;
   std::string* err = nullptr;  // where this lane's error messages go
@@ -90,9 +95,9 @@ struct Lane {
   static_assert(kSlots >= 2 && kSlots <= kSlotsMax, "two to four batch slots");
   BatchSlot slot[kSlots];
   // table screens of the pair this lane last ran: the ladder's levels 0..2,
-  // then the tighter tables 3..5 a level-0 sweep switches to once a task's
-  // bound is known
-  static constexpr int kTables = 6;
+  // then three tighter tables per level (tight_slot) that a sweep switches
+  // to once a task's bound is known
+  static constexpr int kTables = kLadderTaus;
   uint16_t* dKthr[kTables] = {};
   size_t kthrBytes[kTables] = {};
   unsigned long long kthr_pair[kTables] = {};  // pair serial the table was built for (0: none)
@@ -144,7 +149,7 @@ struct dto_pair {
   // run starts its pipeline with it instead of measuring a first batch.
   std::mutex ladder_mu;
   bool ladder_ok = false;
-  int ladder_tau[6] = {0, 0, 0, 0, 0, 0};
+  int ladder_tau[dto::kLadderTaus] = {};
 };
 
 namespace dto {

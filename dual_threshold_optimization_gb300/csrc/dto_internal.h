@@ -178,9 +178,9 @@ struct TableGridArgs {
   int ntask;
   int tau;                // the guess the table was built for
   const uint16_t* kthr;   // [n1][table_cq(C) / 8][32][8]
-  // tighter tables (bounds tight_tau[0] > tight_tau[1] > ...), for level 0:
-  // once a resolve has set a task's bound B, its remaining rows are swept
-  // against the tightest table whose bound is still >= B
+  // tighter tables (bounds tight_tau[0] > tight_tau[1] > ...): once a
+  // resolve has set a task's bound B, its remaining rows are swept against
+  // the tightest table whose bound is still >= B
   const uint16_t* tight[3];
   int tight_tau[3];
   int ntight;

@@ -39,12 +39,17 @@ constexpr long long kFirstBatch = DTO_FIRST_BATCH;
 #endif
 constexpr int kLadderLevels = DTO_LADDER_LEVELS;
 static_assert(kLadderLevels == 2 || kLadderLevels == 3, "two or three table levels");
-// Tighter tables a level-0 sweep may switch to (0 to 3).
+// Tighter tables a sweep may switch to (0 to 3), for the levels below
+// kTightLevels.
 #ifndef DTO_TIGHT_TABLES
 #define DTO_TIGHT_TABLES 3
 #endif
 constexpr int kTightTables = DTO_TIGHT_TABLES;
 static_assert(kTightTables >= 0 && kTightTables <= 3, "at most three tighter tables");
+#ifndef DTO_TIGHT_LEVELS
+#define DTO_TIGHT_LEVELS 3
+#endif
+constexpr int kTightLevels = DTO_TIGHT_LEVELS;
 // The first batch's screen with a CTA per task (see grid_kernel).
 #ifndef DTO_FIRST_COOP
 #define DTO_FIRST_COOP 1
@@ -317,10 +322,10 @@ int table_levels(Lane* L, dto_pair* P, const int16_t* X, long long xstride, int 
     a.ntask = ntask;
     a.tau = L->kthr_tau[level];
     a.kthr = L->dKthr[level];
-    a.ntight = level == 0 ? kTightTables : 0;
+    a.ntight = level < kTightLevels ? kTightTables : 0;
     for (int q = 0; q < a.ntight; ++q) {
-      a.tight[q] = L->dKthr[3 + q];
-      a.tight_tau[q] = L->kthr_tau[3 + q];
+      a.tight[q] = L->dKthr[tight_slot(level, q)];
+      a.tight_tau[q] = L->kthr_tau[tight_slot(level, q)];
     }
     a.packed = P->ncommon <= kPackedMaxCommon ? 1 : 0;
     a.smemF = table_smem_bytes(P->C, P->dev.n1, P->dev.n2, P->npop, 1) <= L->ctx->smem_optin ? 1 : 0;
@@ -454,8 +459,9 @@ int make_labels_launch(Lane* L, dto_pair* P, uint64_t seed, uint32_t first, int 
 
 // Bounds of the table levels from a sample of minimum p-values: the
 // 90th percentile (level 0), the 99th (level 1), one nat above the maximum
-// (level 2), as fixed-point ln p, each above the one before.
-void ladder_of(const std::vector<double>& all, int fshift, int tau[6]) {
+// (level 2), as fixed-point ln p, each above the one before; then each
+// level's three tighter tables (kLadderTaus entries in all).
+void ladder_of(const std::vector<double>& all, int fshift, int tau[kLadderTaus]) {
   // the quantiles from an evenly strided sample of at most 16,384 minima
   // (the permutations are in random order), the maximum from all of them
   const size_t stride = (all.size() + 16383) / 16384;
@@ -474,12 +480,17 @@ void ladder_of(const std::vector<double>& all, int fshift, int tau[6]) {
   tau[1] = std::max(fixed_log(p99, fshift), tau[0] + 1);
   tau[2] = std::max((int)std::min(0.0, std::floor((std::log(pmax) + 1.0) * std::ldexp(1.0, fshift))), tau[1] + 1);
   if (kLadderLevels == 2) tau[1] = tau[2];
-  // the tighter tables of the level-0 sweep: 50th, 10th and 1st percentiles
-  const double ptight[3] = {q(0.5), q(0.1), q(0.01)};
-  int prev = tau[0];
-  for (int t = 0; t < 3; ++t) {
-    tau[3 + t] = std::min(fixed_log(ptight[t], fshift), prev - 1);
-    prev = tau[3 + t];
+  // the tighter tables a sweep switches to once a task's bound is known,
+  // each below the one before: for level 0 the 50th, 10th and 1st
+  // percentiles, for level 1 the 98th, 96th and 93rd, for level 2 the
+  // maximum, the 99.9th and the 99.5th
+  const double ptight[3][3] = {{q(0.5), q(0.1), q(0.01)}, {q(0.98), q(0.96), q(0.93)}, {pmax, q(0.999), q(0.995)}};
+  for (int l = 0; l < 3; ++l) {
+    int prev = tau[l];
+    for (int t = 0; t < 3; ++t) {
+      tau[tight_slot(l, t)] = std::min(fixed_log(ptight[l][t], fshift), prev - 1);
+      prev = tau[tight_slot(l, t)];
+    }
   }
 }
 
@@ -596,13 +607,13 @@ int lane_run_range(Lane* L, dto_pair* P, uint32_t perm_first, int64_t n_perm, ui
     // first batch's slowest tasks (the permutations with the largest minimum
     // p) take several times a typical task; meanwhile the main stream draws
     // the labels of the first two pipelined batches.
-    int tau[6] = {0, 0, 0, 0, 0, 0};
+    int tau[kLadderTaus] = {};
     bool warm = false;
     {
       std::lock_guard<std::mutex> g(P->ladder_mu);
       if (P->ladder_ok) {
         warm = true;
-        for (int l = 0; l < 6; ++l) tau[l] = P->ladder_tau[l];
+        for (int l = 0; l < kLadderTaus; ++l) tau[l] = P->ladder_tau[l];
       }
     }
     const int cnt0 = warm ? 0 : (int)first_batch;
@@ -677,10 +688,11 @@ int lane_run_range(Lane* L, dto_pair* P, uint32_t perm_first, int64_t n_perm, ui
       rc = ensure_table(L, P, l, tau[l]);
       if (rc) return rc;
     }
-    for (int l = 0; l < kTightTables; ++l) {
-      rc = ensure_table(L, P, 3 + l, tau[3 + l]);
-      if (rc) return rc;
-    }
+    for (int l = 0; l < std::min(kTightLevels, kLadderLevels); ++l)
+      for (int q = 0; q < kTightTables; ++q) {
+        rc = ensure_table(L, P, tight_slot(l, q), tau[tight_slot(l, q)]);
+        if (rc) return rc;
+      }
     const int nlev = kLadderLevels;
     // Batches in flight: while batch b's later table levels, exhaustive
     // fallback and result copy run on the side stream, the next batches'
@@ -756,14 +768,14 @@ int lane_run_range(Lane* L, dto_pair* P, uint32_t perm_first, int64_t n_perm, ui
     // rebuild of the table screens (they are screens: any bounds give the
     // same results).
     {
-      int t[6];
+      int t[kLadderTaus];
       ladder_of(minp, P->fshift, t);
       const long long slack = (long long)std::ldexp(kLadderSlack, P->fshift);
       std::lock_guard<std::mutex> g(P->ladder_mu);
       bool keep = P->ladder_ok;
-      for (int l = 0; l < 6 && keep; ++l) keep = std::llabs((long long)t[l] - P->ladder_tau[l]) <= slack;
+      for (int l = 0; l < kLadderTaus && keep; ++l) keep = std::llabs((long long)t[l] - P->ladder_tau[l]) <= slack;
       if (!keep)
-        for (int l = 0; l < 6; ++l) P->ladder_tau[l] = t[l];
+        for (int l = 0; l < kLadderTaus; ++l) P->ladder_tau[l] = t[l];
       P->ladder_ok = true;
     }
     // the main stream's timing event follows the side streams' last work

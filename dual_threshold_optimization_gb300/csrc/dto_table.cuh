@@ -592,8 +592,8 @@ __global__ void __launch_bounds__(kTableWarps * 32, kTableCtasPerSm) table_grid_
       // the next row's counter updates wait for every lane's reads of this row
       __syncwarp();
       // every fourth row: could a task's buffer overflow within the next four
-      // rows (hcap leaves room for four full rows)?  Or, at level 0, has a
-      // task gathered kEarlyHits hits while a tighter table is left?  Then
+      // rows (hcap leaves room for four full rows)?  Or has a task gathered
+      // kEarlyHits hits while a tighter table is left?  Then
       // resolve what it holds; the bound B it sets lets the remaining rows be
       // compared with the tightest table whose bound is still >= B: every
       // cell with ln p <= B (the final B is lower still) stays a hit.
