@@ -68,9 +68,12 @@ constexpr bool kSidePriority = DTO_SIDE_PRIORITY != 0;
 #define DTO_LAST_LEVELS 3
 #endif
 constexpr int kLastLevels = DTO_LAST_LEVELS;
-// How far (in nats of ln p) a run's ladder bounds may lie from the pair's
-// stored ladder before they replace it.
-constexpr double kLadderSlack = 0.1;
+// How far (in nats of ln p) a run's ladder bound may lie from the pair's
+// stored one before it replaces it.
+constexpr double kLadderSlack = 0.25;
+// Runs shorter than this build the tighter tables of level 0 only: the
+// later levels of a short run see too few tasks to repay six more builds.
+constexpr long long kTightAllMin = 32768;
 
 int set_err(dto_ctx* ctx, int code, const std::string& msg) {
   if (ctx) ctx->err = msg;
@@ -305,9 +308,10 @@ int ensure_table(Lane* L, dto_pair* P, int level, int tau) {
 // could not settle (their minimum lies above its bound); table_exhaustive
 // takes what the last level leaves.  The lists and their counts stay on the
 // device: `fall` holds one list of ntask entries per level, `cnts` 8 task
-// counters then 4 list counts (zeroed by the launch of level 0).
+// counters then 4 list counts (zeroed by the launch of level 0).  Levels
+// below `tight_levels` switch to their tighter tables.
 int table_levels(Lane* L, dto_pair* P, const int16_t* X, long long xstride, int ntask, TaskResult* dOut,
-                 int lev_begin, int lev_end, int* fall, int* cnts, cudaStream_t stream, int hb) {
+                 int lev_begin, int lev_end, int* fall, int* cnts, cudaStream_t stream, int hb, int tight_levels) {
   const int cap = std::max(ntask, 1);
   const int hitcap = kTableHitCap * kTableTasks;
   int rc = lane_grow(L, &L->dHits[hb], &L->hitBytes[hb], (size_t)kTableCtasPerSm * L->ctx->nsm * kTableWarps * hitcap * 8);
@@ -322,7 +326,7 @@ int table_levels(Lane* L, dto_pair* P, const int16_t* X, long long xstride, int 
     a.ntask = ntask;
     a.tau = L->kthr_tau[level];
     a.kthr = L->dKthr[level];
-    a.ntight = level < kTightLevels ? kTightTables : 0;
+    a.ntight = level < tight_levels ? kTightTables : 0;
     for (int q = 0; q < a.ntight; ++q) {
       a.tight[q] = L->dKthr[tight_slot(level, q)];
       a.tight_tau[q] = L->kthr_tau[tight_slot(level, q)];
@@ -461,6 +465,21 @@ int make_labels_launch(Lane* L, dto_pair* P, uint64_t seed, uint32_t first, int 
 // 90th percentile (level 0), the 99th (level 1), one nat above the maximum
 // (level 2), as fixed-point ln p, each above the one before; then each
 // level's three tighter tables (kLadderTaus entries in all).
+// The ladder's order: each level's bound above the one before, each level's
+// tighter tables below its bound and below one another.
+void ladder_order(int tau[kLadderTaus]) {
+  tau[1] = std::max(tau[1], tau[0] + 1);
+  tau[2] = std::max(tau[2], tau[1] + 1);
+  if (kLadderLevels == 2) tau[1] = tau[2];
+  for (int l = 0; l < 3; ++l) {
+    int prev = tau[l];
+    for (int t = 0; t < 3; ++t) {
+      tau[tight_slot(l, t)] = std::min(tau[tight_slot(l, t)], prev - 1);
+      prev = tau[tight_slot(l, t)];
+    }
+  }
+}
+
 void ladder_of(const std::vector<double>& all, int fshift, int tau[kLadderTaus]) {
   // the quantiles from an evenly strided sample of at most 16,384 minima
   // (the permutations are in random order), the maximum from all of them
@@ -477,21 +496,16 @@ void ladder_of(const std::vector<double>& all, int fshift, int tau[kLadderTaus])
   const double p99 = q(0.99);
   const double pmax = std::max(*std::max_element(all.begin(), all.end()), 1e-300);
   tau[0] = fixed_log(p90, fshift);
-  tau[1] = std::max(fixed_log(p99, fshift), tau[0] + 1);
-  tau[2] = std::max((int)std::min(0.0, std::floor((std::log(pmax) + 1.0) * std::ldexp(1.0, fshift))), tau[1] + 1);
-  if (kLadderLevels == 2) tau[1] = tau[2];
+  tau[1] = fixed_log(p99, fshift);
+  tau[2] = (int)std::min(0.0, std::floor((std::log(pmax) + 1.0) * std::ldexp(1.0, fshift)));
   // the tighter tables a sweep switches to once a task's bound is known,
   // each below the one before: for level 0 the 50th, 10th and 1st
   // percentiles, for level 1 the 98th, 96th and 93rd, for level 2 the
   // maximum, the 99.9th and the 99.5th
   const double ptight[3][3] = {{q(0.5), q(0.1), q(0.01)}, {q(0.98), q(0.96), q(0.93)}, {pmax, q(0.999), q(0.995)}};
-  for (int l = 0; l < 3; ++l) {
-    int prev = tau[l];
-    for (int t = 0; t < 3; ++t) {
-      tau[tight_slot(l, t)] = std::min(fixed_log(ptight[l][t], fshift), prev - 1);
-      prev = tau[tight_slot(l, t)];
-    }
-  }
+  for (int l = 0; l < 3; ++l)
+    for (int t = 0; t < 3; ++t) tau[tight_slot(l, t)] = fixed_log(ptight[l][t], fshift);
+  ladder_order(tau);
 }
 
 int lane_run_range(Lane* L, dto_pair* P, uint32_t perm_first, int64_t n_perm, uint64_t seed,
@@ -688,7 +702,8 @@ int lane_run_range(Lane* L, dto_pair* P, uint32_t perm_first, int64_t n_perm, ui
       rc = ensure_table(L, P, l, tau[l]);
       if (rc) return rc;
     }
-    for (int l = 0; l < std::min(kTightLevels, kLadderLevels); ++l)
+    const int tight_levels = std::min(n_perm >= kTightAllMin ? kTightLevels : 1, kLadderLevels);
+    for (int l = 0; l < tight_levels; ++l)
       for (int q = 0; q < kTightTables; ++q) {
         rc = ensure_table(L, P, tight_slot(l, q), tau[tight_slot(l, q)]);
         if (rc) return rc;
@@ -728,14 +743,14 @@ int lane_run_range(Lane* L, dto_pair* P, uint32_t perm_first, int64_t n_perm, ui
       int16_t* X = (int16_t*)sl.dX;
       TaskResult* dR = (TaskResult*)sl.dRes;
       LCK(cudaEventRecord(sl.ev[2], L->stream));
-      rc = table_levels(L, P, X, xs, cnt, dR, 0, 1, (int*)sl.dFall, sl.dCnt, L->stream, 0);
+      rc = table_levels(L, P, X, xs, cnt, dR, 0, 1, (int*)sl.dFall, sl.dCnt, L->stream, 0, tight_levels);
       if (rc) return rc;
       LCK(cudaEventRecord(sl.ev[6], L->stream));
       const int si = (int)(it % Lane::kSlots);
       LCK(cudaStreamWaitEvent(sl.side, sl.ev[6], 0));
       LCK(cudaEventRecord(sl.ev[4], sl.side));
       const int nl = it + 1 == npipe ? std::min(nlev, kLastLevels) : nlev;
-      rc = table_levels(L, P, X, xs, cnt, dR, 1, nl, (int*)sl.dFall, sl.dCnt, sl.side, 1 + si);
+      rc = table_levels(L, P, X, xs, cnt, dR, 1, nl, (int*)sl.dFall, sl.dCnt, sl.side, 1 + si, tight_levels);
       if (rc) return rc;
       rc = table_exhaustive(L, P, X, xs, cnt, dR, nl, (const int*)sl.dFall, sl.dCnt, sl.side);
       if (rc) return rc;
@@ -763,19 +778,18 @@ int lane_run_range(Lane* L, dto_pair* P, uint32_t perm_first, int64_t n_perm, ui
     }
     // this run's minimum p-values set the ladder of the pair's next run.
     // The bounds are quantiles of the pair's null distribution, so another
-    // seed moves them a little; the ladder is replaced only when a bound has
-    // moved by more than kLadderSlack nats, which spares the next run the
-    // rebuild of the table screens (they are screens: any bounds give the
-    // same results).
+    // seed moves them a little; a bound is replaced only when it has moved
+    // by more than kLadderSlack nats, which spares the next run the rebuild
+    // of that table screen (they are screens: any bounds give the same
+    // results).
     {
       int t[kLadderTaus];
       ladder_of(minp, P->fshift, t);
       const long long slack = (long long)std::ldexp(kLadderSlack, P->fshift);
       std::lock_guard<std::mutex> g(P->ladder_mu);
-      bool keep = P->ladder_ok;
-      for (int l = 0; l < kLadderTaus && keep; ++l) keep = std::llabs((long long)t[l] - P->ladder_tau[l]) <= slack;
-      if (!keep)
-        for (int l = 0; l < kLadderTaus; ++l) P->ladder_tau[l] = t[l];
+      for (int l = 0; l < kLadderTaus; ++l)
+        if (!P->ladder_ok || std::llabs((long long)t[l] - P->ladder_tau[l]) > slack) P->ladder_tau[l] = t[l];
+      ladder_order(P->ladder_tau);
       P->ladder_ok = true;
     }
     // the main stream's timing event follows the side streams' last work
