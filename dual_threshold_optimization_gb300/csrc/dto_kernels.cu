@@ -97,23 +97,32 @@ __device__ __forceinline__ void perm_body(const PermArgs& A, int* cnt, uint16_t*
   };
 
   for (int b = tid; b < kBuckets; b += kPermThreads) cnt[b] = 0;
-  // the label table goes to shared memory by asynchronous 16-byte copies
-  // that land while the words are drawn (waited for before the gather)
-  const bool asyncY = sY && (reinterpret_cast<uintptr_t>(A.Ylab) & 15) == 0;
-  if (asyncY) {
-    const char* src = reinterpret_cast<const char*>(A.Ylab);
-    const uint32_t dst = (uint32_t)__cvta_generic_to_shared(sY);
-    const int bytes = 2 * L;
-    for (int o = 16 * tid; o < bytes; o += 16 * kPermThreads) {
-      const int n = min(16, bytes - o);
-      asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(dst + o), "l"(src + o), "r"(n)
-                   : "memory");
-    }
-    asm volatile("cp.async.commit_group;\n" ::: "memory");
-  } else if (sY) {
-    for (int q = tid; q < L; q += kPermThreads) sY[q] = __ldg(A.Ylab + q);
-  }
   const bool rows = A.X && A.rowstart;
+  // The label table goes to shared memory by asynchronous 16-byte copies
+  // (waited for before the gather).  Without kept words, the label area
+  // first holds each element's bucket (uint16), so that the scatter need not
+  // redraw the words; the copies then start once the row starts have found
+  // their buckets, and land during the shuffles.  (Up to two row starts a
+  // thread: longer grids redraw.)
+  const bool asyncY = sY && (reinterpret_cast<uintptr_t>(A.Ylab) & 15) == 0;
+  const bool ids = !kWords && sY && (!rows || A.n1 + 1 <= 2 * kPermThreads);
+  uint16_t* sId = reinterpret_cast<uint16_t*>(sY);
+  auto stage_labels = [&]() {
+    if (asyncY) {
+      const char* src = reinterpret_cast<const char*>(A.Ylab);
+      const uint32_t dst = (uint32_t)__cvta_generic_to_shared(sY);
+      const int bytes = 2 * L;
+      for (int o = 16 * tid; o < bytes; o += 16 * kPermThreads) {
+        const int n = min(16, bytes - o);
+        asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(dst + o), "l"(src + o), "r"(n)
+                     : "memory");
+      }
+      asm volatile("cp.async.commit_group;\n" ::: "memory");
+    } else if (sY) {
+      for (int q = tid; q < L; q += kPermThreads) sY[q] = __ldg(A.Ylab + q);
+    }
+  };
+  if (!ids) stage_labels();
   // this thread's first two row starts (and the ones before them), loaded
   // now so that the loads are done by the time the shuffles need them
   const int r1 = tid + kPermThreads;
@@ -130,6 +139,7 @@ __device__ __forceinline__ void perm_body(const PermArgs& A, int* cnt, uint16_t*
     for (int q = 0; q < 4; ++q) {
       if (4 * g + q < L) {
         if (kWords) sW[4 * g + q] = wv[q];
+        if (ids) sId[4 * g + q] = (uint16_t)(wv[q] >> kLowBits);
         atomicAdd(&cnt[wv[q] >> kLowBits], 1);
       }
     }
@@ -173,6 +183,11 @@ __device__ __forceinline__ void perm_body(const PermArgs& A, int* cnt, uint16_t*
   if (kWords) {
     for (int e = tid; e < L; e += kPermThreads) {
       const int pos = atomicAdd(&cnt[sW[e] >> kLowBits], 1);
+      sA[pos] = (uint16_t)e;
+    }
+  } else if (ids) {
+    for (int e = tid; e < L; e += kPermThreads) {
+      const int pos = atomicAdd(&cnt[sId[e]], 1);
       sA[pos] = (uint16_t)e;
     }
   } else {
@@ -224,21 +239,34 @@ __device__ __forceinline__ void perm_body(const PermArgs& A, int* cnt, uint16_t*
     // bucket inside one row gives the same multisets in any order (the sort
     // and the Fisher-Yates pass only decide which of its elements fall on
     // which side of a row start).  So only the buckets with a row start
-    // strictly inside are shuffled: each row start finds its bucket from the
-    // word of the element the scatter put there, and the lowest row start
-    // inside a bucket takes it.  (Positions past the last row form one more
-    // range.)
-    for (int r = tid, u = 0; r <= A.n1; r += kPermThreads, ++u) {
+    // strictly inside are shuffled: each row start finds the bucket of the
+    // element the scatter put there, and the lowest row start inside a
+    // bucket takes it.  (Positions past the last row form one more range.)
+    // Returns (bucket, start), or bucket -1.
+    auto claim = [&](int r, int u) -> int2 {
       const int p = u == 0 ? rs0 : u == 1 ? rs1 : __ldg(A.rowstart + r);
-      if (p <= 0 || p >= L) continue;
-      const int lo = (int)(word_of(sA[p]) >> kLowBits);  // the bucket holding position p
+      if (p <= 0 || p >= L) return make_int2(-1, 0);
+      const int lo = ids ? (int)sId[sA[p]] : (int)(word_of(sA[p]) >> kLowBits);
       const int s0 = lo == 0 ? 0 : cnt[lo - 1];
-      if (s0 >= p) continue;                                // p starts the bucket
+      if (s0 >= p) return make_int2(-1, 0);  // p starts the bucket
       const int prev = u == 0 ? rsPrev0 : u == 1 ? rsPrev1 : __ldg(A.rowstart + r - 1);
-      if (r > 0 && prev > s0) continue;  // a lower row start takes it
-      shuffle_bucket(lo, s0, cnt[lo] - s0);
+      if (r > 0 && prev > s0) return make_int2(-1, 0);  // a lower row start takes it
+      return make_int2(lo, s0);
+    };
+    const int2 cl0 = tid <= A.n1 ? claim(tid, 0) : make_int2(-1, 0);
+    const int2 cl1 = r1 <= A.n1 ? claim(r1, 1) : make_int2(-1, 0);
+    if (ids) {
+      __syncthreads();  // every claim has read the buckets: the labels may come
+      stage_labels();
+    }
+    if (cl0.x >= 0) shuffle_bucket(cl0.x, cl0.y, cnt[cl0.x] - cl0.y);
+    if (cl1.x >= 0) shuffle_bucket(cl1.x, cl1.y, cnt[cl1.x] - cl1.y);
+    for (int r = tid + 2 * kPermThreads, u = 2; r <= A.n1; r += kPermThreads, ++u) {
+      const int2 c = claim(r, u);
+      if (c.x >= 0) shuffle_bucket(c.x, c.y, cnt[c.x] - c.y);
     }
   } else {
+    if (ids) stage_labels();
     for (int b = tid; b < kBuckets; b += kPermThreads) {
       const int s0 = b == 0 ? 0 : cnt[b - 1];
       const int sz = cnt[b] - s0;
