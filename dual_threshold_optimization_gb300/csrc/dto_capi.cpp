@@ -225,11 +225,33 @@ int dto_pair_create(dto_ctx* ctx, const uint32_t* ranks1, const int32_t* feat1, 
   P->N2 = n2;
   P->npop = population;
   P->nfeat = n_features;
-  // stable sort by rank (src/collections/ranked.rs:527-542)
+  // stable sort by rank (src/collections/ranked.rs:527-542): a counting
+  // sort when the ranks are dense, else a byte-wise LSD radix sort; both keep
+  // equal ranks in input order, as the stable comparison sort does
   auto sort_list = [](const uint32_t* r, int64_t n, std::vector<int32_t>& order) {
     order.resize((size_t)n);
+    if (n == 0) return;
+    uint32_t mx = 0;
+    for (int64_t q = 0; q < n; ++q) mx = std::max(mx, r[q]);
+    if ((uint64_t)mx <= 4 * (uint64_t)n + 1024) {
+      std::vector<int64_t> at((size_t)mx + 2, 0);  // at[v]: first slot of rank v
+      for (int64_t q = 0; q < n; ++q) ++at[(size_t)r[q] + 1];
+      for (size_t v = 1; v < at.size(); ++v) at[v] += at[v - 1];
+      for (int64_t q = 0; q < n; ++q) order[(size_t)at[r[q]]++] = (int32_t)q;
+      return;
+    }
+    std::vector<int32_t> tmp((size_t)n);
     for (int64_t q = 0; q < n; ++q) order[(size_t)q] = (int32_t)q;
-    std::stable_sort(order.begin(), order.end(), [&](int32_t a, int32_t b) { return r[a] < r[b]; });
+    for (int shift = 0; shift < 32 && (mx >> shift) != 0; shift += 8) {
+      int64_t at[257] = {0};
+      for (int64_t q = 0; q < n; ++q) ++at[((r[order[(size_t)q]] >> shift) & 255u) + 1];
+      for (int d = 1; d <= 256; ++d) at[d] += at[d - 1];
+      for (int64_t q = 0; q < n; ++q) {
+        const int32_t e = order[(size_t)q];
+        tmp[(size_t)at[(r[e] >> shift) & 255u]++] = e;
+      }
+      order.swap(tmp);
+    }
   };
   sort_list(ranks1, n1, P->order1);
   sort_list(ranks2, n2, P->order2);
@@ -306,19 +328,33 @@ int dto_pair_create(dto_ctx* ctx, const uint32_t* ranks1, const int32_t* feat1, 
   std::vector<int> row((size_t)nt1 + 1);
   row[0] = 0;
   for (int i = 0; i < nt1; ++i) row[(size_t)i + 1] = P->c1[(size_t)i];
-  auto up = [&](void** d, const void* h, size_t bytes) -> cudaError_t {
-    cudaError_t e = cudaMalloc(d, std::max(bytes, (size_t)16));
-    if (e != cudaSuccess) return e;
-    P->upload_bytes += (long long)bytes;
-    return cudaMemcpyAsync(*d, h, bytes, cudaMemcpyHostToDevice, ctx->lane0->stream);
+  // the pair's device arrays: one allocation and one copy, each array on a
+  // 256-byte boundary
+  struct Part {
+    const void* h;
+    size_t bytes;
+    void** d;
   };
-  cudaError_t e = cudaSuccess;
-  if (e == cudaSuccess) e = up((void**)&P->dRow, row.data(), row.size() * 4);
-  if (e == cudaSuccess) e = up((void**)&P->dNcnt, P->c2.data(), P->c2.size() * 4);
-  if (e == cudaSuccess) e = up((void**)&P->dF, F.data(), F.size() * 4);
-  if (e == cudaSuccess) e = up((void**)&P->dYlab, P->ylab.data(), P->ylab.size() * 2);
-  if (e == cudaSuccess) e = up((void**)&P->dLab2, P->lab2.data(), P->lab2.size() * 2);
-  if (e == cudaSuccess) e = up((void**)&P->dMap12, P->map12.data(), P->map12.size() * 4);
+  const Part parts[6] = {{row.data(), row.size() * 4, (void**)&P->dRow},
+                         {P->c2.data(), P->c2.size() * 4, (void**)&P->dNcnt},
+                         {F.data(), F.size() * 4, (void**)&P->dF},
+                         {P->ylab.data(), P->ylab.size() * 2, (void**)&P->dYlab},
+                         {P->lab2.data(), P->lab2.size() * 2, (void**)&P->dLab2},
+                         {P->map12.data(), P->map12.size() * 4, (void**)&P->dMap12}};
+  size_t off[6], total = 0;
+  for (int k = 0; k < 6; ++k) {
+    off[k] = total;
+    total += (parts[k].bytes + 255) & ~(size_t)255;
+    P->upload_bytes += (long long)parts[k].bytes;
+  }
+  std::vector<unsigned char> host(total, 0);
+  for (int k = 0; k < 6; ++k)
+    if (parts[k].bytes) std::memcpy(host.data() + off[k], parts[k].h, parts[k].bytes);
+  cudaError_t e = cudaMalloc(&P->dBase, std::max(total, (size_t)256));
+  if (e == cudaSuccess) {
+    for (int k = 0; k < 6; ++k) *parts[k].d = static_cast<unsigned char*>(P->dBase) + off[k];
+    e = cudaMemcpyAsync(P->dBase, host.data(), total, cudaMemcpyHostToDevice, ctx->lane0->stream);
+  }
   if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->lane0->stream);
   if (e != cudaSuccess) {
     dto_pair_destroy(P);
@@ -345,12 +381,7 @@ int dto_pair_create(dto_ctx* ctx, const uint32_t* ranks1, const int32_t* feat1, 
 
 int dto_pair_destroy(dto_pair* P) {
   if (!P) return DTO_ERR_INVALID;
-  cudaFree(P->dRow);
-  cudaFree(P->dNcnt);
-  cudaFree(P->dF);
-  cudaFree(P->dYlab);
-  cudaFree(P->dLab2);
-  cudaFree(P->dMap12);
+  cudaFree(P->dBase);
   delete P;
   return DTO_OK;
 }

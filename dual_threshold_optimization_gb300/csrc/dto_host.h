@@ -136,7 +136,8 @@ struct dto_pair {
   std::vector<int16_t> lab2, ylab;
   int C = 0, fshift = 0;
   long long upload_bytes = 0;  // host-to-device bytes of dto_pair_create
-  // device
+  // device: views into one allocation (dBase)
+  void* dBase = nullptr;
   int* dRow = nullptr;
   int* dNcnt = nullptr;
   uint32_t* dF = nullptr;
