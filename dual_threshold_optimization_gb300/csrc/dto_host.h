@@ -62,6 +62,7 @@ struct Lane {
   cudaStream_t stream = nullptr;
   cudaStream_t side = nullptr;  // first batch, later table levels and fallbacks
   cudaEvent_t evSide = nullptr;
+  cudaEvent_t evTables = nullptr;  // the later levels' tables, built on the side stream
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   cudaEvent_t evk[4] = {nullptr, nullptr, nullptr, nullptr};  // perm start/end, grid start/end
   // per-run accounting

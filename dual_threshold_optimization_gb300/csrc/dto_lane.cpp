@@ -141,6 +141,7 @@ int lane_create(dto_ctx* ctx, Lane** out, std::string* err_sink) {
       cudaSuccess)
     return fail(e, "stream");
   if ((e = cudaEventCreateWithFlags(&L->evSide, cudaEventDisableTiming)) != cudaSuccess) return fail(e, "event");
+  if ((e = cudaEventCreateWithFlags(&L->evTables, cudaEventDisableTiming)) != cudaSuccess) return fail(e, "event");
   if ((e = cudaEventCreate(&L->ev0)) != cudaSuccess) return fail(e, "event");
   if ((e = cudaEventCreate(&L->ev1)) != cudaSuccess) return fail(e, "event");
   for (int q = 0; q < 4; ++q)
@@ -184,6 +185,7 @@ void lane_destroy(Lane* L) {
   for (int q = 0; q < 4; ++q)
     if (L->evk[q]) cudaEventDestroy(L->evk[q]);
   if (L->evSide) cudaEventDestroy(L->evSide);
+  if (L->evTables) cudaEventDestroy(L->evTables);
   if (L->side) cudaStreamDestroy(L->side);
   if (L->stream) cudaStreamDestroy(L->stream);
   delete L;
@@ -280,8 +282,9 @@ int lane_grid_tasks(Lane* L, dto_pair* P, const int16_t* dX, long long xstride, 
 
 // Table screen `level` for bound tau (fixed-point ln p), built on the device
 // into the lane's buffer (kept while the lane runs the same pair and bound).
-int ensure_table(Lane* L, dto_pair* P, int level, int tau) {
+int ensure_table(Lane* L, dto_pair* P, int level, int tau, cudaStream_t stream, bool* built) {
   if (L->kthr_pair[level] == P->serial && L->kthr_tau[level] == tau) return DTO_OK;
+  *built = true;
   int rc = lane_grow(L, (void**)&L->dKthr[level], &L->kthrBytes[level], table_entries(P->C, P->dev.n1) * 2);
   if (rc) return rc;
   TableArgs t{};
@@ -296,7 +299,7 @@ int ensure_table(Lane* L, dto_pair* P, int level, int tau) {
   t.tau = tau;
   t.packed = P->ncommon <= kPackedMaxCommon ? 1 : 0;
   t.kthr = L->dKthr[level];
-  LCK(launch_table_build(t, L->ctx->nsm, L->stream));
+  LCK(launch_table_build(t, L->ctx->nsm, stream));
   L->acc_launches += 1;
   L->kthr_pair[level] = P->serial;
   L->kthr_tau[level] = tau;
@@ -698,16 +701,23 @@ int lane_run_range(Lane* L, dto_pair* P, uint32_t perm_first, int64_t n_perm, ui
       if (rc) return rc;
       ladder_of(std::vector<double>(minp.begin(), minp.begin() + cnt0), P->fshift, tau);
     }
+    // The table screens: level 0's on the main stream (the first level-0
+    // sweep needs them), the later levels' on the side stream behind the
+    // first batch (their first sweeps come a level-0 sweep later; each
+    // slot's side stream waits for them).
+    const int tight_levels = std::min(n_perm >= kTightAllMin ? kTightLevels : 1, kLadderLevels);
+    bool built0 = false, built_late = false;
     for (int l = 0; l < kLadderLevels; ++l) {
-      rc = ensure_table(L, P, l, tau[l]);
+      rc = ensure_table(L, P, l, tau[l], l == 0 ? L->stream : L->side, l == 0 ? &built0 : &built_late);
       if (rc) return rc;
     }
-    const int tight_levels = std::min(n_perm >= kTightAllMin ? kTightLevels : 1, kLadderLevels);
     for (int l = 0; l < tight_levels; ++l)
       for (int q = 0; q < kTightTables; ++q) {
-        rc = ensure_table(L, P, tight_slot(l, q), tau[tight_slot(l, q)]);
+        rc = ensure_table(L, P, tight_slot(l, q), tau[tight_slot(l, q)], l == 0 ? L->stream : L->side,
+                          l == 0 ? &built0 : &built_late);
         if (rc) return rc;
       }
+    if (built_late) LCK(cudaEventRecord(L->evTables, L->side));
     const int nlev = kLadderLevels;
     // Batches in flight: while batch b's later table levels, exhaustive
     // fallback and result copy run on the side stream, the next batches'
@@ -748,6 +758,7 @@ int lane_run_range(Lane* L, dto_pair* P, uint32_t perm_first, int64_t n_perm, ui
       LCK(cudaEventRecord(sl.ev[6], L->stream));
       const int si = (int)(it % Lane::kSlots);
       LCK(cudaStreamWaitEvent(sl.side, sl.ev[6], 0));
+      if (built_late) LCK(cudaStreamWaitEvent(sl.side, L->evTables, 0));
       LCK(cudaEventRecord(sl.ev[4], sl.side));
       const int nl = it + 1 == npipe ? std::min(nlev, kLastLevels) : nlev;
       rc = table_levels(L, P, X, xs, cnt, dR, 1, nl, (int*)sl.dFall, sl.dCnt, sl.side, 1 + si, tight_levels);
