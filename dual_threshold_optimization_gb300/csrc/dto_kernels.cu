@@ -63,20 +63,14 @@ struct PhiloxStream {
   }
 };
 
-__device__ __forceinline__ uint32_t bucket_of(uint4 w, int q) {
-  uint32_t v = (q == 0) ? w.x : (q == 1) ? w.y : (q == 2) ? w.z : w.w;
-  return v >> (32 - kBucketBits);
-}
-
 // One CTA per permutation.  Shared memory: the bucket counters (int32,
 // kBuckets; after the scatter they hold each bucket's end), the shuffled
-// element indices
-// (uint16, L), where the launch keeps them every element's Philox word
-// (uint32, L), so that the scatter and the shuffle draws reuse the words of
-// the counting pass (otherwise a word is recomputed where it is needed),
-// and where it fits the label table.  kBuckets = 4096 keeps buckets at a few elements for the list
-// lengths of interest, so the per-bucket canonical sort and Fisher-Yates are
-// a few operations per element.
+// element indices (uint16, L), where the launch keeps them every element's
+// Philox word (uint32, L: the scatter and the shuffle draws reuse the words
+// of the counting pass; otherwise a shuffle draw recomputes its word), and
+// where it fits the label table (int16, L).  kBuckets = 4096 keeps buckets
+// at a few elements for the list lengths of interest, so the per-bucket
+// canonical sort and Fisher-Yates are a few operations per element.
 template <bool kWords, int kPermThreads>
 __device__ __forceinline__ void perm_body(const PermArgs& A, int* cnt, uint16_t* sA, uint32_t* sW,
                                           int16_t* sY) {
