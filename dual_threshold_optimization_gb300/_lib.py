@@ -25,7 +25,7 @@ PRECISION_SCREEN = 1
 # Every symbol include/dto.h declares.
 EXPORTS = (
     "dto_version", "dto_status_string", "dto_ctx_create", "dto_ctx_destroy", "dto_last_error",
-    "dto_ctx_stream", "dto_generate_thresholds", "dto_pair_create", "dto_pair_destroy",
+    "dto_ctx_stream", "dto_generate_thresholds", "dto_rank_order", "dto_pair_create", "dto_pair_destroy",
     "dto_pair_info", "dto_pair_thresholds", "dto_pair_order", "dto_pair_upload_bytes", "dto_pair_set_stream", "dto_run", "dto_run_range", "dto_run_range_noalloc",
     "dto_optimize",
     "dto_grid_dump", "dto_hypergeom_sf", "dto_export_permutations", "dto_fdr",
@@ -92,6 +92,8 @@ def lib():
     L.dto_ctx_stream.restype = _P
     L.dto_generate_thresholds.argtypes = [C.c_uint32, _P, C.c_int64]
     L.dto_generate_thresholds.restype = C.c_int64
+    L.dto_rank_order.argtypes = [_P, C.c_int64, _P]
+    L.dto_rank_order.restype = C.c_int
     L.dto_pair_create.argtypes = [_P, _P, _P, C.c_int64, _P, _P, C.c_int64, C.c_int64, C.c_int64,
                                   C.POINTER(_P)]
     L.dto_pair_destroy.argtypes = [_P]

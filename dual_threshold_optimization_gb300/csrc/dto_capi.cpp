@@ -135,6 +135,39 @@ int pick_C(int n2) {
 
 }  // namespace
 
+namespace {
+
+// Stable sort by rank (src/collections/ranked.rs:527-542): a counting sort
+// when the ranks are dense, else a byte-wise LSD radix sort; both keep equal
+// ranks in input order, as the reference's stable comparison sort does.
+void rank_order(const uint32_t* r, int64_t n, std::vector<int32_t>& order) {
+  order.resize((size_t)n);
+  if (n == 0) return;
+  uint32_t mx = 0;
+  for (int64_t q = 0; q < n; ++q) mx = std::max(mx, r[q]);
+  if ((uint64_t)mx <= 4 * (uint64_t)n + 1024) {
+    std::vector<int64_t> at((size_t)mx + 2, 0);  // at[v]: first slot of rank v
+    for (int64_t q = 0; q < n; ++q) ++at[(size_t)r[q] + 1];
+    for (size_t v = 1; v < at.size(); ++v) at[v] += at[v - 1];
+    for (int64_t q = 0; q < n; ++q) order[(size_t)at[r[q]]++] = (int32_t)q;
+    return;
+  }
+  std::vector<int32_t> tmp((size_t)n);
+  for (int64_t q = 0; q < n; ++q) order[(size_t)q] = (int32_t)q;
+  for (int shift = 0; shift < 32 && (mx >> shift) != 0; shift += 8) {
+    int64_t at[257] = {0};
+    for (int64_t q = 0; q < n; ++q) ++at[((r[order[(size_t)q]] >> shift) & 255u) + 1];
+    for (int d = 1; d <= 256; ++d) at[d] += at[d - 1];
+    for (int64_t q = 0; q < n; ++q) {
+      const int32_t e = order[(size_t)q];
+      tmp[(size_t)at[(r[e] >> shift) & 255u]++] = e;
+    }
+    order.swap(tmp);
+  }
+}
+
+}  // namespace
+
 extern "C" {
 
 int dto_version(void) { return 10000; }
@@ -190,6 +223,14 @@ const char* dto_last_error(const dto_ctx* ctx) { return ctx ? ctx->err.c_str() :
 
 void* dto_ctx_stream(dto_ctx* ctx) { return ctx ? (void*)ctx->lane0->stream : nullptr; }
 
+int dto_rank_order(const uint32_t* ranks, int64_t n, int32_t* order) {
+  if (n < 0 || n > 0x7fffffffLL || (n > 0 && (!ranks || !order))) return DTO_ERR_INVALID;
+  std::vector<int32_t> o;
+  rank_order(ranks, n, o);
+  std::copy(o.begin(), o.end(), order);
+  return DTO_OK;
+}
+
 int64_t dto_generate_thresholds(uint32_t max_rank, uint32_t* out, int64_t cap) {
   std::vector<uint32_t> t = thresholds_of(max_rank);
   for (size_t q = 0; q < t.size() && (int64_t)q < cap; ++q) out[q] = t[q];
@@ -225,36 +266,8 @@ int dto_pair_create(dto_ctx* ctx, const uint32_t* ranks1, const int32_t* feat1, 
   P->N2 = n2;
   P->npop = population;
   P->nfeat = n_features;
-  // stable sort by rank (src/collections/ranked.rs:527-542): a counting
-  // sort when the ranks are dense, else a byte-wise LSD radix sort; both keep
-  // equal ranks in input order, as the stable comparison sort does
-  auto sort_list = [](const uint32_t* r, int64_t n, std::vector<int32_t>& order) {
-    order.resize((size_t)n);
-    if (n == 0) return;
-    uint32_t mx = 0;
-    for (int64_t q = 0; q < n; ++q) mx = std::max(mx, r[q]);
-    if ((uint64_t)mx <= 4 * (uint64_t)n + 1024) {
-      std::vector<int64_t> at((size_t)mx + 2, 0);  // at[v]: first slot of rank v
-      for (int64_t q = 0; q < n; ++q) ++at[(size_t)r[q] + 1];
-      for (size_t v = 1; v < at.size(); ++v) at[v] += at[v - 1];
-      for (int64_t q = 0; q < n; ++q) order[(size_t)at[r[q]]++] = (int32_t)q;
-      return;
-    }
-    std::vector<int32_t> tmp((size_t)n);
-    for (int64_t q = 0; q < n; ++q) order[(size_t)q] = (int32_t)q;
-    for (int shift = 0; shift < 32 && (mx >> shift) != 0; shift += 8) {
-      int64_t at[257] = {0};
-      for (int64_t q = 0; q < n; ++q) ++at[((r[order[(size_t)q]] >> shift) & 255u) + 1];
-      for (int d = 1; d <= 256; ++d) at[d] += at[d - 1];
-      for (int64_t q = 0; q < n; ++q) {
-        const int32_t e = order[(size_t)q];
-        tmp[(size_t)at[(r[e] >> shift) & 255u]++] = e;
-      }
-      order.swap(tmp);
-    }
-  };
-  sort_list(ranks1, n1, P->order1);
-  sort_list(ranks2, n2, P->order2);
+  rank_order(ranks1, n1, P->order1);
+  rank_order(ranks2, n2, P->order2);
   P->r1.resize((size_t)n1);
   P->f1.resize((size_t)n1);
   P->r2.resize((size_t)n2);

@@ -103,6 +103,11 @@ DTO_API void* dto_ctx_stream(dto_ctx* ctx);
  * Writes min(count, cap) thresholds; returns count. */
 DTO_API int64_t dto_generate_thresholds(uint32_t max_rank, uint32_t* out, int64_t cap);
 
+/* The stable order by rank that dto_pair_create uses for each list
+ * (src/collections/ranked.rs:527-542, a stable sort by rank): order[k] is the
+ * input index of the k-th feature, equal ranks in input order.  Host only. */
+DTO_API int dto_rank_order(const uint32_t* ranks, int64_t n, int32_t* order);
+
 /* A list pair, resident on the device.  Replaces RankedFeatureList::from for
  * both lists (src/collections/ranked.rs:176-191: stable sort by rank, then the
  * thresholds) and the per-task set extraction (ranked.rs:561-568).

@@ -45,6 +45,25 @@ def test_host_utilities(L):
     assert L.dto_version() >= 10000
 
 
+def test_rank_order_is_the_stable_sort(L):
+    # dto_pair_create's order by rank (counting sort for dense ranks, radix
+    # sort for sparse ones) equals a stable comparison sort, ties in input order
+    import numpy as np
+    from dual_threshold_optimization_gb300._lib import ptr
+    rng = np.random.default_rng(17)
+    cases = [np.zeros(0, np.uint32), np.array([7], np.uint32), np.full(1000, 3, np.uint32)]
+    for n in (2, 17, 1000, 20000):
+        cases.append(rng.permutation(n).astype(np.uint32) + 1)            # dense, no ties
+        cases.append(rng.integers(1, max(2, n // 4), n, dtype=np.uint32))  # dense, many ties
+        cases.append(rng.integers(0, 2**32, n, dtype=np.uint64).astype(np.uint32))  # sparse
+        cases.append((rng.integers(0, 300, n) * 65537 + 5).astype(np.uint32))       # sparse, ties
+    for r in cases:
+        out = np.full(max(len(r), 1), -1, np.int32)
+        assert L.dto_rank_order(ptr(r), len(r), ptr(out)) == 0
+        assert np.array_equal(out[:len(r)], np.argsort(r, kind="stable").astype(np.int32))
+    assert L.dto_rank_order(None, -1, None) != 0
+
+
 def test_no_oracle_in_product():
     # the product package never imports, includes or links the oracle
     pkg = os.path.join(ROOT, "dual_threshold_optimization_gb300")
