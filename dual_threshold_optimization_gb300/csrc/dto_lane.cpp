@@ -218,13 +218,12 @@ void fill_result(const dto_pair* P, const TaskResult& r, int permuted, dto_resul
   o->status = r.status;
 }
 
-// Batch size of a run: bounded by 1 GiB of labels (and of index scratch for
-// test mode and for pairs whose lists hold different features).
-// Label bytes of one pipelined batch (2^DTO_BATCH_SHIFT).  Every batch's
-// later levels pay a latency floor (their slowest tasks), so fewer, larger
-// batches win: per 100,000 permutations 2 GiB measured 36.2 ms at N = 20,000
-// and 39.6 ms on the 18,000-feature background pair, 1 GiB 36.2-36.8 and
-// 43.1 ms, 512 MiB 40-41 ms and 46 ms.
+// Batch size of a run: 2^DTO_BATCH_SHIFT bytes of labels (2 GiB), and at
+// most 1 GiB of index scratch for test mode and for pairs whose lists hold
+// different features.  Every batch's later levels pay a latency floor (their
+// slowest tasks), so fewer, larger batches win: per 100,000 permutations
+// 2 GiB measured 36.2 ms at N = 20,000 and 39.6 ms on the 18,000-feature
+// background pair, 1 GiB 36.2-36.8 and 43.1 ms, 512 MiB 40-41 ms and 46 ms.
 #ifndef DTO_BATCH_SHIFT
 #define DTO_BATCH_SHIFT 31
 #endif

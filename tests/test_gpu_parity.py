@@ -190,7 +190,7 @@ def test_pipelined_batches_equal_short_runs(engine, kind):
     # optimum that short runs of the same permutation ids give
     if kind == "same_set":
         p = synth.copula_pair(20000, 0.2, seed=57)
-        P = 110000  # 512 + 26,843 x 4 + 2,116 at 40,000 label bytes a permutation: slots reused
+        P = 170000  # 512 + 53,687 x 3 + 8,427 at 40,000 label bytes a permutation: a slot reused
     else:
         p = synth.small_pair(20000, 0.2, seed=58, subset1=19000, subset2=19500)
         P = 15000  # 512 + 6,972 + 6,972 + 544 at 1 GiB of two-list index scratch
