@@ -26,6 +26,7 @@ Printed JSON line (one, from rank 0):
 host threads, on the same workload and metric.
 """
 import argparse
+import datetime
 import json
 import os
 import statistics
@@ -69,29 +70,67 @@ def host_threads():
 # clocks sampled during the timed region
 # ---------------------------------------------------------------------------
 class ClockSampler:
-    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+    """nvidia-smi every 50 ms from start() to stop(); when the timed region is
+    marked (begin() / end()), only the samples whose timestamps fall inside it
+    count (all samples if none parse)."""
+    QUERY = ("timestamp,index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+    NAMES = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
 
     def __init__(self, device_index):
         self.device_index = device_index
         self.proc = None
         self.lines = []
+        self.t_begin = self.t_end = None
 
     def start(self):
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.device_index), "--query-gpu=" + self.QUERY,
-                 "--format=csv,noheader,nounits", "-lms", "200"],
+                 "--format=csv,noheader,nounits", "-lms", "50"],
                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.thread = threading.Thread(target=self._read, daemon=True)
             self.thread.start()
         except Exception:
             self.proc = None
 
+    def begin(self):
+        self.t_begin = datetime.datetime.now()
+
+    def end(self):
+        self.t_end = datetime.datetime.now()
+
     def _read(self):
         for ln in self.proc.stdout:
             self.lines.append(ln.strip())
+
+    @classmethod
+    def summarize(cls, lines, t_begin=None, t_end=None):
+        rows = []
+        for ln in lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 10:
+                continue
+            try:
+                sm, smax = float(parts[2]), float(parts[3])
+            except ValueError:
+                continue
+            try:
+                ts = datetime.datetime.strptime(parts[0], "%Y/%m/%d %H:%M:%S.%f")
+            except ValueError:
+                ts = None
+            rows.append((ts, sm, smax, parts[6:10]))
+        window = "all samples"
+        if t_begin is not None and t_end is not None:
+            slack = datetime.timedelta(milliseconds=60)
+            inside = [r for r in rows if r[0] is not None and t_begin - slack <= r[0] <= t_end + slack]
+            if inside:
+                rows, window = inside, "timed region"
+        reasons = sorted({nm for r in rows for nm, v in zip(cls.NAMES, r[3]) if v.lower() == "active"})
+        return {"sm_mhz": statistics.median([r[1] for r in rows]) if rows else None,
+                "sm_max_mhz": max(r[2] for r in rows) if rows else None,
+                "reasons": reasons, "samples": len(rows), "window": window}
 
     def stop(self):
         if self.proc is None:
@@ -101,23 +140,7 @@ class ClockSampler:
             self.proc.wait(timeout=5)
         except Exception:
             self.proc.kill()
-        sm, smax, reasons = [], [], set()
-        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for ln in self.lines:
-            parts = [p.strip() for p in ln.split(",")]
-            if len(parts) < 9:
-                continue
-            try:
-                sm.append(float(parts[1]))
-                smax.append(float(parts[2]))
-            except ValueError:
-                continue
-            for nm, v in zip(names, parts[5:9]):
-                if v.lower() == "active":
-                    reasons.add(nm)
-        return {"sm_mhz": statistics.median(sm) if sm else None,
-                "sm_max_mhz": max(smax) if smax else None,
-                "reasons": sorted(reasons), "samples": len(sm)}
+        return self.summarize(self.lines, self.t_begin, self.t_end)
 
 
 # ---------------------------------------------------------------------------
@@ -270,11 +293,12 @@ def run_gpu(args):
         torch.cuda.synchronize()
 
     # ---- device-resident throughput ----
+    sampler = ClockSampler(dev)
+    sampler.start()  # before the warm-up, so that it samples from the timed region's start
     for w in range(args.warmup):
         dp.run(P, seed=seed + 1000 + w, precision="screen")
     barrier()
-    sampler = ClockSampler(dev)
-    sampler.start()
+    sampler.begin()
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
     e0.record(stream)
@@ -288,6 +312,7 @@ def run_gpu(args):
         summaries.append(r.summary)
     e1.record(stream)
     barrier()
+    sampler.end()
     clocks = sampler.stop()
     total_ms = e0.elapsed_time(e1)
     t_max = total_ms
