@@ -223,6 +223,25 @@ def test_table_sweep_beyond_16_bit_overlaps(engine):
     dp.close()
 
 
+@pytest.mark.parametrize("N", [3, 7, 8, 9, 17, 33])
+def test_philox_permutations_tiny_lists(engine, N):
+    # lists shorter than one 16-byte label chunk and grids of one-element rows:
+    # the device permutations follow the spec, and the label path (which
+    # shuffles only the buckets a row starts inside) gives the optima of the
+    # full permutations
+    p = synth.small_pair(N=N, rho=0.2, seed=60 + N)
+    dp = engine.pair(p.ranks1, p.feat1, p.ranks2, p.feat2, p.n_features, p.population)
+    seed, P = 77, 40
+    i1, i2 = dp.export_permutations(seed, 1, P)
+    for b in range(P):
+        assert np.array_equal(O.shuffle(seed, 0, b + 1, 1, dp.N1), i1[b])
+    res_ph = dp.run(P, seed=seed, precision="screen", want_records=True)
+    res_tm = dp.run(P, perm_idx=np.concatenate([i1, i2], axis=1), precision="screen", want_records=True)
+    assert np.array_equal(res_ph.minp, res_tm.minp)
+    assert np.array_equal(res_ph.records, res_tm.records)
+    dp.close()
+
+
 @pytest.mark.parametrize("N", [30000, 40000])
 def test_philox_permutations_long_lists_match_spec(engine, N):
     # 30,000 elements: the kernel keeps every Philox word in shared memory;
