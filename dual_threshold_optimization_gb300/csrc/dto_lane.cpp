@@ -719,8 +719,8 @@ int lane_run_range(Lane* L, dto_pair* P, uint32_t perm_first, int64_t n_perm, ui
     if (built_late) LCK(cudaEventRecord(L->evTables, L->side));
     const int nlev = kLadderLevels;
     // Batches in flight: while batch b's later table levels, exhaustive
-    // fallback and result copy run on the side stream, the next batches'
-    // labels and level-0 table sweeps run on the main stream.
+    // fallback and result copy run on its slot's side stream, the next
+    // batches' labels and level-0 table sweeps run on the main stream.
     auto harvest = [&](BatchSlot& sl) -> int {
       LCK(cudaEventSynchronize(sl.ev[7]));
       float ms = 0.f;
