@@ -43,13 +43,31 @@ METRIC = "perms/s on 1 GB300 at N=20k (FP32-screen vs plain FP64, same argmin); 
 N_FEATURES = 20000
 RHO = 0.2
 PERMS_PER_STEP = 100000
-# DRAM bytes per task of the level-0 table sweep at N = 20,000 (ncu capture
-# summarised in profiles/table_grid_level0_n20k.md): labels read once, hit
-# buffer written and re-read.
+# DRAM bytes per task of the level-0 table sweep at N = 20,000, from an ncu
+# capture of one level-0 launch (dram__bytes_read.sum + dram__bytes_write.sum
+# over its tasks): labels read once, hit buffer written and re-read.
 SWEEP0_DRAM_BYTES_PER_TASK = 51900.0
 WORKLOAD = ("single pair, N=20000 features, list 2 Gaussian copula rho=0.2 to list 1, no ties, "
             "100000 on-device Philox permutations per step + the unpermuted task, "
             "FP32 screen + FP64 refine")
+
+
+def single_config(P):
+    """The config object of the headline workload, the same for both arms."""
+    import math
+    from dual_threshold_optimization_gb300 import synth
+
+    def n_thresholds(max_rank):  # T = 1, T <- floor(1.01 T + 1) while T <= max rank
+        n, t = 0, 1
+        while t <= max_rank:
+            n, t = n + 1, int(math.floor(t * 1.01 + 1.0))
+        return n
+    pair = synth.copula_pair(N_FEATURES, RHO, seed=2)
+    grid = [n_thresholds(int(pair.ranks1.max())), n_thresholds(int(pair.ranks2.max()))]
+    return {"workload": WORKLOAD, "n_features": N_FEATURES, "rho": RHO, "permutations": P,
+            "grid": grid, "pair_seed": 2,
+            "l2": "inputs larger than L2: each step streams %d MB of permutation labels"
+                  % (P * N_FEATURES * 2 // 1000000)}
 
 
 def dist_env():
@@ -256,8 +274,7 @@ def run_reference(args):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total / max(args.steps, 1),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (seeded Gaussian-copula lists)",
-        "config": {"workload": WORKLOAD, "n_features": N_FEATURES, "rho": RHO,
-                   "permutations": PERMS_PER_STEP},
+        "config": single_config(PERMS_PER_STEP),
         "cpu_baseline": {"value": value, "unit": "perms/s", "cores": threads, "kind": "port",
                          "sample": sample},
         "e2e": {"value": value, "unit": "perms/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -362,8 +379,8 @@ def run_gpu(args):
                 "launch_ms": s0_ms / s0_launches if s0_launches else None,
                 "tasks_per_launch": s0_tasks / s0_launches if s0_launches else None,
                 "peak_source": "measured: cuBLAS SGEMM 8192^3 without TF32 on this GPU (FP32 pipe)",
-                "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one level-0 launch "
-                                  "(profiles/table_grid_level0_n20k.md), scaled to this launch's tasks",
+                "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one level-0 "
+                                  "launch at N=20000, per task, scaled to this launch's tasks",
                 "whole_search": {"achieved": whole, "frac": whole / fp32_peak if fp32_peak else None,
                                  "note": "all search kernels of a step (table levels, exhaustive "
                                          "fallback, first batch), CUDA-event times summed over streams"},
@@ -396,12 +413,11 @@ def run_gpu(args):
         "warmup": args.warmup, "ms_per_step": t_max / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "int32+f32 screen, f64 refine",
         "data": "synthetic (seeded Gaussian-copula lists)",
-        "config": {"workload": WORKLOAD, "n_features": N_FEATURES, "rho": RHO, "permutations": P,
-                   "grid": [dp.n1, dp.n2],
-                   "ladder": "value: the pair keeps the table ladder its warm-up runs measured; "
-                             "e2e: a new pair each step, so its first run measures the ladder",
-                   "l2": "inputs larger than L2: each step streams %d MB of permutation labels"
-                         % (P * N_FEATURES * 2 // 1000000)},
+        "config": single_config(P),
+        "ladder": "value: the pair keeps the table ladder its warm-up runs measured; e2e: a new "
+                  "pair each step, so its first run measures the ladder",
+        "routes_per_step": {k: v / args.steps for k, v in
+                            ((k, sum(s_["n_route"][k] for s_ in summaries)) for k in summaries[0]["n_route"])},
         "latency_ms": {"p50": statistics.median(step_ms),
                        "p99": sorted(step_ms)[min(len(step_ms) - 1, int(0.99 * len(step_ms)))]},
         "e2e": {"value": e2e_value, "unit": "perms/s", "h2d_bytes_per_step": h2d,

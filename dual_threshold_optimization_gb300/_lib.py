@@ -39,17 +39,23 @@ class DtoResult(C.Structure):
                 ("set2_len", C.c_int64), ("population_size", C.c_int64),
                 ("intersection_size", C.c_int64), ("pvalue", C.c_double),
                 ("permuted", C.c_int32), ("i", C.c_int32), ("j", C.c_int32),
-                ("status", C.c_int32)]
+                ("status", C.c_int32), ("route", C.c_int32), ("reserved", C.c_int32)]
 
     def as_dict(self):
-        return {k: getattr(self, k) for k, _ in self._fields_}
+        return {k: getattr(self, k) for k, _ in self._fields_ if k != "reserved"}
 
 
 RESULT_DTYPE = np.dtype([("rank1", np.uint32), ("rank2", np.uint32), ("set1_len", np.int64),
                          ("set2_len", np.int64), ("population_size", np.int64),
                          ("intersection_size", np.int64), ("pvalue", np.float64),
                          ("permuted", np.int32), ("i", np.int32), ("j", np.int32),
-                         ("status", np.int32)], align=True)
+                         ("status", np.int32), ("route", np.int32), ("reserved", np.int32)],
+                        align=True)
+# The fields that describe a task's optimum: every search path gives the same
+# values here; "route" names the path that settled the task.
+OPTIMUM_FIELDS = ("rank1", "rank2", "set1_len", "set2_len", "population_size", "intersection_size",
+                  "pvalue", "permuted", "i", "j", "status")
+ROUTE_NAMES = ("none", "screen", "level0", "level1", "level2", "fallback", "fp64", "unused")
 assert RESULT_DTYPE.itemsize == C.sizeof(DtoResult)
 
 
@@ -60,10 +66,13 @@ class DtoSummary(C.Structure):
                 ("n_refined", C.c_int64), ("n_stage2", C.c_int64),
                 ("device_ms", C.c_double), ("grid_ms", C.c_double), ("perm_ms", C.c_double),
                 ("n_launches", C.c_int64), ("h2d_bytes", C.c_int64), ("d2h_bytes", C.c_int64),
-                ("sweep0_ms", C.c_double), ("sweep0_launches", C.c_int64), ("sweep0_tasks", C.c_int64)]
+                ("sweep0_ms", C.c_double), ("sweep0_launches", C.c_int64), ("sweep0_tasks", C.c_int64),
+                ("n_route", C.c_int64 * 8)]
 
     def as_dict(self):
-        return {k: getattr(self, k) for k, _ in self._fields_}
+        d = {k: getattr(self, k) for k, _ in self._fields_ if k != "n_route"}
+        d["n_route"] = {ROUTE_NAMES[q]: int(self.n_route[q]) for q in range(7)}
+        return d
 
 
 class DtoError(RuntimeError):

@@ -58,16 +58,6 @@ def build(force=False, verbose=False, jobs=None):
     flags = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
                     "-Xcompiler", "-ffp-contract=off", "-Xcompiler", "-fvisibility=hidden",
                     "-I", INCLUDE, "-I", CSRC]
-    for knob in ("DTO_GRID_WARPS", "DTO_BUCKET_BITS", "DTO_TABLE_PACKED",
-                  "DTO_TABLE_WARPS", "DTO_TABLE_MINB", "DTO_TABLE_TASKS", "DTO_FIRST_BATCH",
-                  "DTO_FIRST_COOP", "DTO_LADDER_LEVELS", "DTO_SIDE_PRIORITY",
-                  "DTO_TIGHT_TABLES", "DTO_EARLY_HITS", "DTO_SLOTS", "DTO_PERM_WORDS_MAXL",
-                  "DTO_LAST_LEVELS", "DTO_BATCH_SHIFT",
-                  "DTO_TIGHT_LEVELS"):
-        if os.environ.get(knob):
-            flags += ["-D%s=%d" % (knob, int(os.environ[knob]))]
-    if os.environ.get("DTO_L0_QUANTILE"):
-        flags += ["-DDTO_L0_QUANTILE=%.4f" % float(os.environ["DTO_L0_QUANTILE"])]
     if verbose:
         flags += ["-Xptxas", "-v"]
     srcs = _sources()

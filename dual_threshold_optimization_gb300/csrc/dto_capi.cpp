@@ -127,6 +127,14 @@ std::vector<uint32_t> thresholds_of(uint32_t max_rank) {
 
 constexpr int kCs[] = {4, 8, 12, 16, 20, 24, 28, 32};
 
+// The pair argument of an entry point: present and created on this context.
+int pair_check(dto_ctx* ctx, const dto_pair* P, const char* fn) {
+  if (!ctx) return DTO_ERR_INVALID;
+  if (!P) return set_err(ctx, DTO_ERR_INVALID, std::string(fn) + ": null pair");
+  if (P->ctx != ctx) return set_err(ctx, DTO_ERR_INVALID, std::string(fn) + ": the pair belongs to another context");
+  return DTO_OK;
+}
+
 int pick_C(int n2) {
   for (int c : kCs)
     if (32 * c >= n2) return c;
@@ -439,7 +447,8 @@ int dto_run(dto_ctx* ctx, dto_pair* P, int64_t n_perm, uint64_t seed, const int3
 int dto_run_range(dto_ctx* ctx, dto_pair* P, uint32_t perm_first, int64_t n_perm, uint64_t seed,
                   const int32_t* perm_idx, int precision, dto_result* out_unpermuted, double* out_minp,
                   dto_result* out_perm, dto_summary* out_summary) {
-  if (!ctx || !P || P->ctx != ctx || !out_unpermuted) return set_err(ctx, DTO_ERR_INVALID, "null argument");
+  if (int rc = pair_check(ctx, P, "dto_run_range")) return rc;
+  if (!out_unpermuted) return set_err(ctx, DTO_ERR_INVALID, "dto_run_range: null out_unpermuted");
   std::lock_guard<std::mutex> g(ctx->mu);
   return lane_run_range(ctx->lane0, P, perm_first, n_perm, seed, perm_idx, precision, out_unpermuted, out_minp,
                         out_perm, out_summary);
@@ -447,7 +456,8 @@ int dto_run_range(dto_ctx* ctx, dto_pair* P, uint32_t perm_first, int64_t n_perm
 
 int dto_optimize(dto_ctx* ctx, dto_pair* P, int permute, uint64_t seed, uint32_t perm_id, const int32_t* idx1,
                  const int32_t* idx2, int precision, dto_result* out) {
-  if (!ctx || !P || P->ctx != ctx || !out) return set_err(ctx, DTO_ERR_INVALID, "null argument");
+  if (int rc = pair_check(ctx, P, "dto_optimize")) return rc;
+  if (!out) return set_err(ctx, DTO_ERR_INVALID, "dto_optimize: null out");
   if (precision != DTO_PRECISION_FP64 && precision != DTO_PRECISION_SCREEN)
     return set_err(ctx, DTO_ERR_INVALID, "unknown precision");
   std::lock_guard<std::mutex> g(ctx->mu);
@@ -487,7 +497,8 @@ int dto_optimize(dto_ctx* ctx, dto_pair* P, int permute, uint64_t seed, uint32_t
 }
 
 int dto_grid_dump(dto_ctx* ctx, dto_pair* P, const int32_t* idx1, const int32_t* idx2, dto_result* records) {
-  if (!ctx || !P || P->ctx != ctx || !records) return set_err(ctx, DTO_ERR_INVALID, "null argument");
+  if (int rc = pair_check(ctx, P, "dto_grid_dump")) return rc;
+  if (!records) return set_err(ctx, DTO_ERR_INVALID, "dto_grid_dump: null records");
   std::lock_guard<std::mutex> g(ctx->mu);
   Lane* L = ctx->lane0;
   CK(cudaSetDevice(ctx->device));
@@ -521,7 +532,7 @@ int dto_grid_dump(dto_ctx* ctx, dto_pair* P, const int32_t* idx1, const int32_t*
   const int permuted = (idx1 && idx2) ? 1 : 0;
   const long long nt2 = (long long)P->T2.size();
   for (long long c = 0; c < ncell; ++c) {
-    TaskResult r{hp[(size_t)c], (int)(c / nt2), (int)(c % nt2), hk[(size_t)c], 0};
+    TaskResult r{hp[(size_t)c], (int)(c / nt2), (int)(c % nt2), hk[(size_t)c], DTO_ROUTE_FP64};
     fill_result(P, r, permuted, &records[c]);
   }
   return DTO_OK;
@@ -561,8 +572,9 @@ int dto_hypergeom_sf(dto_ctx* ctx, const int64_t* N, const int64_t* K, const int
 
 int dto_export_permutations(dto_ctx* ctx, dto_pair* P, uint64_t seed, uint32_t perm_first, int64_t count,
                             int32_t* idx1, int32_t* idx2) {
-  if (!ctx || !P || P->ctx != ctx || count < 0 || (count > 0 && (!idx1 || !idx2)))
-    return set_err(ctx, DTO_ERR_INVALID, "null argument");
+  if (int rc = pair_check(ctx, P, "dto_export_permutations")) return rc;
+  if (count < 0 || (count > 0 && (!idx1 || !idx2)))
+    return set_err(ctx, DTO_ERR_INVALID, "dto_export_permutations: null argument");
   if (count == 0) return DTO_OK;
   std::lock_guard<std::mutex> g(ctx->mu);
   Lane* L = ctx->lane0;
@@ -598,7 +610,8 @@ int dto_export_permutations(dto_ctx* ctx, dto_pair* P, uint64_t seed, uint32_t p
 
 int dto_run_range_noalloc(dto_ctx* ctx, dto_pair* P, uint32_t perm_first, int64_t n_perm, uint64_t seed,
                           double* d_minp) {
-  if (!ctx || !P || P->ctx != ctx || n_perm < 0 || (n_perm > 0 && !d_minp))
+  if (int rc = pair_check(ctx, P, "dto_run_range_noalloc")) return rc;
+  if (n_perm < 0 || (n_perm > 0 && !d_minp))
     return set_err(ctx, DTO_ERR_INVALID, "dto_run_range_noalloc: null argument");
   if ((long long)perm_first + n_perm > 0xffffffffLL)
     return set_err(ctx, DTO_ERR_INVALID, "dto_run_range_noalloc: permutation ids out of range");
@@ -641,6 +654,10 @@ int dto_run_range_noalloc(dto_ctx* ctx, dto_pair* P, uint32_t perm_first, int64_
     a.list_tag = 1;
     a.Ylab = P->dYlab;
     a.X = X;
+    // only each grid row's multiset of labels reaches the search, so buckets
+    // that lie inside one row keep their order, as in a dto_run_range run
+    a.rowstart = P->dRow;
+    a.n1 = P->dev.n1;
     CK(launch_perm(a, cnt, L->stream));
   } else {
     const long long ss = P->N1 + P->N2;
@@ -673,6 +690,7 @@ int dto_run_range_noalloc(dto_ctx* ctx, dto_pair* P, uint32_t perm_first, int64_
   gk.xstride = xs;
   gk.ntask = cnt;
   gk.mode = kModeScreen;
+  gk.route = DTO_ROUTE_SCREEN;
   gk.smemF = grid_smem_bytes(P->C, P->dev.n1, P->npop, 1) <= ctx->smem_optin ? 1 : 0;
   gk.out = res;
   gk.work = work;

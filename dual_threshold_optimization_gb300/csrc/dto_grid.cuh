@@ -403,7 +403,7 @@ __global__ void __launch_bounds__(kGridWarps * 32, 1) grid_kernel(const GridArgs
       });
       n64 += (unsigned long long)n1 * (unsigned long long)tvalid;
       warp_best(best);
-      if (lane == 0) A.out[b] = TaskResult{best.p, best.i, best.j, best.k, 0};
+      if (lane == 0) A.out[b] = TaskResult{best.p, best.i, best.j, best.k, A.route};
       continue;
     }
 
@@ -627,12 +627,12 @@ __global__ void __launch_bounds__(kGridWarps * 32, 1) grid_kernel(const GridArgs
         Best bb = best_init();
         if (lane < kGridWarps) bb = Best{sBestP[lane], sBestK[lane], sBestI[lane], sBestJ[lane]};
         warp_best(bb);
-        if (lane == 0) A.out[b] = TaskResult{bb.p, bb.i, bb.j, bb.k, 0};
+        if (lane == 0) A.out[b] = TaskResult{bb.p, bb.i, bb.j, bb.k, A.route};
       }
       continue;
     }
     if (A.guess_hist != nullptr && lane == 0) bound_record(A.guess_hist, B, scale);
-    if (lane == 0) A.out[b] = TaskResult{best64.p, best64.i, best64.j, best64.k, 0};
+    if (lane == 0) A.out[b] = TaskResult{best64.p, best64.i, best64.j, best64.k, A.route};
   }
   if (lane == 0 && A.n_refined) {
     atomicAdd(A.n_refined, n64);

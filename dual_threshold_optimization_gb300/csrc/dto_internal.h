@@ -65,11 +65,11 @@ struct PairDev {
   const int* map12;      // [N1]: list-2 position of the feature at list-1 position p, or -1
 };
 
-// One task's optimum.
+// One task's optimum; route is the DTO_ROUTE_* code of the path that settled it.
 struct TaskResult {
   double p;
   int i, j, k;
-  int status;
+  int route;
 };
 
 enum GridMode { kModeFull64 = 0, kModeScreen = 1, kModeDump = 2 };
@@ -80,6 +80,7 @@ struct GridArgs {
   long long xstride;
   int ntask;
   int mode;
+  int route;             // DTO_ROUTE_* written with each result
   int smemF;             // 1: the fixed-point table is staged in shared memory
   int coop;              // screen mode: the CTA's warps share each task
   TaskResult* out;       // [ntask]
@@ -185,6 +186,7 @@ struct TableGridArgs {
   int tight_tau[3];
   int ntight;
   int packed;             // 16-bit overlap sweep (every overlap <= 0x7FFF)
+  int route;              // DTO_ROUTE_* written with each result
   int smemF;              // the ln m! table is copied to shared memory
   TaskResult* out;
   int* work;

@@ -215,7 +215,9 @@ void fill_result(const dto_pair* P, const TaskResult& r, int permuted, dto_resul
   o->permuted = permuted;
   o->i = r.i;
   o->j = r.j;
-  o->status = r.status;
+  o->status = DTO_OK;
+  o->route = r.route;
+  o->reserved = 0;
 }
 
 // Batch size of a run: 2^DTO_BATCH_SHIFT bytes of labels (2 GiB), and at
@@ -260,6 +262,7 @@ int lane_grid_tasks(Lane* L, dto_pair* P, const int16_t* dX, long long xstride, 
   a.xstride = xstride;
   a.ntask = ntask;
   a.mode = mode;
+  a.route = mode == kModeFull64 ? DTO_ROUTE_FP64 : DTO_ROUTE_SCREEN;
   size_t smemF = grid_smem_bytes(P->C, P->dev.n1, P->npop, 1);
   a.smemF = smemF <= L->ctx->smem_optin ? 1 : 0;
   a.out = dOut;
@@ -334,6 +337,7 @@ int table_levels(Lane* L, dto_pair* P, const int16_t* X, long long xstride, int 
       a.tight_tau[q] = L->kthr_tau[tight_slot(level, q)];
     }
     a.packed = P->ncommon <= kPackedMaxCommon ? 1 : 0;
+    a.route = DTO_ROUTE_LEVEL0 + level;
     a.smemF = table_smem_bytes(P->C, P->dev.n1, P->dev.n2, P->npop, 1) <= L->ctx->smem_optin ? 1 : 0;
     a.out = dOut;
     a.work = cnts + level;
@@ -366,6 +370,7 @@ int table_exhaustive(Lane* L, dto_pair* P, const int16_t* X, long long xstride, 
   g.xstride = xstride;
   g.ntask = ntask;
   g.mode = kModeScreen;
+  g.route = DTO_ROUTE_FALLBACK;
   g.smemF = grid_smem_bytes(P->C, P->dev.n1, P->npop, 1) <= L->ctx->smem_optin ? 1 : 0;
   g.coop = 1;  // the few tasks left here are the hard ones: a CTA each
   g.out = dOut;
@@ -513,7 +518,8 @@ void ladder_of(const std::vector<double>& all, int fshift, int tau[kLadderTaus])
 int lane_run_range(Lane* L, dto_pair* P, uint32_t perm_first, int64_t n_perm, uint64_t seed,
                    const int32_t* perm_idx, int precision, dto_result* out_unpermuted, double* out_minp,
                    dto_result* out_perm, dto_summary* out_summary) {
-  if (!P || P->ctx != L->ctx || !out_unpermuted) return lane_err(L, DTO_ERR_INVALID, "null argument");
+  if (!P || !out_unpermuted) return lane_err(L, DTO_ERR_INVALID, "null argument");
+  if (P->ctx != L->ctx) return lane_err(L, DTO_ERR_INVALID, "the pair belongs to another context");
   if (n_perm < 0 || n_perm > 0x7fffffffLL || (long long)perm_first + n_perm > 0xffffffffLL)
     return lane_err(L, DTO_ERR_INVALID, "n_perm out of range");
   if (precision != DTO_PRECISION_FP64 && precision != DTO_PRECISION_SCREEN)
@@ -544,6 +550,7 @@ int lane_run_range(Lane* L, dto_pair* P, uint32_t perm_first, int64_t n_perm, ui
   LCK(cudaMemsetAsync(L->dGuess, 0, 2048, L->stream));
   LCK(cudaEventRecord(L->ev0, L->stream));
   std::vector<double> minp((size_t)n_perm);
+  long long nroute[DTO_ROUTES] = {};
   TaskResult unperm{};
   // Short runs (and FP64 runs) go through the exhaustive screen in batches,
   // the unpermuted task (task 0) in row 0 of the first.  Long runs go through
@@ -564,6 +571,7 @@ int lane_run_range(Lane* L, dto_pair* P, uint32_t perm_first, int64_t n_perm, ui
         return lane_err(L, DTO_ERR_CUDA, msg);
       }
       minp[(size_t)(b0 + q)] = r.p;
+      ++nroute[(r.route >= 0 && r.route < DTO_ROUTES) ? r.route : DTO_ROUTE_NONE];
       if (out_minp) out_minp[b0 + q] = r.p;
       if (out_perm) fill_result(P, r, 1, &out_perm[b0 + q]);
     }
@@ -812,6 +820,7 @@ int lane_run_range(Lane* L, dto_pair* P, uint32_t perm_first, int64_t n_perm, ui
     }
   }
   fill_result(P, unperm, 0, out_unpermuted);
+  ++nroute[(unperm.route >= 0 && unperm.route < DTO_ROUTES) ? unperm.route : DTO_ROUTE_NONE];
   const double p_obs = unperm.p;
   long long count_le = 0;
   for (long long q = 0; q < n_perm; ++q) count_le += (minp[(size_t)q] <= p_obs);
@@ -842,6 +851,7 @@ int lane_run_range(Lane* L, dto_pair* P, uint32_t perm_first, int64_t n_perm, ui
     s.sweep0_ms = L->acc_sweep0_ms;
     s.sweep0_launches = L->acc_sweep0_launches;
     s.sweep0_tasks = L->acc_sweep0_tasks;
+    for (int q = 0; q < DTO_ROUTES; ++q) s.n_route[q] = nroute[q];
   }
   return DTO_OK;
 }

@@ -2,20 +2,24 @@
 // that allocates nothing.
 //
 // Some callers cannot call cudaMalloc at the moment they want a permutation
-// null: code running while a CUDA graph is being captured, a memory manager
-// that owns every device allocation of the process, or a host runtime that
-// forbids allocation on its request path.  For them, the intermediates of the
-// run (permutation labels, the task counter, per-task optima) live in one
-// file-scope device array of fixed size, kNoAllocBytes.  Every GPU that loads
-// libdto.so holds that array until the process exits.
+// null: a process whose memory manager owns every device allocation (a
+// framework's pool with a fixed budget, an embedding host that hands device
+// memory out itself), or a host runtime that forbids allocation on its
+// request path.  For them, the intermediates of the run (permutation labels,
+// the task counter, per-task optima) live in one file-scope device array of
+// fixed size, kNoAllocBytes.  Every GPU that loads libdto.so holds that array
+// until the process exits.
 //
 // Host code cannot use the array's name as a device address: in host code it
 // names a host-side stand-in.  The device address is obtained once per
 // device, with that device current, by cudaGetSymbolAddress, and passed to the
-// kernels.  All calls share the array and it keeps the last call's contents;
-// the task counter is cleared by every call.  Calls whose GPU work overlaps
-// (two streams, or two host threads on different contexts of one device)
-// race on the array.
+// kernels.  The cached address belongs to the device's primary context (every
+// call makes the device current with cudaSetDevice, which selects it); after
+// cudaDeviceReset, or under another context of the same device, the cache is
+// not valid, and those uses are not supported.  All calls share the array and
+// it keeps the last call's contents; the task counter is cleared by every
+// call.  Calls whose GPU work overlaps (two streams, or two host threads with
+// contexts on one device) race on the array.
 #include <cuda_runtime.h>
 
 #include <mutex>
@@ -34,9 +38,9 @@ std::mutex g_mu;
 void* g_ptr[kMaxDevices] = {};
 }  // namespace
 
-// Device address of the scratch array on `device` (which must be current).
-// The first call on a device resolves it; it must come before any stream
-// capture that the caller wants to record the entry point into.
+// Device address of the scratch array on `device` (which must be current, in
+// its primary context).  The first call on a device resolves it, so that first
+// call should come before any stream capture.
 cudaError_t noalloc_scratch(int device, void** ptr, size_t* bytes) {
   if (device < 0 || device >= kMaxDevices) return cudaErrorInvalidDevice;
   std::lock_guard<std::mutex> g(g_mu);

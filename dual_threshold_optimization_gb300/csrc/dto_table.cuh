@@ -199,7 +199,7 @@ static __device__ __noinline__ void table_pending_flush(const TableGridArgs& A, 
       Best b = best_init();
       for (int r = q; r < np && m.pendTask[r] == task; ++r)
         best_take(b, m.pendP[r], m.pendK[r], m.pendCell[r] >> 16, m.pendCell[r] & 0xffff);
-      A.out[task] = TaskResult{b.p, b.i, b.j, b.k, 0};
+      A.out[task] = TaskResult{b.p, b.i, b.j, b.k, A.route};
     }
   }
   __syncwarp();
@@ -636,7 +636,7 @@ __global__ void __launch_bounds__(kTableWarps * 32, kTableCtasPerSm) table_grid_
           table_defer(A, g, mt, lane, bt[t]);
         } else {
           table_refine(A, g, mt, lane);
-          if (lane == 0) A.out[bt[t]] = TaskResult{mt.st->bp, mt.st->bi, mt.st->bj, mt.st->bk, 0};
+          if (lane == 0) A.out[bt[t]] = TaskResult{mt.st->bp, mt.st->bi, mt.st->bj, mt.st->bk, A.route};
         }
       } else {
         // no cell reaches the guess: the next level (or the exhaustive

@@ -13,6 +13,7 @@ run_multi_node    src/run/multi_node.rs:47-162 -- the reference scatters task ch
                   every result; the other ranks return [].
 """
 import os
+import time
 
 import numpy as np
 
@@ -38,6 +39,25 @@ def make_tasks(permutations):
     return [Task(0, False)] + [Task(i, True) for i in range(1, permutations + 1)]
 
 
+class RunResults(list):
+    """The per-task OptimizationResults of a run, in task order (what the
+    reference's run_single_node returns), plus ``summary``: the run's error
+    bounds and throughput, which empirical_pvalue adds to its output
+    (logp_err_bound_fp32, logp_err_bound_fp64, perms_per_s)."""
+
+    def __init__(self, items=(), summary=None):
+        super().__init__(items)
+        self.summary = summary or {}
+
+
+def run_summary(summary, n_perm, seconds):
+    """The extra output keys of a run from its dto_summary."""
+    return {"logp_err_bound_fp32": float(summary["logp_err_bound_screen"]),
+            "logp_err_bound_fp64": float(summary["logp_err_bound_fp64"]),
+            "perms_per_s": (n_perm / seconds) if seconds > 0 else None,
+            "n_perm": int(n_perm), "seconds": float(seconds)}
+
+
 def _records_to_results(recs, permuted):
     out = []
     for r in recs:
@@ -54,12 +74,15 @@ def _seed_or_random(seed):
 
 
 def run_single_node(tasks, ranked_feature_list1, ranked_feature_list2, population_size,
-                    num_threads=1, *, seed=None, precision="screen", engine=None):
-    """Run every task; returns one OptimizationResult per task, in task order.
+                    num_threads=1, *, seed=None, precision="screen", engine=None, perm_indices=None):
+    """Run every task; returns one OptimizationResult per task, in task order
+    (a RunResults list carrying the run's summary).
 
     num_threads is accepted for the reference's signature; the GPU path ignores
     it (the reference treats 0 as 1, main.rs:73-76).  Permuted task t uses
-    permutation id t of the Philox stream ``seed``.
+    permutation id t of the Philox stream ``seed``, or, in test mode, row t - 1
+    of ``perm_indices`` ([P][N1 + N2]: the permuted views' index arrays of
+    both lists, src/collections/permuted.rs:34).
     """
     eng = engine or default_engine()
     r1, f1, r2, f2, nf = dense_ids(ranked_feature_list1, ranked_feature_list2)
@@ -67,11 +90,19 @@ def run_single_node(tasks, ranked_feature_list1, ranked_feature_list2, populatio
     seed = _seed_or_random(seed)
     perm_ids = sorted(t.id for t in tasks if t.permute)
     out = {}
+    t0 = time.perf_counter()
     if perm_ids:
         lo, hi = perm_ids[0], perm_ids[-1]
-        res = dp.run(hi, seed=seed, precision=precision, want_records=True) if lo >= 1 else None
-        if res is None:
+        if lo < 1:
             raise ValueError("permuted task ids must be >= 1")
+        idx = None
+        if perm_indices is not None:
+            idx = np.ascontiguousarray(perm_indices, np.int32)
+            if idx.ndim != 2 or idx.shape[0] < hi or idx.shape[1] != dp.N1 + dp.N2:
+                raise ValueError("perm_indices must have shape (P, N1 + N2) with P >= %d rows of %d"
+                                 % (hi, dp.N1 + dp.N2))
+            idx = idx[:hi]
+        res = dp.run(hi, seed=seed, perm_idx=idx, precision=precision, want_records=True)
         unperm = res.unpermuted
         for t in tasks:
             if t.permute:
@@ -79,14 +110,16 @@ def run_single_node(tasks, ranked_feature_list1, ranked_feature_list2, populatio
                 d["permuted"] = True
                 out[t.id] = OptimizationResult.Best(OptimizationResultRecord.from_abi(d))
     else:
-        unperm = dp.run(0, precision=precision).unpermuted
+        res = dp.run(0, precision=precision)
+        unperm = res.unpermuted
+    seconds = time.perf_counter() - t0
     for t in tasks:
         if not t.permute:
             d = dict(unperm)
             d["permuted"] = False
             out[t.id] = OptimizationResult.Best(OptimizationResultRecord.from_abi(d))
     dp.close()
-    return [out[t.id] for t in tasks]
+    return RunResults([out[t.id] for t in tasks], run_summary(res.summary, len(perm_ids), seconds))
 
 
 def shard_range(n_perm, rank, world):

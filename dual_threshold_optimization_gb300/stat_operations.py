@@ -59,7 +59,15 @@ def empirical_pvalue(results):
     """empirical_pvalue.rs:109-187: the fraction of permuted optima with p <= the
     unpermuted optimum's p (1.0 without permutations), plus the FDR at
     sensitivity 0.8.  ``results``: OptimizationResult objects (Best) or dicts
-    with the record fields."""
+    with the record fields.
+
+    The keys are the reference's (empirical_pvalue.rs:176-186).  When
+    ``results`` is a run's output carrying its summary (run.RunResults), three
+    more are added: ``logp_err_bound_fp32`` (bound, in nats, on the error of
+    the 32-bit screen's log-pmf; 0 for the plain FP64 path),
+    ``logp_err_bound_fp64`` (bound on the relative error of an FP64 p-value,
+    hence on its log) and ``perms_per_s`` (permutations per second of the run,
+    host wall time)."""
     recs = [_record(r) for r in results]
     unperm = [r for r in recs if r is not None and not r["permuted"]]
     perm = [r for r in recs if r is not None and r["permuted"]]
@@ -74,9 +82,14 @@ def empirical_pvalue(results):
         emp = float(np.count_nonzero(pv <= u["pvalue"])) / float(len(pv))
     else:
         emp = 1.0
-    return {
+    out = {
         "rank1": int(u["rank1"]), "rank2": int(u["rank2"]), "set1_len": int(u["set1_len"]),
         "set2_len": int(u["set2_len"]), "population_size": int(u["population_size"]),
         "unpermuted_intersection_size": int(u["intersection_size"]),
         "unpermuted_pvalue": float(u["pvalue"]), "empirical_pvalue": emp, "fdr": est_fdr,
     }
+    summary = getattr(results, "summary", None)
+    if summary:
+        for k in ("logp_err_bound_fp32", "logp_err_bound_fp64", "perms_per_s"):
+            out[k] = summary.get(k)
+    return out

@@ -44,6 +44,17 @@ extern "C" {
 #define DTO_PRECISION_SCREEN 1 /* 32-bit log-space screen of every cell, FP64 refine of the
                                   cells within the proven margin; same argmin, same p */
 
+/* Which search path settled a task (dto_result.route).  Every path returns the
+ * same optimum; the code says only which one did the work. */
+#define DTO_ROUTE_NONE 0      /* not recorded */
+#define DTO_ROUTE_SCREEN 1    /* exhaustive screen: short runs, a long run's first batch, task 0 */
+#define DTO_ROUTE_LEVEL0 2    /* table screen, level 0 of the ladder */
+#define DTO_ROUTE_LEVEL1 3    /* table screen, level 1 */
+#define DTO_ROUTE_LEVEL2 4    /* table screen, level 2 */
+#define DTO_ROUTE_FALLBACK 5  /* exhaustive screen of a task no table level settled */
+#define DTO_ROUTE_FP64 6      /* plain FP64 path (DTO_PRECISION_FP64) */
+#define DTO_ROUTES 8
+
 typedef struct dto_ctx dto_ctx;
 typedef struct dto_pair dto_pair;
 
@@ -60,6 +71,8 @@ typedef struct {
     int32_t permuted;            /* 0 for the unpermuted task */
     int32_t i, j;                /* grid indices of (rank1, rank2) */
     int32_t status;              /* 0, or DTO_ERR_* for this task */
+    int32_t route;               /* DTO_ROUTE_*: the search path that settled the task */
+    int32_t reserved;
 } dto_result;
 
 /* Summary of a permutation run: the inputs of empirical_pvalue()
@@ -83,6 +96,7 @@ typedef struct {
     double sweep0_ms;              /* CUDA-event time of the level-0 table sweeps (main stream) */
     int64_t sweep0_launches;       /* their launches */
     int64_t sweep0_tasks;          /* permutations they took */
+    int64_t n_route[DTO_ROUTES];   /* tasks (unpermuted included) settled by each DTO_ROUTE_* */
 } dto_summary;
 
 DTO_API int dto_version(void);
@@ -160,20 +174,23 @@ DTO_API int dto_run_range(dto_ctx* ctx, dto_pair* pair, uint32_t perm_first, int
                           dto_summary* out_summary);
 
 /* No counterpart in the reference.  dto_run_range for callers that cannot
- * allocate device memory when they run it -- code recording a CUDA graph, or a
- * process whose memory manager owns every device allocation.  It calls no
- * allocating routine: permutation labels, the task counter and the per-task
- * optima live in a fixed 32 MiB device array inside libdto.so (held on every
- * GPU that loads the library until the process exits).  The caller passes the
- * pair (created beforehand with dto_pair_create) and d_minp, device memory of
- * n_perm doubles that receives each permutation's minimum p-value (the same
- * values as dto_run_range, exhaustive screen).  At most
+ * allocate device memory when they run it: a process whose memory manager owns
+ * every device allocation (a framework's fixed-budget pool, a host application
+ * that hands out device memory itself), or a runtime that forbids allocation
+ * on its request path.  It calls no allocating routine: permutation labels,
+ * the task counter and the per-task optima live in a fixed 32 MiB device array
+ * inside libdto.so (held on every GPU that loads the library until the process
+ * exits).  The caller passes the pair (created beforehand with
+ * dto_pair_create) and d_minp, device memory of n_perm doubles that receives
+ * each permutation's minimum p-value (the same values as dto_run_range,
+ * exhaustive screen).  At most
  * 32 MiB / (24 + 2 * round8(n1) [+ 4 (n1 + n2) when the lists' feature sets
  * differ]) permutations per call (about 830 at n1 = n2 = 20,000); larger
  * n_perm -> DTO_ERR_INVALID.  The work is enqueued on the context's stream and
  * the call returns without waiting.  The first call on a device resolves the
- * array's device address and should come before any stream capture.  Calls
- * share the array: calls whose GPU work overlaps race. */
+ * array's device address (in the device's primary context) and should come
+ * before any stream capture.  Calls share the array: calls whose GPU work
+ * overlaps race. */
 DTO_API int dto_run_range_noalloc(dto_ctx* ctx, dto_pair* pair, uint32_t perm_first, int64_t n_perm,
                                   uint64_t seed, double* d_minp);
 

@@ -41,6 +41,62 @@ def test_cli_on_reference_test_data(tmp_path, capsys):
     assert json.loads(capsys.readouterr().out)["population_size"] == 30
 
 
+REFERENCE_KEYS = ("empirical_pvalue", "fdr", "population_size", "rank1", "rank2", "set1_len",
+                  "set2_len", "unpermuted_intersection_size", "unpermuted_pvalue")
+EXTRA_KEYS = ("logp_err_bound_fp32", "logp_err_bound_fp64", "perms_per_s")
+
+
+def test_cli_output_contract_and_test_mode(tmp_path, capsys):
+    # the reference's nine keys, unchanged and in sorted order, plus the three
+    # extra keys; --perm-indices runs the uploaded permutations, whose optima
+    # equal the oracle's
+    from dual_threshold_optimization_gb300 import synth
+    from dual_threshold_optimization_gb300.cli import main
+    from oracle import oracle as O
+    p = synth.copula_pair(400, 0.3, seed=81, frac_tied2=0.1)
+    names = p.feature_names()
+    for q, (r, f) in enumerate(((p.ranks1, p.feat1), (p.ranks2, p.feat2))):
+        (tmp_path / ("l%d.csv" % (q + 1))).write_text("".join("%s,%d\n" % (names[x], y) for x, y in zip(f, r)))
+    l1 = col.RankedFeatureList.from_(col.FeatureList([names[f] for f in p.feat1]), p.ranks1)
+    l2 = col.RankedFeatureList.from_(col.FeatureList([names[f] for f in p.feat2]), p.ranks2)
+    rng = np.random.default_rng(4)
+    P = 24
+    idx = np.stack([np.concatenate([rng.permutation(400), rng.permutation(400)]) for _ in range(P)])
+    np.save(tmp_path / "perms.npy", idx.astype(np.int32))
+    rc = main(["-1", str(tmp_path / "l1.csv"), "-2", str(tmp_path / "l2.csv"),
+               "--perm-indices", str(tmp_path / "perms.npy")])
+    assert rc == 0
+    text = capsys.readouterr().out
+    out = json.loads(text)
+    assert set(out) == set(REFERENCE_KEYS) | set(EXTRA_KEYS)
+    assert list(out) == sorted(out)
+    ref = [k for k in out if k in REFERENCE_KEYS]
+    assert ref == list(REFERENCE_KEYS)
+    assert out["logp_err_bound_fp32"] > 0 and 0 < out["logp_err_bound_fp64"] < 1e-12
+    assert out["perms_per_s"] > 0
+    # the empirical p-value of the uploaded permutations, from the oracle
+    r1, f1, r2, f2, nf = col.dense_ids(l1, l2)
+    ob, _ = O.optimize(r1, f1, r2, f2, nf, 400)
+    pv = [O.optimize(r1, f1, r2, f2, nf, 400, idx[b, :400], idx[b, 400:])[0]["pvalue"] for b in range(P)]
+    assert out["unpermuted_pvalue"] == ob["pvalue"]
+    assert out["empirical_pvalue"] == O.empirical(ob["pvalue"], pv)
+    # text rows work too; a row count that disagrees with -p is an error
+    (tmp_path / "perms.txt").write_text("\n".join(",".join(map(str, r)) for r in idx[:5]))
+    assert main(["-1", str(tmp_path / "l1.csv"), "-2", str(tmp_path / "l2.csv"),
+                 "--perm-indices", str(tmp_path / "perms.txt"), "--precision", "fp64"]) == 0
+    o5 = json.loads(capsys.readouterr().out)
+    assert o5["empirical_pvalue"] == O.empirical(ob["pvalue"], pv[:5])
+    assert o5["logp_err_bound_fp32"] == 0.0
+    assert main(["-1", str(tmp_path / "l1.csv"), "-2", str(tmp_path / "l2.csv"), "-p", "7",
+                 "--perm-indices", str(tmp_path / "perms.txt")]) == 101
+    bad = idx[:2].copy()
+    bad[0, 0] = bad[0, 1]
+    np.save(tmp_path / "bad.npy", bad.astype(np.int32))
+    assert main(["-1", str(tmp_path / "l1.csv"), "-2", str(tmp_path / "l2.csv"),
+                 "--perm-indices", str(tmp_path / "bad.npy")]) == 101
+    assert "not a permutation" in capsys.readouterr().err
+
+
 def test_optimize_and_debug():
     g = GOLDEN["optimize_10"]
     l1, l2 = rlist(g["genes1"], g["ranks1"]), rlist(g["genes2"], g["ranks2"])
