@@ -430,6 +430,24 @@ int dto_pair_set_stream(dto_pair* P, uint32_t stream_id) {
   return DTO_OK;
 }
 
+int dto_pair_set_ladder(dto_pair* P, const double* minp, int64_t count) {
+  if (!P || count < 0 || (count > 0 && !minp)) return DTO_ERR_INVALID;
+  std::vector<double> v;
+  v.reserve((size_t)count);
+  for (int64_t q = 0; q < count; ++q) {
+    if (!(minp[q] >= 0.0 && minp[q] <= 1.0)) return set_err(P->ctx, DTO_ERR_INVALID, "dto_pair_set_ladder: p-values must lie in [0, 1]");
+    v.push_back(minp[q]);
+  }
+  std::lock_guard<std::mutex> g(P->ladder_mu);
+  if (count == 0) {
+    P->ladder_ok = false;
+    return DTO_OK;
+  }
+  ladder_of(v, P->fshift, P->ladder_tau);
+  P->ladder_ok = true;
+  return DTO_OK;
+}
+
 int dto_pair_order(const dto_pair* P, int32_t* o1, int32_t* o2) {
   if (!P) return DTO_ERR_INVALID;
   if (o1) std::copy(P->order1.begin(), P->order1.end(), o1);
@@ -448,7 +466,6 @@ int dto_run_range(dto_ctx* ctx, dto_pair* P, uint32_t perm_first, int64_t n_perm
                   const int32_t* perm_idx, int precision, dto_result* out_unpermuted, double* out_minp,
                   dto_result* out_perm, dto_summary* out_summary) {
   if (int rc = pair_check(ctx, P, "dto_run_range")) return rc;
-  if (!out_unpermuted) return set_err(ctx, DTO_ERR_INVALID, "dto_run_range: null out_unpermuted");
   std::lock_guard<std::mutex> g(ctx->mu);
   return lane_run_range(ctx->lane0, P, perm_first, n_perm, seed, perm_idx, precision, out_unpermuted, out_minp,
                         out_perm, out_summary);

@@ -197,6 +197,10 @@ int lane_run_range(Lane* L, dto_pair* P, uint32_t perm_first, int64_t n_perm, ui
                    const int32_t* perm_idx, int precision, dto_result* out_unpermuted, double* out_minp,
                    dto_result* out_perm, dto_summary* out_summary);
 
+// The table ladder's bounds (fixed-point ln p, kLadderTaus of them) from a
+// sample of minimum p-values, in ladder order.
+void ladder_of(const std::vector<double>& all, int fshift, int tau[kLadderTaus]);
+
 // Bytes of device scratch a run of the pair holds at its peak (labels of the
 // batches in flight, results, hit buffers, table screens).
 long long run_device_bytes(const dto_ctx* ctx, const dto_pair* P, int64_t n_perm, bool test_mode);

@@ -518,7 +518,7 @@ void ladder_of(const std::vector<double>& all, int fshift, int tau[kLadderTaus])
 int lane_run_range(Lane* L, dto_pair* P, uint32_t perm_first, int64_t n_perm, uint64_t seed,
                    const int32_t* perm_idx, int precision, dto_result* out_unpermuted, double* out_minp,
                    dto_result* out_perm, dto_summary* out_summary) {
-  if (!P || !out_unpermuted) return lane_err(L, DTO_ERR_INVALID, "null argument");
+  if (!P) return lane_err(L, DTO_ERR_INVALID, "null argument");
   if (P->ctx != L->ctx) return lane_err(L, DTO_ERR_INVALID, "the pair belongs to another context");
   if (n_perm < 0 || n_perm > 0x7fffffffLL || (long long)perm_first + n_perm > 0xffffffffLL)
     return lane_err(L, DTO_ERR_INVALID, "n_perm out of range");
@@ -533,6 +533,9 @@ int lane_run_range(Lane* L, dto_pair* P, uint32_t perm_first, int64_t n_perm, ui
     }
   }
   const int mode = precision == DTO_PRECISION_FP64 ? kModeFull64 : kModeScreen;
+  // without out_unpermuted the unpermuted task is not run (a replica that
+  // takes a range of permutation ids while another computes the observed p)
+  const bool want0 = out_unpermuted != nullptr;
   const long long xs = xstride_of(P->N1);
   const long long batch = batch_of(P, n_perm, perm_idx != nullptr);
   int rc = lane_grow(L, &L->dRes, &L->resBytes, (size_t)(batch + 1) * sizeof(TaskResult));
@@ -590,7 +593,7 @@ int lane_run_range(Lane* L, dto_pair* P, uint32_t perm_first, int64_t n_perm, ui
   };
   if (!use_table) {
     for (long long b0 = 0; b0 < std::max<long long>(n_perm, 1); b0 += batch) {
-      const int row0 = (b0 == 0) ? 1 : 0;
+      const int row0 = (b0 == 0 && want0) ? 1 : 0;
       const int cnt = (int)std::max(0LL, std::min(batch, n_perm - b0));
       const int32_t* dI = nullptr;
       rc = upload_idx(&dIdx, &idxBytes, b0, cnt, &dI);
@@ -604,6 +607,7 @@ int lane_run_range(Lane* L, dto_pair* P, uint32_t perm_first, int64_t n_perm, ui
       }
       if (row0) LCK(cudaMemcpyAsync(L->dX, P->dYlab, (size_t)P->N1 * 2, cudaMemcpyDeviceToDevice, L->stream));
       const int ntask = cnt + row0;
+      if (ntask == 0) continue;
       rc = lane_grid_tasks(L, P, (const int16_t*)L->dX, xs, ntask, mode, dRes, nullptr, nullptr, true);
       if (rc) return rc;
       LCK(cudaMemcpyAsync(hRes, dRes, (size_t)ntask * sizeof(TaskResult), cudaMemcpyDeviceToHost, L->stream));
@@ -654,11 +658,17 @@ int lane_run_range(Lane* L, dto_pair* P, uint32_t perm_first, int64_t n_perm, ui
     LCK(cudaMemcpyAsync(L->dX, P->dYlab, (size_t)P->N1 * 2, cudaMemcpyDeviceToDevice, L->stream));
     LCK(cudaEventRecord(L->evSide, L->stream));
     LCK(cudaStreamWaitEvent(L->side, L->evSide, 0));
-    rc = lane_grid_tasks(L, P, (const int16_t*)L->dX, xs, cnt0 + 1, mode, dRes, nullptr, nullptr, !warm, L->side,
-                         warm || (kFirstBatchCoop && L->coop_first));
-    if (rc) return rc;
-    LCK(cudaMemcpyAsync(hRes, dRes, (size_t)(cnt0 + 1) * sizeof(TaskResult), cudaMemcpyDeviceToHost, L->side));
-    L->acc_d2h += (long long)(cnt0 + 1) * (long long)sizeof(TaskResult);
+    // task 0 sits in row 0 of the first batch; without want0 only rows 1.. run
+    const int r0 = want0 ? 0 : 1;
+    const bool first_launch = cnt0 + 1 - r0 > 0;
+    if (first_launch) {
+      rc = lane_grid_tasks(L, P, (const int16_t*)L->dX + (size_t)r0 * xs, xs, cnt0 + 1 - r0, mode, dRes + r0,
+                           nullptr, nullptr, !warm, L->side, warm || (kFirstBatchCoop && L->coop_first));
+      if (rc) return rc;
+      LCK(cudaMemcpyAsync(hRes + r0, dRes + r0, (size_t)(cnt0 + 1 - r0) * sizeof(TaskResult),
+                          cudaMemcpyDeviceToHost, L->side));
+      L->acc_d2h += (long long)(cnt0 + 1 - r0) * (long long)sizeof(TaskResult);
+    }
     LCK(cudaEventRecord(L->evSide, L->side));
     // Labels of the pipelined batches b = 0, 1, ... (permutations
     // cnt0 + b * batch on), slot b % kSlots; the first two are drawn now.
@@ -698,9 +708,11 @@ int lane_run_range(Lane* L, dto_pair* P, uint32_t perm_first, int64_t n_perm, ui
       LCK(cudaEventSynchronize(L->evSide));
       float ms = 0.f;
       if (cnt0 > 0 && cudaEventElapsedTime(&ms, L->evk[0], L->evk[1]) == cudaSuccess) L->acc_perm_ms += ms;
-      if (cudaEventElapsedTime(&ms, L->evk[2], L->evk[3]) == cudaSuccess) L->acc_grid_ms += ms;
-      if (!valid(hRes[0])) return lane_err(L, DTO_ERR_CUDA, "unpermuted task: the search returned no grid cell");
-      unperm = hRes[0];
+      if (first_launch && cudaEventElapsedTime(&ms, L->evk[2], L->evk[3]) == cudaSuccess) L->acc_grid_ms += ms;
+      if (want0) {
+        if (!valid(hRes[0])) return lane_err(L, DTO_ERR_CUDA, "unpermuted task: the search returned no grid cell");
+        unperm = hRes[0];
+      }
       return take(hRes + 1, 0, cnt0);
     };
     if (!warm) {
@@ -819,11 +831,14 @@ int lane_run_range(Lane* L, dto_pair* P, uint32_t perm_first, int64_t n_perm, ui
       LCK(cudaStreamWaitEvent(L->stream, sl.ev[3], 0));
     }
   }
-  fill_result(P, unperm, 0, out_unpermuted);
-  ++nroute[(unperm.route >= 0 && unperm.route < DTO_ROUTES) ? unperm.route : DTO_ROUTE_NONE];
-  const double p_obs = unperm.p;
-  long long count_le = 0;
-  for (long long q = 0; q < n_perm; ++q) count_le += (minp[(size_t)q] <= p_obs);
+  long long count_le = -1;
+  if (want0) {
+    fill_result(P, unperm, 0, out_unpermuted);
+    ++nroute[(unperm.route >= 0 && unperm.route < DTO_ROUTES) ? unperm.route : DTO_ROUTE_NONE];
+    const double p_obs = unperm.p;
+    count_le = 0;
+    for (long long q = 0; q < n_perm; ++q) count_le += (minp[(size_t)q] <= p_obs);
+  }
   LCK(cudaEventRecord(L->ev1, L->stream));
   unsigned long long refined[3] = {0, 0, 0};
   LCK(cudaMemcpyAsync(refined, L->dRefined, sizeof(refined), cudaMemcpyDeviceToHost, L->stream));
@@ -834,9 +849,14 @@ int lane_run_range(Lane* L, dto_pair* P, uint32_t perm_first, int64_t n_perm, ui
     dto_summary& s = *out_summary;
     s.n_perm = n_perm;
     s.count_le = count_le;
-    s.empirical_pvalue = n_perm > 0 ? (double)count_le / (double)n_perm : 1.0;
-    s.fdr = dto_fdr(out_unpermuted->set1_len, out_unpermuted->set2_len, out_unpermuted->intersection_size,
-                    P->npop, 0.8);
+    if (want0) {
+      s.empirical_pvalue = n_perm > 0 ? (double)count_le / (double)n_perm : 1.0;
+      s.fdr = dto_fdr(out_unpermuted->set1_len, out_unpermuted->set2_len, out_unpermuted->intersection_size,
+                      P->npop, 0.8);
+    } else {
+      s.empirical_pvalue = std::nan("");
+      s.fdr = std::nan("");
+    }
     s.logp_err_bound_screen = precision == DTO_PRECISION_SCREEN ? 4.5 * std::ldexp(1.0, -P->fshift) : 0.0;
     s.logp_err_bound_fp64 = 2.0e-13;
     s.n_fallback = (int64_t)refined[2];

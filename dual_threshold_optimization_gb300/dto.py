@@ -63,15 +63,23 @@ class OptimizationResultRecord:
 
     def __init__(self, rank1, rank2, set1_len, set2_len, population_size, intersection_size,
                  pvalue, permuted, feature_sets=None):
-        self.rank1 = int(rank1)
-        self.rank2 = int(rank2)
-        self.set1_len = int(set1_len)
-        self.set2_len = int(set2_len)
-        self.population_size = int(population_size)
-        self.intersection_size = int(intersection_size)
+        def opt_int(v):
+            return None if v is None else int(v)
+        self.rank1 = opt_int(rank1)
+        self.rank2 = opt_int(rank2)
+        self.set1_len = opt_int(set1_len)
+        self.set2_len = opt_int(set2_len)
+        self.population_size = opt_int(population_size)
+        self.intersection_size = opt_int(intersection_size)
         self.pvalue = float(pvalue)
         self.permuted = bool(permuted)
         self.feature_sets = feature_sets if feature_sets is not None else FeatureSets.none()
+
+    @classmethod
+    def pvalue_only(cls, pvalue, permuted=True):
+        """A permuted task's record when only its minimum p-value was gathered
+        (run_multi_node with gather="minp"): the other fields are None."""
+        return cls(None, None, None, None, None, None, pvalue, permuted)
 
     @classmethod
     def from_abi(cls, rec, feature_sets=None):

@@ -227,6 +227,14 @@ class DevicePair:
         """Philox stream id of this pair's permutations (default 0)."""
         check(lib().dto_pair_set_stream(self.handle, int(stream_id)))
 
+    def set_ladder(self, minp):
+        """Seed the table ladder of this pair's next long run from a sample of
+        minimum p-values (an earlier run's ``minp``); an empty sample forgets
+        it.  The ladder decides only which path settles each permutation."""
+        a = np.ascontiguousarray(np.asarray(minp, np.float64).reshape(-1))
+        check(lib().dto_pair_set_ladder(self.handle, ptr(a) if a.size else None, a.size),
+              self.engine.handle)
+
     @property
     def upload_bytes(self):
         """Host-to-device bytes dto_pair_create copied for this pair."""
@@ -245,7 +253,11 @@ class DevicePair:
         return o1, o2
 
     def run(self, n_perm, seed=0, perm_idx=None, precision="screen", want_minp=True,
-            want_records=False, first=1):
+            want_records=False, first=1, unpermuted=True):
+        """dto_run_range: permutations first .. first + n_perm - 1 of ``seed``
+        (or the rows of ``perm_idx``), plus the unpermuted task unless
+        ``unpermuted`` is False (then ``RunResult.unpermuted`` is None and the
+        summary's count_le is -1)."""
         ctx = self.engine.handle
         n_perm = int(n_perm)
         idx = None
@@ -258,9 +270,10 @@ class DevicePair:
         recs = np.zeros(n_perm, RESULT_DTYPE) if want_records else None
         summ = DtoSummary()
         check(lib().dto_run_range(ctx, self.handle, int(first), n_perm, int(seed) & (2**64 - 1),
-                                  ptr(idx), precision_code(precision), C.byref(unp), ptr(minp),
+                                  ptr(idx), precision_code(precision),
+                                  C.byref(unp) if unpermuted else None, ptr(minp),
                                   ptr(recs), C.byref(summ)), ctx)
-        return RunResult(unp.as_dict(), minp, recs, summ.as_dict())
+        return RunResult(unp.as_dict() if unpermuted else None, minp, recs, summ.as_dict())
 
     def optimize(self, permute=False, seed=0, perm_id=1, idx1=None, idx2=None, precision="screen"):
         ctx = self.engine.handle

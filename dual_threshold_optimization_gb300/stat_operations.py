@@ -71,13 +71,18 @@ def empirical_pvalue(results):
     recs = [_record(r) for r in results]
     unperm = [r for r in recs if r is not None and not r["permuted"]]
     perm = [r for r in recs if r is not None and r["permuted"]]
+    summary = getattr(results, "summary", None) or {}
     if len(unperm) != 1:
         warnings.warn("Expected exactly one unpermuted result, but found %d." % len(unperm))
     if not unperm:
         raise ValueError("No unpermuted result found in the provided results.")
     u = unperm[0]
     est_fdr = fdr(u["set1_len"], u["set2_len"], u["intersection_size"], u["population_size"], 0.8)
-    if perm:
+    if "count_le" in summary and "n_perm" in summary:
+        # a sharded run (run_multi_node) counted on every rank
+        n = int(summary["n_perm"])
+        emp = float(summary["count_le"]) / float(n) if n else 1.0
+    elif perm:
         pv = np.array([r["pvalue"] for r in perm], np.float64)
         emp = float(np.count_nonzero(pv <= u["pvalue"])) / float(len(pv))
     else:
@@ -88,8 +93,8 @@ def empirical_pvalue(results):
         "unpermuted_intersection_size": int(u["intersection_size"]),
         "unpermuted_pvalue": float(u["pvalue"]), "empirical_pvalue": emp, "fdr": est_fdr,
     }
-    summary = getattr(results, "summary", None)
     if summary:
         for k in ("logp_err_bound_fp32", "logp_err_bound_fp64", "perms_per_s"):
-            out[k] = summary.get(k)
+            if k in summary:
+                out[k] = summary[k]
     return out

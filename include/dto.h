@@ -144,6 +144,13 @@ DTO_API int dto_pair_thresholds(const dto_pair* pair, uint32_t* t1, uint32_t* t2
  * pair is a function of (seed, stream id, t).  Pairs that share a seed get
  * independent permutations by taking different stream ids. */
 DTO_API int dto_pair_set_stream(dto_pair* pair, uint32_t stream_id);
+/* No counterpart in the reference.  The pair's table ladder (the bounds that
+ * decide which table screen settles each permutation of a long run) from a
+ * sample of minimum p-values, e.g. a previous run's out_minp saved by another
+ * process; count = 0 forgets the ladder, so that the next long run measures
+ * it from a first batch.  The ladder decides only which path settles a task,
+ * never a result.  p-values outside [0, 1] -> DTO_ERR_INVALID. */
+DTO_API int dto_pair_set_ladder(dto_pair* pair, const double* minp, int64_t count);
 /* Host-to-device bytes that dto_pair_create copied (the pair's device tables). */
 DTO_API int64_t dto_pair_upload_bytes(const dto_pair* pair);
 DTO_API int dto_pair_order(const dto_pair* pair, int32_t* order1, int32_t* order2);
@@ -155,7 +162,7 @@ DTO_API int dto_pair_order(const dto_pair* pair, int32_t* order1, int32_t* order
  *   perm_idx:  NULL, or the permuted views' index arrays to use instead
  *              (src/collections/permuted.rs:34), host memory laid out
  *              [n_perm][n1 + n2]: idx1 (positions of list 1) then idx2.
- *   out_unpermuted: the unpermuted optimum (required).
+ *   out_unpermuted: the unpermuted optimum (NULL: not run, see dto_run_range).
  *   out_minp:  NULL or [n_perm] per-permutation minimum p-values.
  *   out_perm:  NULL or [n_perm] per-permutation optima.
  *   out_summary: NULL or the empirical p-value, FDR and error bounds. */
@@ -167,7 +174,10 @@ DTO_API int dto_run(dto_ctx* ctx, dto_pair* pair, int64_t n_perm, uint64_t seed,
  * is perm_first = 1).  A permutation depends only on (seed, pair, id), so
  * processes that split an id range between them (one GPU each) reproduce a
  * single run exactly; this replaces the MPI scatter of task chunks in
- * run_multi_node (src/run/multi_node.rs:114-161). */
+ * run_multi_node (src/run/multi_node.rs:114-161).  out_unpermuted may be NULL
+ * here: the unpermuted task is then not run (replicas other than the one that
+ * computes the observed optimum), and the summary's count_le is -1 and its
+ * empirical_pvalue and fdr NaN. */
 DTO_API int dto_run_range(dto_ctx* ctx, dto_pair* pair, uint32_t perm_first, int64_t n_perm,
                           uint64_t seed, const int32_t* perm_idx, int precision,
                           dto_result* out_unpermuted, double* out_minp, dto_result* out_perm,

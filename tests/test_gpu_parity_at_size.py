@@ -122,3 +122,27 @@ def test_config1_as_stated_vs_oracle(engine):
     assert set(np.unique(res.records["route"]).tolist()) == {SCREEN}
     _check_run(dp, pair, res, 11, np.random.default_rng(1), per_route=250, n_random=0, n_extreme=4)
     dp.close()
+
+
+def test_fallback_route_at_size(engine):
+    # A ladder seeded from the lower 70 % of an earlier run's minima is too
+    # tight for the rest: their permutations fall through all three table
+    # levels to the exhaustive screen (route "fallback"), whose optima must
+    # equal the oracle's like every other route's.
+    pair = synth.copula_pair(20000, 0.2, seed=2)
+    dp = engine.pair(pair.ranks1, pair.feat1, pair.ranks2, pair.feat2, pair.n_features,
+                     pair.population)
+    earlier = dp.run(20000, seed=3)
+    dp.set_ladder(np.sort(earlier.minp)[:14000])
+    res = dp.run(20000, seed=4, precision="screen", want_records=True)
+    routes = res.records["route"]
+    assert np.count_nonzero(routes == FALLBACK) > 100, res.summary["n_route"]
+    seen, _ = _check_run(dp, pair, res, 4, np.random.default_rng(9), per_route=32)
+    assert {LEVEL0, LEVEL1, LEVEL2, FALLBACK} <= seen
+    # the ladder decides only the route: a run with the pair's own ladder
+    # gives the same optima
+    dp.set_ladder([])
+    again = dp.run(20000, seed=4, precision="screen", want_records=True)
+    for f in FIELDS:
+        assert np.array_equal(again.records[f], res.records[f]), f
+    dp.close()
