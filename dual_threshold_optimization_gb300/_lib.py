@@ -18,6 +18,7 @@ DTO_ERR_OOM = 2
 DTO_ERR_TIMEOUT = 3
 DTO_ERR_CUDA = 4
 DTO_ERR_NOT_FOUND = 5
+DTO_ERR_CANCELLED = 6
 
 PRECISION_FP64 = 0
 PRECISION_SCREEN = 1
@@ -30,6 +31,7 @@ EXPORTS = (
     "dto_optimize",
     "dto_grid_dump", "dto_hypergeom_sf", "dto_export_permutations", "dto_fdr",
     "dto_serve_create", "dto_serve_destroy", "dto_serve_submit", "dto_serve_poll", "dto_serve_wait",
+    "dto_serve_wait_for", "dto_serve_cancel",
     "dto_serve_last_error", "dto_serve_stats", "dto_run_device_bytes", "dto_batch_run",
 )
 
@@ -134,6 +136,11 @@ def lib():
                                    C.POINTER(DtoResult), _P, C.POINTER(DtoSummary), C.POINTER(C.c_int64)]
     L.dto_serve_poll.argtypes = [_P, C.c_int64, C.POINTER(C.c_int)]
     L.dto_serve_wait.argtypes = [_P, C.c_int64, C.POINTER(C.c_double), C.POINTER(C.c_double)]
+    L.dto_serve_wait_for.argtypes = [_P, C.c_int64, C.c_double, C.POINTER(C.c_double),
+                                     C.POINTER(C.c_double)]
+    L.dto_serve_wait_for.restype = C.c_int
+    L.dto_serve_cancel.argtypes = [_P, C.c_int64]
+    L.dto_serve_cancel.restype = C.c_int
     L.dto_serve_last_error.argtypes = [_P]
     L.dto_serve_last_error.restype = C.c_char_p
     L.dto_serve_stats.argtypes = [_P, _P, _P, _P, _P]

@@ -188,6 +188,7 @@ const char* dto_status_string(int s) {
     case DTO_ERR_TIMEOUT: return "timeout";
     case DTO_ERR_CUDA: return "CUDA error";
     case DTO_ERR_NOT_FOUND: return "not found";
+    case DTO_ERR_CANCELLED: return "cancelled";
     default: return "unknown status";
   }
 }

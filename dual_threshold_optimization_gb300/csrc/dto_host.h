@@ -53,6 +53,10 @@ constexpr int tight_slot(int level, int q) { return 3 + 3 * level + q; }
 
 struct Lane {
   dto_ctx* ctx = nullptr;
+  // set by a server's worker to its request's cancel flag: a run checks it
+  // between batches and returns DTO_ERR_CANCELLED once its work in flight
+  // has drained (kernels are never interrupted)
+  std::atomic<int>* cancel = nullptr;
   std::string* err = nullptr;  // where this lane's error messages go
   std::string own_err;
   // first batch with a CTA per task: lowest latency for a run alone; lanes

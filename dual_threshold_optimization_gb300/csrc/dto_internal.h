@@ -151,7 +151,9 @@ constexpr int kTableCtasPerSm = DTO_TABLE_MINB;
 #endif
 constexpr int kTableTasks = DTO_TABLE_TASKS;
 static_assert(kTableTasks == 1 || kTableTasks == 2, "one or two tasks per warp");
-constexpr int kTableHitCap = 8192;
+constexpr int kTableHitCap = 8192;  // hit slots per task
+// hit slots per warp of a table sweep (the half-warp sweep runs two tasks)
+constexpr int kTableWarpHits = 2 * kTableHitCap;
 
 // The packed table sweep holds overlaps in 16-bit halves and tests
 // k >= kthr as the sign bit of k + (0x8000 - kthr): it needs every overlap,
@@ -162,14 +164,15 @@ constexpr int kTableHitCap = 8192;
 constexpr long long kPackedMaxCommon = DTO_TABLE_PACKED ? 0x7FFF : -1;
 
 struct TableArgs {
-  int n1, n2, N, C;
+  int n1, n2, N, C;      // C: columns per lane
+  int lanes;             // 32 (32-bit sweep) or 16 (half-warp packed sweep)
   const int* rowstart;   // K_i = rowstart[i+1]
   const int* ncnt;
   const uint32_t* F;
   int fshift;
   int tau;               // fixed-point ln p guess
   int packed;            // entry form of the packed (16-bit overlap) sweep
-  uint16_t* kthr;        // [n1][table_cq(C) / 8][32][8]
+  uint16_t* kthr;        // [n1][table_cq(C) / 8][lanes][8]
 };
 
 struct TableGridArgs {
@@ -178,7 +181,7 @@ struct TableGridArgs {
   long long xstride;
   int ntask;
   int tau;                // the guess the table was built for
-  const uint16_t* kthr;   // [n1][table_cq(C) / 8][32][8]
+  const uint16_t* kthr;   // table_build_kernel's layout for the sweep that reads it
   // tighter tables (bounds tight_tau[0] > tight_tau[1] > ...): once a
   // resolve has set a task's bound B, its remaining rows are swept against
   // the tightest table whose bound is still >= B
@@ -206,8 +209,10 @@ struct TableGridArgs {
 cudaError_t raise_smem_limit(const void* kernel, size_t bytes);
 
 size_t grid_smem_bytes(int C, int n1, long long Npop, int smemF);
-size_t table_smem_bytes(int C, int n1, int n2, long long Npop, int smemF);
-size_t table_entries(int C, int n1);
+// C is the pair's columns per lane of the 32-lane layout; packed pairs use
+// the half-warp sweep (16 lanes of 2 C columns).
+size_t table_smem_bytes(int C, int n1, int n2, long long Npop, int smemF, bool packed);
+size_t table_entries(int C, int n1, bool packed);
 cudaError_t launch_table_build(const TableArgs& a, int nsm, cudaStream_t s);
 cudaError_t launch_table_grid(const TableGridArgs& a, int C, int ctas, cudaStream_t s);
 cudaError_t launch_grid(const GridArgs& a, int grid_ctas, cudaStream_t s);

@@ -245,8 +245,8 @@ long long run_device_bytes(const dto_ctx* ctx, const dto_pair* P, int64_t n_perm
   long long b = first * xs * 2 + (long long)(batch + 1) * (long long)sizeof(TaskResult);  // first batch
   if (n_perm > 2048) {
     b += Lane::kSlots * batch * (xs * 2 + (long long)sizeof(TaskResult) + 12);                // batch slots
-    b += (1LL + Lane::kSlots) * kTableCtasPerSm * ctx->nsm * kTableWarps * kTableHitCap * kTableTasks * 8;  // hits
-    b += (long long)Lane::kTables * (long long)table_entries(P->C, P->dev.n1) * 2;           // tables
+    b += (1LL + Lane::kSlots) * kTableCtasPerSm * ctx->nsm * kTableWarps * kTableWarpHits * 8;  // hits
+    b += (long long)Lane::kTables * (long long)table_entries(P->C, P->dev.n1, P->ncommon <= kPackedMaxCommon) * 2;  // tables
   }
   if (test_mode || !P->same_set) b += 2 * batch * L12 * 4;  // index scratch
   return b;
@@ -287,19 +287,23 @@ int lane_grid_tasks(Lane* L, dto_pair* P, const int16_t* dX, long long xstride, 
 int ensure_table(Lane* L, dto_pair* P, int level, int tau, cudaStream_t stream, bool* built) {
   if (L->kthr_pair[level] == P->serial && L->kthr_tau[level] == tau) return DTO_OK;
   *built = true;
-  int rc = lane_grow(L, (void**)&L->dKthr[level], &L->kthrBytes[level], table_entries(P->C, P->dev.n1) * 2);
+  const bool packed = P->ncommon <= kPackedMaxCommon;
+  int rc = lane_grow(L, (void**)&L->dKthr[level], &L->kthrBytes[level], table_entries(P->C, P->dev.n1, packed) * 2);
   if (rc) return rc;
   TableArgs t{};
   t.n1 = P->dev.n1;
   t.n2 = P->dev.n2;
   t.N = (int)P->npop;
-  t.C = P->C;
+  // the half-warp packed sweep reads 16 lanes of 2 C columns, the 32-bit
+  // sweep 32 lanes of C
+  t.C = packed ? 2 * P->C : P->C;
+  t.lanes = packed ? 16 : 32;
   t.rowstart = P->dRow;
   t.ncnt = P->dNcnt;
   t.F = P->dF;
   t.fshift = P->fshift;
   t.tau = tau;
-  t.packed = P->ncommon <= kPackedMaxCommon ? 1 : 0;
+  t.packed = packed ? 1 : 0;
   t.kthr = L->dKthr[level];
   LCK(launch_table_build(t, L->ctx->nsm, stream));
   L->acc_launches += 1;
@@ -318,7 +322,8 @@ int ensure_table(Lane* L, dto_pair* P, int level, int tau, cudaStream_t stream, 
 int table_levels(Lane* L, dto_pair* P, const int16_t* X, long long xstride, int ntask, TaskResult* dOut,
                  int lev_begin, int lev_end, int* fall, int* cnts, cudaStream_t stream, int hb, int tight_levels) {
   const int cap = std::max(ntask, 1);
-  const int hitcap = kTableHitCap * kTableTasks;
+  const int hitcap = kTableWarpHits;
+  const bool packed = P->ncommon <= kPackedMaxCommon;
   int rc = lane_grow(L, &L->dHits[hb], &L->hitBytes[hb], (size_t)kTableCtasPerSm * L->ctx->nsm * kTableWarps * hitcap * 8);
   if (rc) return rc;
   if (lev_begin == 0) LCK(cudaMemsetAsync(cnts, 0, 12 * sizeof(int), stream));
@@ -336,9 +341,9 @@ int table_levels(Lane* L, dto_pair* P, const int16_t* X, long long xstride, int 
       a.tight[q] = L->dKthr[tight_slot(level, q)];
       a.tight_tau[q] = L->kthr_tau[tight_slot(level, q)];
     }
-    a.packed = P->ncommon <= kPackedMaxCommon ? 1 : 0;
+    a.packed = packed ? 1 : 0;
     a.route = DTO_ROUTE_LEVEL0 + level;
-    a.smemF = table_smem_bytes(P->C, P->dev.n1, P->dev.n2, P->npop, 1) <= L->ctx->smem_optin ? 1 : 0;
+    a.smemF = table_smem_bytes(P->C, P->dev.n1, P->dev.n2, P->npop, 1, packed) <= L->ctx->smem_optin ? 1 : 0;
     a.out = dOut;
     a.work = cnts + level;
     a.n_refined = L->dRefined;
@@ -351,7 +356,8 @@ int table_levels(Lane* L, dto_pair* P, const int16_t* X, long long xstride, int 
     // a later level sees the tasks the earlier ones left (about 10 % and 1 %
     // of the batch); one warp per expected task keeps its latency to one sweep
     const double expect = level == 0 ? 1.0 : level == 1 ? 0.15 : 0.03;
-    const int want = (int)(expect * (double)ntask / kTableWarps) + 1;
+    const int per_warp = packed ? 2 : kTableTasks;  // tasks a warp sweeps at once
+    const int want = (int)(expect * (double)ntask / (kTableWarps * per_warp)) + 1;
     const int ctas = std::max(1, std::min(kTableCtasPerSm * L->ctx->nsm, want));
     LCK(launch_table_grid(a, P->C, ctas, stream));
   }
@@ -552,6 +558,18 @@ int lane_run_range(Lane* L, dto_pair* P, uint32_t perm_first, int64_t n_perm, ui
   LCK(cudaMemsetAsync(L->dRefined, 0, 3 * sizeof(unsigned long long), L->stream));
   LCK(cudaMemsetAsync(L->dGuess, 0, 2048, L->stream));
   LCK(cudaEventRecord(L->ev0, L->stream));
+  // a server's cancel request, checked between batches: the work in flight
+  // drains and the run returns DTO_ERR_CANCELLED
+  auto cancelled = [&]() -> int {
+    if (!L->cancel || L->cancel->load() == 0) return DTO_OK;
+    cudaStreamSynchronize(L->stream);
+    cudaStreamSynchronize(L->side);
+    for (BatchSlot& sl : L->slot) {
+      if (sl.side) cudaStreamSynchronize(sl.side);
+      sl.busy = false;
+    }
+    return lane_err(L, DTO_ERR_CANCELLED, "the request was cancelled");
+  };
   std::vector<double> minp((size_t)n_perm);
   long long nroute[DTO_ROUTES] = {};
   TaskResult unperm{};
@@ -593,6 +611,7 @@ int lane_run_range(Lane* L, dto_pair* P, uint32_t perm_first, int64_t n_perm, ui
   };
   if (!use_table) {
     for (long long b0 = 0; b0 < std::max<long long>(n_perm, 1); b0 += batch) {
+      if ((rc = cancelled())) return rc;
       const int row0 = (b0 == 0 && want0) ? 1 : 0;
       const int cnt = (int)std::max(0LL, std::min(batch, n_perm - b0));
       const int32_t* dI = nullptr;
@@ -759,6 +778,7 @@ int lane_run_range(Lane* L, dto_pair* P, uint32_t perm_first, int64_t n_perm, ui
       return DTO_OK;
     };
     for (long long it = 0; it < npipe; ++it) {
+      if ((rc = cancelled())) return rc;
       BatchSlot& sl = L->slot[it % Lane::kSlots];
       if (sl.busy) {
         rc = harvest(sl);

@@ -12,6 +12,7 @@
 // exactly what dto_run_range computes for it alone: permutations are a
 // function of (seed, stream id, permutation id), and every kernel's result is
 // independent of what else runs.
+#include <atomic>
 #include <chrono>
 #include <condition_variable>
 #include <deque>
@@ -42,6 +43,8 @@ struct Job {
   long long need = 0;  // device bytes reserved while it runs
   int status = DTO_OK;
   bool done = false;
+  bool started = false;
+  std::atomic<int> cancel{0};  // set by dto_serve_cancel; the run stops at its next batch
   std::string err;
   Clock::time_point t_submit, t_start, t_end;
 };
@@ -89,13 +92,16 @@ void worker(dto_server* s, int w) {
       s->queue.pop_front();
       s->reserved += j->need;
       s->running += 1;
+      j->started = true;
       j->t_start = Clock::now();
     }
     s->lane_err[(size_t)w].clear();
     dto_result unperm{};
+    L->cancel = &j->cancel;
     const int rc = lane_run_range(L, j->pair, j->first, j->n_perm, j->seed, nullptr, j->precision,
                                   j->out_unpermuted ? j->out_unpermuted : &unperm, j->out_minp, nullptr,
                                   j->out_summary);
+    L->cancel = nullptr;
     {
       std::lock_guard<std::mutex> lk(s->mu);
       j->status = rc;
@@ -205,7 +211,10 @@ int dto_serve_poll(dto_server* s, dto_job job, int* done) {
   return DTO_OK;
 }
 
-int dto_serve_wait(dto_server* s, dto_job job, double* queue_ms, double* run_ms) {
+// Waits for a request (timeout_ms < 0: without limit).  A finished request
+// returns its status and is forgotten; one still queued or running when the
+// time runs out returns DTO_ERR_TIMEOUT and stays known.
+static int serve_wait(dto_server* s, dto_job job, double timeout_ms, double* queue_ms, double* run_ms) {
   if (!s) return DTO_ERR_INVALID;
   std::unique_lock<std::mutex> lk(s->mu);
   auto it = s->jobs.find(job);
@@ -214,14 +223,59 @@ int dto_serve_wait(dto_server* s, dto_job job, double* queue_ms, double* run_ms)
     return DTO_ERR_NOT_FOUND;
   }
   Job* j = it->second;
-  s->cv_done.wait(lk, [&] { return j->done; });
-  if (queue_ms) *queue_ms = ms_between(j->t_submit, j->t_start);
-  if (run_ms) *run_ms = ms_between(j->t_start, j->t_end);
+  if (timeout_ms < 0.0) {
+    s->cv_done.wait(lk, [&] { return j->done; });
+  } else if (!s->cv_done.wait_for(lk, std::chrono::duration<double, std::milli>(timeout_ms),
+                                  [&] { return j->done; })) {
+    s->err = j->started ? "dto_serve_wait: the request is still running" : "dto_serve_wait: the request is still queued";
+    return DTO_ERR_TIMEOUT;
+  }
+  if (queue_ms) *queue_ms = j->started ? ms_between(j->t_submit, j->t_start) : ms_between(j->t_submit, j->t_end);
+  if (run_ms) *run_ms = j->started ? ms_between(j->t_start, j->t_end) : 0.0;
   const int status = j->status;
   if (status) s->err = j->err;
   s->jobs.erase(it);
   delete j;
   return status;
+}
+
+int dto_serve_wait(dto_server* s, dto_job job, double* queue_ms, double* run_ms) {
+  return serve_wait(s, job, -1.0, queue_ms, run_ms);
+}
+
+int dto_serve_wait_for(dto_server* s, dto_job job, double timeout_ms, double* queue_ms, double* run_ms) {
+  if (!(timeout_ms >= 0.0)) return DTO_ERR_INVALID;
+  return serve_wait(s, job, timeout_ms, queue_ms, run_ms);
+}
+
+int dto_serve_cancel(dto_server* s, dto_job job) {
+  if (!s) return DTO_ERR_INVALID;
+  {
+    std::lock_guard<std::mutex> lk(s->mu);
+    auto it = s->jobs.find(job);
+    if (it == s->jobs.end()) {
+      s->err = "dto_serve_cancel: unknown request";
+      return DTO_ERR_NOT_FOUND;
+    }
+    Job* j = it->second;
+    if (j->done) return DTO_OK;  // finished already: its results stand
+    if (!j->started) {
+      for (auto q = s->queue.begin(); q != s->queue.end(); ++q)
+        if (*q == j) {
+          s->queue.erase(q);
+          break;
+        }
+      j->status = DTO_ERR_CANCELLED;
+      j->err = "dto_serve_cancel: cancelled before it started";
+      j->t_end = Clock::now();
+      j->done = true;
+    } else {
+      j->cancel.store(1);  // the run stops at its next batch boundary
+    }
+  }
+  s->cv_done.notify_all();
+  s->cv_work.notify_all();  // the next request may now be the head
+  return DTO_OK;
 }
 
 const char* dto_serve_last_error(dto_server* s) { return s ? s->err.c_str() : "null server"; }

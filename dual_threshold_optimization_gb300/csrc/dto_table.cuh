@@ -32,21 +32,24 @@ __host__ __device__ constexpr int table_cq(int C) { return (C + 7) & ~7; }
 __host__ __device__ constexpr int table_wp(int C) { return 4 * ((table_cq(C) / 8) | 1); }
 
 // One thread per entry: binary search for the first overlap that passes.
-// Layout [i][q][lane][8]: entry t of a lane's row is in its q = t / 8-th
-// 16-byte chunk, so a warp's load of chunk q reads 512 contiguous bytes.
+// Layout [i][q][lane][8] for A.lanes lanes of A.C columns each (32 lanes of C
+// for the 32-bit sweep, 16 lanes of 2 C for the half-warp packed sweep):
+// entry t of a lane's row is in its q = t / 8-th 16-byte chunk, so a load of
+// chunk q by the lanes reads lanes x 16 contiguous bytes.
 // Plain entries hold kthr (0xFFFF: never); packed entries hold
 // 0x8000 - min(kthr, 0x8000) (0: never).
 static __global__ void table_build_kernel(const TableArgs A) {
   const int Cq = table_cq(A.C);
-  const long long cells = (long long)A.n1 * 32 * Cq;
+  const int lanes = A.lanes;
+  const long long cells = (long long)A.n1 * lanes * Cq;
   const double scale = ldexp(1.0, A.fshift);
   const int tauT = A.tau + (int)ceil(kTableMargin * scale);
   const uint32_t FN = __ldg(A.F + A.N);
   for (long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x; c < cells;
        c += (long long)gridDim.x * blockDim.x) {
-    const int i = (int)(c / (32 * Cq));
-    const int rem = (int)(c % (32 * Cq));
-    const int q = rem / 256, lane = (rem / 8) % 32;
+    const int i = (int)(c / (lanes * Cq));
+    const int rem = (int)(c % (lanes * Cq));
+    const int q = rem / (8 * lanes), lane = (rem / 8) % lanes;
     const int t = 8 * q + rem % 8;
     const int j = lane * A.C + t;
     int thr = 0x10000;  // never
@@ -655,6 +658,316 @@ __global__ void __launch_bounds__(kTableWarps * 32, kTableCtasPerSm) table_grid_
   }
 }
 
+// ---------------------------------------------------------------------------
+// The packed sweep with a half-warp per task.
+//
+// Lane h (0..15) of half-warp t owns the C2 consecutive columns
+// [h C2, (h + 1) C2) of task t as C2 / 2 words of two 16-bit counts, so two
+// tasks share every instruction of the row loop: the row bounds, the loop
+// control, the table-row loads (both halves read the same 256 bytes) and the
+// scan.  Per row:
+//   1. each label of the row adds 1 to its column's half-word (one shared
+//      atomic; a 2 KB table maps a label to its word and half);
+//   2. each lane runs the in-lane prefix of its counts in NG independent
+//      chains (x 0x10001 + R, then the upper half carried), keeping every
+//      word's two partial overlaps in registers; the chains' totals give the
+//      lane's total, and a 4-step scan over the half-warp its offset E;
+//   3. overlap + (0x8000 - kthr) sets bit 15 (31) of a half exactly when the
+//      overlap reaches the table's threshold, tested for all words with one
+//      OR; only a lane with a set bit records its hits, straight from the
+//      registers.
+// Overlaps stay below 0x8000 (the lists share at most 0x7FFF features), so no
+// half carries into the other.  The hits, resolves and task ends are those of
+// table_grid_kernel (one task at a time, the whole warp).
+// ---------------------------------------------------------------------------
+__host__ __device__ constexpr int hw_cq(int C2) { return (C2 + 7) & ~7; }
+// counter words per lane: C2 / 2 words padded to an odd number of 16-byte
+// chunks (a quarter-warp's 128-bit loads hit distinct banks)
+__host__ __device__ constexpr int hw_wp(int C2) { return 4 * ((hw_cq(C2) / 8) | 1); }
+__host__ __device__ constexpr int hw_task_ints(int C2) {
+  return 16 * hw_wp(C2) + (int)(sizeof(WarpTask) / 4) + 3 * kTableSurvCap;
+}
+__host__ __device__ constexpr int hw_warp_ints(int C2) { return 2 * hw_task_ints(C2) + 2 * kCandCap + 5 * kPend; }
+// label -> counter offset table: one entry per counter slot of the 32-lane
+// label encoding (lane * (C | 1) + t)
+__host__ __device__ constexpr int hw_lut_entries(int C) { return 32 * (C | 1); }
+
+__device__ __forceinline__ TableWarpMem hw_warp_mem(int* base, int C2, int t) {
+  TableWarpMem m;
+  int* tb = base + t * hw_task_ints(C2);
+  m.cnt = tb;
+  m.tot = nullptr;
+  m.st = reinterpret_cast<WarpTask*>(tb + 16 * hw_wp(C2));
+  m.q = reinterpret_cast<WarpTask*>(base + 16 * hw_wp(C2));
+  m.survCell = reinterpret_cast<int*>(m.st + 1);
+  m.survK = m.survCell + kTableSurvCap;
+  m.survLo = m.survK + kTableSurvCap;
+  int* sh = base + 2 * hw_task_ints(C2);
+  m.cand = reinterpret_cast<int2*>(sh);
+  m.pendP = reinterpret_cast<double*>(m.cand + kCandCap);
+  m.pendTask = reinterpret_cast<int*>(m.pendP + kPend);
+  m.pendCell = m.pendTask + kPend;
+  m.pendK = m.pendCell + kPend;
+  return m;
+}
+
+template <int C2>
+__global__ void __launch_bounds__(kTableWarps * 32, 1) table_hw_kernel(const TableGridArgs A) {
+  constexpr int C = C2 / 2;        // columns per lane of the 32-lane label encoding
+  constexpr int Cp = C | 1;
+  constexpr int NQ = hw_cq(C2) / 8;  // 16-byte table chunks per lane per row
+  constexpr int NW = C2 / 2;         // counter words per lane
+  constexpr int Wp = hw_wp(C2);
+  constexpr int TI = hw_task_ints(C2);
+  constexpr int NG = (NW % 4 == 0) ? 4 : (NW % 2 == 0 ? 2 : 1);  // independent chains
+  constexpr int GW = NW / NG;
+  static_assert(C2 % 2 == 0 && NW <= 4 * NQ, "packed columns come in pairs");
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int h = lane & 15, half = lane >> 4;
+  const int n1 = A.P.n1;
+  const int Npop = (int)A.P.Npop;
+  uint32_t* sF = reinterpret_cast<uint32_t*>(smem_raw);
+  int* sRow = reinterpret_cast<int*>(sF + (A.smemF ? ((Npop + 1 + 3) & ~3) : 0));
+  int* sNcnt = sRow + ((n1 + 1 + 3) & ~3);
+  uint16_t* sLut = reinterpret_cast<uint16_t*>(sNcnt + ((A.P.n2 + 3) & ~3));
+  int* sWarp = reinterpret_cast<int*>(sLut + ((hw_lut_entries(C) + 7) & ~7));
+  int* const wb = sWarp + warp * hw_warp_ints(C2);
+  for (int q = threadIdx.x; q <= n1; q += blockDim.x) sRow[q] = __ldg(A.P.rowstart + q);
+  for (int q = threadIdx.x; q < A.P.n2; q += blockDim.x) sNcnt[q] = __ldg(A.P.ncnt + q);
+  if (A.smemF)
+    for (int q = threadIdx.x; q <= Npop; q += blockDim.x) sF[q] = __ldg(A.P.F + q);
+  for (int q = threadIdx.x; q < hw_lut_entries(C); q += blockDim.x) {
+    const int l = q / Cp, tcol = q - (q / Cp) * Cp;
+    const int j = l * C + min(tcol, C - 1);
+    const int hh = j / C2, tc2 = j - (j / C2) * C2;
+    sLut[q] = (uint16_t)((4 * (hh * Wp + (tc2 >> 1))) | ((tc2 & 1) << 15));
+  }
+  const TabGrid g{sRow, sNcnt, A.smemF ? sF : A.P.F};
+  int* const cnt_t = wb + half * TI;  // this lane's task's counters
+  WarpTask* const st_me = reinterpret_cast<WarpTask*>(cnt_t + 16 * Wp);
+  auto st_of = [&](int t) { return reinterpret_cast<WarpTask*>(wb + t * TI + 16 * Wp); };
+  if (lane == 0) {
+    st_of(0)->n32 = 0;
+    st_of(0)->n64 = 0;
+    st_of(0)->npend = 0;
+  }
+  __syncthreads();
+  const uint4* ktab0 = reinterpret_cast<const uint4*>(A.kthr);
+  const int hcap = A.hitcap / 2;  // per task
+  int2* const hbw = A.hitbuf + (size_t)(blockIdx.x * kTableWarps + warp) * A.hitcap;
+  int2* const hb_me = hbw + half * hcap;
+  unsigned long long nfall = 0;
+  const int ntask = A.ntask_dev ? *((volatile const int*)A.ntask_dev) : A.ntask;
+  for (;;) {
+    int b0 = 0;
+    if (lane == 0) b0 = atomicAdd(A.work, 2);
+    b0 = __shfl_sync(kFull, b0, 0);
+    if (b0 >= ntask) break;
+    const bool live = b0 + half < ntask;
+    const int bt_me = live ? (A.task_list ? A.task_list[b0 + half] : b0 + half) : -1;
+    const int* const x32 = reinterpret_cast<const int*>(A.X + (long long)(live ? bt_me : 0) * A.xstride);
+    if (h == 0) {
+      st_me->B = A.tau;
+      st_me->B_valid = 0;
+      st_me->ncand = 0;
+      st_me->nsurv = 0;
+      st_me->nhits = 0;
+      const Best z = best_init();
+      st_me->bp = z.p;
+      st_me->bk = z.k;
+      st_me->bi = z.i;
+      st_me->bj = z.j;
+    }
+    for (int q = h; q < 16 * Wp; q += 16) cnt_t[q] = 0;
+    __syncwarp();
+    // labels as 32-bit words (two each), a row's words prefetched one row
+    // ahead: 16 words (32 labels) per task, and 16 more for rows that long
+    int s = sRow[0], e = sRow[1];
+    int w0, w1;
+    {
+      const int q0 = (s >> 1) + h;
+      w0 = (live && 2 * q0 < e) ? __ldg(x32 + q0) : -1;
+      w1 = (live && 2 * (q0 + 16) < e) ? __ldg(x32 + q0 + 16) : -1;
+    }
+    bool anyhits[2] = {false, false};
+    int cur_tight[2] = {-1, -1};  // the table each task's rows are compared with (uniform)
+    const uint4* ktab_me = ktab0;
+    auto add_lab = [&](int lab) {
+      const uint32_t v = sLut[lab];
+      atomicAdd(reinterpret_cast<uint32_t*>(reinterpret_cast<unsigned char*>(cnt_t) + (v & 0x7FFFu)),
+                1u << ((v >> 11) & 16u));
+    };
+    auto add_word = [&](int w, int q, int rs, int re) {
+      const int p = 2 * q;
+      const int lab0 = (int)(short)(w & 0xffff), lab1 = w >> 16;  // sign-extended labels
+      if (p >= rs && p < re && lab0 >= 0) add_lab(lab0);
+      if (p + 1 >= rs && p + 1 < re && lab1 >= 0) add_lab(lab1);
+    };
+    auto push_hit = [&](int i, int col, int k) {
+      const int pos = atomicAdd(&st_me->nhits, 1);
+      if (pos < hcap) hb_me[pos] = make_int2((i << 16) | (h * C2 + col), k);
+    };
+    for (int i = 0; i < n1; ++i) {
+      const int c0 = w0, c1 = w1;
+      const int sN = e;
+      const int eN = (i + 2 <= n1) ? sRow[i + 2] : e;
+      {
+        const int q0 = (sN >> 1) + h;
+        w0 = (live && 2 * q0 < eN) ? __ldg(x32 + q0) : -1;
+        w1 = -1;
+        if (eN > 2 * (sN >> 1) + 32 && live && 2 * (q0 + 16) < eN) w1 = __ldg(x32 + q0 + 16);
+      }
+      // this row's table chunks, consumed after the labels and the chains
+      uint4 kt[NQ];
+#pragma unroll
+      for (int u = 0; u < NQ; ++u) kt[u] = __ldg(ktab_me + ((size_t)i * NQ + u) * 16 + h);
+      {
+        const int q0 = (s >> 1) + h;
+        add_word(c0, q0, s, e);
+        if (e > 2 * (s >> 1) + 32) {  // a row of more than 32 labels (uniform)
+          add_word(c1, q0 + 16, s, e);
+          if (live)
+            for (int q = q0 + 32; 2 * q < e; q += 16) add_word(__ldg(x32 + q), q, s, e);
+        }
+      }
+      __syncwarp();
+      // in-lane partial overlaps: NG chains of GW words, each from zero
+      uint32_t v[NW];
+      uint32_t Rg[NG];
+#pragma unroll
+      for (int gq = 0; gq < NG; ++gq) Rg[gq] = 0;
+#pragma unroll
+      for (int u = 0; u < NQ; ++u) {
+        const uint4 c4 = *reinterpret_cast<const uint4*>(cnt_t + h * Wp + 4 * u);
+        const uint32_t cv[4] = {c4.x, c4.y, c4.z, c4.w};
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+          const int w = 4 * u + c;
+          if (w < NW) {
+            const int gq = w / GW;
+            v[w] = cv[c] * 0x10001u + Rg[gq];
+            Rg[gq] = __byte_perm(v[w], 0, 0x3232);
+          }
+        }
+      }
+      // offsets of the chains (both halves), the lane's total, the scan
+      uint32_t off[NG];
+      off[0] = 0;
+#pragma unroll
+      for (int gq = 1; gq < NG; ++gq) off[gq] = off[gq - 1] + Rg[gq - 1];
+      const int mine = (int)((off[NG - 1] + Rg[NG - 1]) & 0xFFFFu);
+      int incl = mine;
+#pragma unroll
+      for (int d = 1; d < 16; d <<= 1) {
+        const int y = __shfl_up_sync(kFull, incl, d, 16);
+        if (h >= d) incl += y;
+      }
+      const uint32_t E = (uint32_t)(incl - mine) * 0x10001u;
+      uint32_t Eg[NG];
+#pragma unroll
+      for (int gq = 0; gq < NG; ++gq) Eg[gq] = E + off[gq];
+      uint32_t acc = 0;
+#pragma unroll
+      for (int u = 0; u < NQ; ++u) {
+        const uint32_t tv[4] = {kt[u].x, kt[u].y, kt[u].z, kt[u].w};
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+          const int w = 4 * u + c;
+          if (w < NW) acc |= v[w] + Eg[w / GW] + tv[c];
+        }
+      }
+      if (acc & 0x80008000u) {
+#pragma unroll
+        for (int u = 0; u < NQ; ++u) {
+          const uint32_t tv[4] = {kt[u].x, kt[u].y, kt[u].z, kt[u].w};
+#pragma unroll
+          for (int c = 0; c < 4; ++c) {
+            const int w = 4 * u + c;
+            if (w < NW) {
+              const uint32_t o = v[w] + Eg[w / GW];
+              const uint32_t d = o + tv[c];
+              if (d & 0x8000u) push_hit(i, 2 * w, (int)(o & 0xFFFFu));
+              if (d & 0x80000000u) push_hit(i, 2 * w + 1, (int)(o >> 16));
+            }
+          }
+        }
+      }
+      // the next row's counter updates wait for every lane's reads of this row
+      __syncwarp();
+      // every fourth row: could a task's buffer overflow within the next four
+      // rows, or has it gathered kEarlyHits hits while a tighter table is
+      // left?  Then resolve what it holds; the bound B it sets lets its
+      // remaining rows be compared with the tightest table whose bound is
+      // still >= B (every cell with ln p <= B stays a hit).
+      if ((i & 3) == 3) {
+#pragma unroll
+        for (int t = 0; t < 2; ++t) {
+          const int nh = st_of(t)->nhits;
+          if (nh > hcap - 4 * 16 * C2 || (cur_tight[t] + 1 < A.ntight && nh >= kEarlyHits)) {
+            table_resolve(A, g, hw_warp_mem(wb, C2, t), lane, hbw + t * hcap, min(nh, hcap));
+            anyhits[t] = true;
+            __syncwarp();
+            if (lane == 0) st_of(t)->nhits = 0;
+            if (st_of(t)->B_valid) {
+              const int B = st_of(t)->B;
+              for (int q = A.ntight - 1; q > cur_tight[t]; --q) {
+                if (A.tight_tau[q] >= B) {
+                  cur_tight[t] = q;
+                  break;
+                }
+              }
+            }
+            __syncwarp();
+          }
+        }
+        const int ct = half ? cur_tight[1] : cur_tight[0];
+        ktab_me = ct < 0 ? ktab0 : reinterpret_cast<const uint4*>(A.tight[ct]);
+      }
+      s = sN;
+      e = eN;
+    }
+    __syncwarp();
+#pragma unroll
+    for (int t = 0; t < 2; ++t) {
+      if (b0 + t >= ntask) continue;
+      const int bt = A.task_list ? A.task_list[b0 + t] : b0 + t;
+      const TableWarpMem mt = hw_warp_mem(wb, C2, t);
+      const int nh = min(mt.st->nhits, hcap);
+      if (nh > 0) table_resolve(A, g, mt, lane, hbw + t * hcap, nh);
+      if ((nh > 0 || anyhits[t]) && mt.st->B_valid) {
+        if (isinf(mt.st->bp)) {
+          // no FP64 tail evaluated yet for this task: queue its survivors
+          table_defer(A, g, mt, lane, bt);
+        } else {
+          table_refine(A, g, mt, lane);
+          if (lane == 0) A.out[bt] = TaskResult{mt.st->bp, mt.st->bi, mt.st->bj, mt.st->bk, A.route};
+        }
+      } else {
+        // no cell reaches the guess: the next level (or the exhaustive
+        // screen) takes the task
+        if (lane == 0) A.fallback[atomicAdd(A.nfallback, 1)] = bt;
+        ++nfall;
+      }
+      __syncwarp();
+    }
+  }
+  if (st_of(0)->npend > 0) table_pending_flush(A, g, hw_warp_mem(wb, C2, 0), lane);
+  if (lane == 0 && A.n_refined) {
+    atomicAdd(A.n_refined, st_of(0)->n64);
+    atomicAdd(A.n_refined + 1, st_of(0)->n32);
+    atomicAdd(A.n_refined + 2, nfall);
+  }
+}
+
+template <int C2>
+cudaError_t launch_table_hw_kernel(const TableGridArgs& a, int ctas, size_t smem, cudaStream_t s) {
+  cudaError_t e = raise_smem_limit((const void*)table_hw_kernel<C2>, smem);
+  if (e != cudaSuccess) return e;
+  table_hw_kernel<C2><<<ctas, kTableWarps * 32, smem, s>>>(a);
+  return cudaGetLastError();
+}
+
 template <int C, bool Packed>
 cudaError_t launch_table_grid_kernel(const TableGridArgs& a, int ctas, size_t smem, cudaStream_t s) {
   cudaError_t e = raise_smem_limit((const void*)table_grid_kernel<C, Packed>, smem);
@@ -663,9 +976,11 @@ cudaError_t launch_table_grid_kernel(const TableGridArgs& a, int ctas, size_t sm
   return cudaGetLastError();
 }
 
+// Packed pairs take the half-warp sweep (2 C columns per lane), the others
+// the 32-bit sweep of table_grid_kernel.
 template <int C>
 cudaError_t launch_table_grid_impl(const TableGridArgs& a, int ctas, size_t smem, cudaStream_t s) {
-  return a.packed ? launch_table_grid_kernel<C, true>(a, ctas, smem, s)
+  return a.packed ? launch_table_hw_kernel<2 * C>(a, ctas, smem, s)
                   : launch_table_grid_kernel<C, false>(a, ctas, smem, s);
 }
 

@@ -163,15 +163,27 @@ class Job:
         check(lib().dto_serve_poll(self.server.handle, self._id.value, C.byref(d)))
         return bool(d.value)
 
-    def wait(self):
+    def wait(self, timeout_ms=None):
+        """The request's RunResult.  With timeout_ms, a request not finished
+        in time raises DtoError(DTO_ERR_TIMEOUT) and can be waited for again
+        or cancelled; a cancelled request raises DtoError(DTO_ERR_CANCELLED)."""
         if self._result is None:
             qm, rm = C.c_double(), C.c_double()
-            st = lib().dto_serve_wait(self.server.handle, self._id.value, C.byref(qm), C.byref(rm))
+            if timeout_ms is None:
+                st = lib().dto_serve_wait(self.server.handle, self._id.value, C.byref(qm), C.byref(rm))
+            else:
+                st = lib().dto_serve_wait_for(self.server.handle, self._id.value, float(timeout_ms),
+                                              C.byref(qm), C.byref(rm))
             if st != 0:
                 raise DtoError(st, lib().dto_serve_last_error(self.server.handle).decode())
             self.queue_ms, self.run_ms = qm.value, rm.value
             self._result = RunResult(self._unp.as_dict(), self._minp, None, self._summ.as_dict())
         return self._result
+
+    def cancel(self):
+        """dto_serve_cancel: a queued request leaves the queue; a running one
+        stops at its next batch boundary."""
+        check(lib().dto_serve_cancel(self.server.handle, self._id.value))
 
 
 class RunResult:

@@ -35,9 +35,10 @@ extern "C" {
 #define DTO_OK 0
 #define DTO_ERR_INVALID 1  /* bad arguments; the reference panics in these cases */
 #define DTO_ERR_OOM 2      /* device or host allocation failed */
-#define DTO_ERR_TIMEOUT 3  /* a bounded device wait gave up */
+#define DTO_ERR_TIMEOUT 3  /* a bounded wait (dto_serve_wait_for) ran out first */
 #define DTO_ERR_CUDA 4     /* any other CUDA runtime failure */
 #define DTO_ERR_NOT_FOUND 5
+#define DTO_ERR_CANCELLED 6 /* the request was cancelled (dto_serve_cancel) */
 
 /* Precision of the threshold-pair search. */
 #define DTO_PRECISION_FP64 0   /* plain FP64: the FP64 tail of every cell (drop-in path) */
@@ -262,6 +263,18 @@ DTO_API int dto_serve_poll(dto_server* srv, dto_job job, int* done);
  * queue_ms / run_ms (nullable) get the host wall time from submission to
  * admission and from admission to completion. */
 DTO_API int dto_serve_wait(dto_server* srv, dto_job job, double* queue_ms, double* run_ms);
+/* No counterpart in the reference (its tasks are joined without a limit,
+ * src/run/single_node.rs:131-133).  dto_serve_wait with a limit: a request
+ * not finished within timeout_ms returns DTO_ERR_TIMEOUT and stays known (wait
+ * again, or cancel it). */
+DTO_API int dto_serve_wait_for(dto_server* srv, dto_job job, double timeout_ms, double* queue_ms,
+                               double* run_ms);
+/* No counterpart in the reference.  Cancels a request: a queued one leaves the
+ * queue at once, a running one stops at its next batch boundary once its
+ * kernels in flight have finished (they are not interrupted).  Its wait then
+ * returns DTO_ERR_CANCELLED and its outputs are undefined; a request that had
+ * already finished keeps its results. */
+DTO_API int dto_serve_cancel(dto_server* srv, dto_job job);
 DTO_API const char* dto_serve_last_error(dto_server* srv);
 DTO_API int dto_serve_stats(dto_server* srv, int64_t* queued, int64_t* running, int64_t* completed,
                             int64_t* reserved_bytes);

@@ -93,3 +93,40 @@ def test_memory_admission_and_errors(engine):
         assert np.array_equal(r.minp, dp.run(5000, seed=s).minp)
     assert np.array_equal(rb.minp, dp.run(20000, seed=4).minp)
     dp.close()
+
+
+def test_bounded_wait_and_cancel(engine):
+    # A one-lane server: a long request runs while a short one waits behind it.
+    # A wait with a 1 ms limit on the queued request gives up (DTO_ERR_TIMEOUT)
+    # and leaves it known; cancelling it takes it out of the queue
+    # (DTO_ERR_CANCELLED).  Cancelling the running request stops it at a batch
+    # boundary, its kernels drained (or it had finished: its results stand).
+    # The server then serves a new request with the same results as a run
+    # alone.  Nothing here interrupts a kernel.
+    from dual_threshold_optimization_gb300._lib import DTO_ERR_CANCELLED, DTO_ERR_TIMEOUT
+    big = synth.copula_pair(20000, 0.2, seed=2)
+    dbig = engine.pair(big.ranks1, big.feat1, big.ranks2, big.feat2, big.n_features, big.population)
+    p = synth.copula_pair(3000, 0.2, seed=5)
+    dp = engine.pair(p.ranks1, p.feat1, p.ranks2, p.feat2, p.n_features, p.population)
+    want = dp.run(3000, seed=9).minp
+    with engine.server(lanes=1) as srv:
+        running = srv.submit(dbig, 400_000, seed=1)
+        queued = srv.submit(dp, 3000, seed=9)
+        with pytest.raises(DtoError) as e:
+            queued.wait(timeout_ms=1.0)
+        assert e.value.status == DTO_ERR_TIMEOUT
+        assert srv.stats()["queued"] + srv.stats()["running"] >= 1
+        queued.cancel()
+        with pytest.raises(DtoError) as e:
+            queued.wait()
+        assert e.value.status == DTO_ERR_CANCELLED
+        running.cancel()
+        try:
+            running.wait()
+        except DtoError as err:
+            assert err.status == DTO_ERR_CANCELLED
+        again = srv.submit(dp, 3000, seed=9)
+        assert np.array_equal(again.wait(timeout_ms=60_000).minp, want)
+        assert srv.stats()["queued"] == 0 and srv.stats()["running"] == 0
+    dbig.close()
+    dp.close()
