@@ -152,8 +152,12 @@ struct TabGrid {
   const uint32_t* F;
 };
 
+// The resolve helpers below are inlined into the sweeps: as calls they made
+// the kernel copy its arguments and per-task pointers to local memory and
+// save live registers around every call (spills in the row loop).
+
 // Stage 3 on the survivors the current B admits.
-static __device__ __noinline__ void table_refine(const TableGridArgs& A, const TabGrid& g, const TableWarpMem& m,
+static __device__ __forceinline__ void table_refine(const TableGridArgs& A, const TabGrid& g, const TableWarpMem& m,
                                           int lane) {
   __syncwarp();
   WarpTask st = *m.st;
@@ -187,7 +191,7 @@ static __device__ __noinline__ void table_refine(const TableGridArgs& A, const T
 // the reference's tie-break and writes its result.  Tasks share the FP64
 // instructions this way: on GB300 an FP64 warp instruction costs the same
 // whether one lane or all 32 are active.
-static __device__ __noinline__ void table_pending_flush(const TableGridArgs& A, const TabGrid& g,
+static __device__ __forceinline__ void table_pending_flush(const TableGridArgs& A, const TabGrid& g,
                                                         const TableWarpMem& m, int lane) {
   __syncwarp();
   const int np = m.q->npend;
@@ -215,7 +219,7 @@ static __device__ __noinline__ void table_pending_flush(const TableGridArgs& A, 
 
 // Queue the task's survivors that the final B admits, without duplicates
 // (a cell can reach stage 2 twice: as a seed and as a hit).
-static __device__ __noinline__ void table_defer(const TableGridArgs& A, const TabGrid& g, const TableWarpMem& m,
+static __device__ __forceinline__ void table_defer(const TableGridArgs& A, const TabGrid& g, const TableWarpMem& m,
                                                 int lane, int task) {
   __syncwarp();
   const int B = m.st->B;
@@ -251,7 +255,7 @@ static __device__ __noinline__ void table_defer(const TableGridArgs& A, const Ta
 }
 
 // Stage 2 on the candidate buffer.
-static __device__ __noinline__ void table_flush(const TableGridArgs& A, const TabGrid& g, const TableWarpMem& m,
+static __device__ __forceinline__ void table_flush(const TableGridArgs& A, const TabGrid& g, const TableWarpMem& m,
                                          int lane) {
   __syncwarp();
   const int N = (int)A.P.Npop;
@@ -321,7 +325,7 @@ __device__ __forceinline__ int cell_lb(const uint32_t* F, int N, uint32_t FN, in
 // partial-sum filter) in batches, B tightening as it goes.  The claim of
 // dto_grid.cuh applies unchanged: the FP64 argmin is among the hits and is
 // never filtered out.
-static __device__ __noinline__ void table_resolve(const TableGridArgs& A, const TabGrid& g,
+static __device__ __forceinline__ void table_resolve(const TableGridArgs& A, const TabGrid& g,
                                                   const TableWarpMem& m, int lane, const int2* hb, int nh) {
   const int N = (int)A.P.Npop;
   const uint32_t* F = g.F;
@@ -369,6 +373,15 @@ static __device__ __noinline__ void table_resolve(const TableGridArgs& A, const 
     }
   }
   if (m.st->ncand > 0) table_flush(A, g, m, lane);
+}
+
+// The tighter tables of the arguments, by selects (a dynamic index into the
+// kernel's argument arrays would copy the arguments to local memory).
+__device__ __forceinline__ const uint16_t* tight_of(const TableGridArgs& A, int q) {
+  return q == 0 ? A.tight[0] : q == 1 ? A.tight[1] : A.tight[2];
+}
+__device__ __forceinline__ int tight_tau_of(const TableGridArgs& A, int q) {
+  return q == 0 ? A.tight_tau[0] : q == 1 ? A.tight_tau[1] : A.tight_tau[2];
 }
 
 template <int C, bool Packed>
@@ -612,9 +625,9 @@ __global__ void __launch_bounds__(kTableWarps * 32, kTableCtasPerSm) table_grid_
             if (T == 1 && st_of(t)->B_valid) {
               const int B = st_of(t)->B;
               for (int q = A.ntight - 1; q > cur_tight; --q) {
-                if (A.tight_tau[q] >= B) {
+                if (tight_tau_of(A, q) >= B) {
                   cur_tight = q;
-                  ktab_cur = reinterpret_cast<const uint4*>(A.tight[q]);
+                  ktab_cur = reinterpret_cast<const uint4*>(tight_of(A, q));
                   break;
                 }
               }
@@ -912,7 +925,7 @@ __global__ void __launch_bounds__(kTableWarps * 32, 1) table_hw_kernel(const Tab
             if (st_of(t)->B_valid) {
               const int B = st_of(t)->B;
               for (int q = A.ntight - 1; q > cur_tight[t]; --q) {
-                if (A.tight_tau[q] >= B) {
+                if (tight_tau_of(A, q) >= B) {
                   cur_tight[t] = q;
                   break;
                 }
@@ -922,7 +935,7 @@ __global__ void __launch_bounds__(kTableWarps * 32, 1) table_hw_kernel(const Tab
           }
         }
         const int ct = half ? cur_tight[1] : cur_tight[0];
-        ktab_me = ct < 0 ? ktab0 : reinterpret_cast<const uint4*>(A.tight[ct]);
+        ktab_me = ct < 0 ? ktab0 : reinterpret_cast<const uint4*>(tight_of(A, ct));
       }
       s = sN;
       e = eN;
