@@ -10,30 +10,20 @@ namespace dto {
 #endif
 constexpr int kGridWarps = DTO_GRID_WARPS;  // warps per CTA of the grid kernel (one task per warp)
 constexpr int kCandCap = 64;         // per-warp candidate buffer of the screen
-#ifndef DTO_BUCKET_BITS
-#define DTO_BUCKET_BITS 12
-#endif
-constexpr int kBucketBits = DTO_BUCKET_BITS;
+constexpr int kBucketBits = 12;
 constexpr int kBuckets = 1 << kBucketBits;  // Rao-Sandelius buckets
 static_assert(kBuckets % 1024 == 0, "perm_kernel: buckets must split evenly over its warps");
-// Longest list whose Philox words the permutation kernel may keep in shared
-// memory (4 + 2 bytes an element + the counters: 208 KB at 32,768).
-#ifndef DTO_PERM_WORDS_MAXL
-#define DTO_PERM_WORDS_MAXL 32768
-#endif
-constexpr int kPermWordsMaxL = DTO_PERM_WORDS_MAXL;
-// Shared-memory budget of one permutation CTA.  The label table Ylab is
-// staged there (random 2-byte gathers hit shared-memory banks instead of L1
-// sectors) when it fits beside the counters, the words and the indices.
-constexpr size_t kPermSmemBudget = 226 * 1024;  // 227 KB per block, less the static arrays
+// Shared-memory budget of one permutation CTA (227 KB per block, less the
+// static arrays).
+constexpr size_t kPermSmemBudget = 226 * 1024;
 __host__ __device__ constexpr size_t perm_round16(size_t b) { return (b + 15) & ~(size_t)15; }
-// counters | indices | words (when kept); every region starts on a 16-byte
-// boundary, the staged labels follow
-__host__ __device__ constexpr size_t perm_base_smem(int L, bool words) {
-  return (size_t)kBuckets * 4 + perm_round16((size_t)L * 2) + (words ? perm_round16((size_t)L * 4) : 0);
+// counters | indices; each region starts on a 16-byte boundary, the bucket /
+// label area (L int16) follows where it fits
+__host__ __device__ constexpr size_t perm_base_smem(int L) {
+  return (size_t)kBuckets * 4 + perm_round16((size_t)L * 2);
 }
-__host__ __device__ constexpr bool perm_stage_ylab(int L, bool words) {
-  return perm_base_smem(L, words) + perm_round16((size_t)L * 2) <= kPermSmemBudget;
+__host__ __device__ constexpr bool perm_stage_area(int L) {
+  return perm_base_smem(L) + perm_round16((size_t)L * 2) <= kPermSmemBudget;
 }
 constexpr int kMaxListLen = 65534;   // positions are uint16; overlaps stay below the 0xFFFF "never" mark
 constexpr int kScreenSlack = 5;      // fixed-point units added to the screen threshold
@@ -110,9 +100,8 @@ struct PermArgs {
   // (nullable: every bucket shuffled as the specification says).
   const int* rowstart;
   int n1;
-  // set by launch_perm: the words are kept in shared memory / the labels
-  // staged there
-  int words, stage;
+  // set by launch_perm: the bucket / label area fits in shared memory
+  int stage;
 };
 
 struct ComposeArgs {

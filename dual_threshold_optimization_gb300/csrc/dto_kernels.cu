@@ -5,19 +5,17 @@
 // (src/collections/permuted.rs:56-60: a uniform shuffle of 0..len with
 // rand's thread_rng).  Here a permutation is a deterministic function of
 // (seed, pair id, permutation id, list tag):
-//   1. every element e draws one Philox4x32-10 word W[e] (counter
-//      (e/4, perm, pair, 0x10000000 | tag<<24), word e%4, key = the two
-//      halves of the seed); its top 12 bits pick a bucket in [0, 4096);
+//   1. element e draws a bucket in [0, 4096): the top 12 bits of the low
+//      (e even) or high (e odd) 16-bit half of word (e/2) % 4 of the
+//      Philox4x32-10 block at counter (e/8, perm, pair, 0x10000000 | tag<<24)
+//      (key = the two halves of the seed): eight elements per block;
 //   2. elements are grouped by bucket, in increasing element order inside a
 //      bucket;
 //   3. each bucket is shuffled by the forward Fisher-Yates pass (i = 1..sz-1:
-//      swap positions i and j, j uniform in [0, i]).  Draw i uses the low 20
-//      bits r of W of the element at position i (untouched before step i, so
-//      r is independent of everything drawn before): j = (r (i+1)) >> 20,
-//      unless the low 20 bits of r (i+1) fall below 2^20 mod (i+1), in which
-//      case j comes from the bucket's own Philox stream (counter (call, perm,
-//      pair, 0x20000000 | tag<<24 | bucket)) by Lemire's multiply-shift with
-//      rejection.  Both are exactly uniform.
+//      swap positions i and j, j uniform in [0, i]), the draws taken from the
+//      bucket's own Philox stream (counter (call, perm, pair,
+//      0x20000000 | tag<<24 | bucket), the four words of each call in order)
+//      by Lemire's multiply-shift with rejection.
 // One level of Rao-Sandelius bucketing followed by uniform shuffles of the
 // buckets gives an exactly uniform permutation.
 #include <algorithm>
@@ -65,15 +63,14 @@ struct PhiloxStream {
 
 // One CTA per permutation.  Shared memory: the bucket counters (int32,
 // kBuckets; after the scatter they hold each bucket's end), the shuffled
-// element indices (uint16, L), where the launch keeps them every element's
-// Philox word (uint32, L: the scatter and the shuffle draws reuse the words
-// of the counting pass; otherwise a shuffle draw recomputes its word), and
-// where it fits the label table (int16, L).  kBuckets = 4096 keeps buckets
-// at a few elements for the list lengths of interest, so the per-bucket
-// canonical sort and Fisher-Yates are a few operations per element.
-template <bool kWords, int kPermThreads>
-__device__ __forceinline__ void perm_body(const PermArgs& A, int* cnt, uint16_t* sA, uint32_t* sW,
-                                          int16_t* sY) {
+// element indices (uint16, L) and, where it fits, an area of L int16 that
+// first holds each element's bucket (so that the scatter and the row starts
+// need not redraw the Philox blocks) and then the staged label table.
+// kBuckets = 4096 keeps buckets at a few elements for the list lengths of
+// interest, so the per-bucket canonical sort and Fisher-Yates pass are a few
+// operations per element.
+template <int kPermThreads>
+__device__ __forceinline__ void perm_body(const PermArgs& A, int* cnt, uint16_t* sA, int16_t* sY) {
   __shared__ int warpTot[kPermThreads / 32];
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int L = A.L;
@@ -81,27 +78,29 @@ __device__ __forceinline__ void perm_body(const PermArgs& A, int* cnt, uint16_t*
   const uint32_t k0 = (uint32_t)A.seed, k1 = (uint32_t)(A.seed >> 32);
   const uint32_t tagB = 0x10000000u | (A.list_tag << 24);
   constexpr int kPerWarp = kBuckets / (kPermThreads / 32);
-  constexpr int kLowBits = 32 - kBucketBits;
-  constexpr uint32_t kLowMask = (1u << kLowBits) - 1u;
-  auto word_of = [&](int e) -> uint32_t {
-    if (kWords) return sW[e];
-    const uint4 w = philox4x32_10(make_uint4((uint32_t)(e >> 2), perm, A.pair_id, tagB), k0, k1);
-    const int q = e & 3;
-    return (q == 0) ? w.x : (q == 1) ? w.y : (q == 2) ? w.z : w.w;
+  static_assert(kBucketBits == 12, "buckets are the top 12 bits of a 16-bit half");
+  auto bucket_in = [](const uint4& w, int e) -> int {
+    const int q = (e >> 1) & 3;
+    const uint32_t word = q == 0 ? w.x : q == 1 ? w.y : q == 2 ? w.z : w.w;
+    return (int)((e & 1) ? (word >> 20) : ((word >> 4) & 0xFFFu));
+  };
+  auto bucket_of = [&](int e) -> int {  // redrawn from its Philox block
+    return bucket_in(philox4x32_10(make_uint4((uint32_t)(e >> 3), perm, A.pair_id, tagB), k0, k1), e);
   };
 
   for (int b = tid; b < kBuckets; b += kPermThreads) cnt[b] = 0;
   const bool rows = A.X && A.rowstart;
   // The label table goes to shared memory by asynchronous 16-byte copies
-  // (waited for before the gather).  Without kept words, the label area
-  // first holds each element's bucket (uint16), so that the scatter need not
-  // redraw the words; the copies then start once the row starts have found
-  // their buckets, and land during the shuffles.  (Up to two row starts a
-  // thread: longer grids redraw.)
+  // (waited for before the gather).  The label area first holds each
+  // element's bucket (uint16), so that the scatter need not redraw the
+  // blocks; the copies start once the row starts have found their buckets,
+  // and land during the shuffles.  (Up to two row starts a thread: longer
+  // grids redraw.)
   const bool asyncY = sY && (reinterpret_cast<uintptr_t>(A.Ylab) & 15) == 0;
-  const bool ids = !kWords && sY && (!rows || A.n1 + 1 <= 2 * kPermThreads);
+  const bool ids = sY && (!rows || A.n1 + 1 <= 2 * kPermThreads);
   uint16_t* sId = reinterpret_cast<uint16_t*>(sY);
   auto stage_labels = [&]() {
+    if (!A.X) return;
     if (asyncY) {
       const char* src = reinterpret_cast<const char*>(A.Ylab);
       const uint32_t dst = (uint32_t)__cvta_generic_to_shared(sY);
@@ -125,16 +124,18 @@ __device__ __forceinline__ void perm_body(const PermArgs& A, int* cnt, uint16_t*
   const int rsPrev1 = (rows && r1 <= A.n1) ? __ldg(A.rowstart + r1 - 1) : 0;
   const int rs1 = (rows && r1 <= A.n1) ? __ldg(A.rowstart + r1) : 0;
   __syncthreads();
-  const int groups = (L + 3) >> 2;
+  // counting: one Philox block per eight elements
+  const int groups = (L + 7) >> 3;
   for (int g = tid; g < groups; g += kPermThreads) {
-    uint4 w = philox4x32_10(make_uint4((uint32_t)g, perm, A.pair_id, tagB), k0, k1);
+    const uint4 w = philox4x32_10(make_uint4((uint32_t)g, perm, A.pair_id, tagB), k0, k1);
     const uint32_t wv[4] = {w.x, w.y, w.z, w.w};
 #pragma unroll
-    for (int q = 0; q < 4; ++q) {
-      if (4 * g + q < L) {
-        if (kWords) sW[4 * g + q] = wv[q];
-        if (ids) sId[4 * g + q] = (uint16_t)(wv[q] >> kLowBits);
-        atomicAdd(&cnt[wv[q] >> kLowBits], 1);
+    for (int q = 0; q < 8; ++q) {
+      const int e = 8 * g + q;
+      if (e < L) {
+        const int b = (int)((q & 1) ? (wv[q >> 1] >> 20) : ((wv[q >> 1] >> 4) & 0xFFFu));
+        if (ids) sId[e] = (uint16_t)b;
+        atomicAdd(&cnt[b], 1);
       }
     }
   }
@@ -174,25 +175,19 @@ __device__ __forceinline__ void perm_body(const PermArgs& A, int* cnt, uint16_t*
     for (int r = 0; r < kPerWarp; r += 32) cnt[warp * kPerWarp + r + lane] += off;
   }
   __syncthreads();
-  if (kWords) {
-    for (int e = tid; e < L; e += kPermThreads) {
-      const int pos = atomicAdd(&cnt[sW[e] >> kLowBits], 1);
-      sA[pos] = (uint16_t)e;
-    }
-  } else if (ids) {
+  if (ids) {
     for (int e = tid; e < L; e += kPermThreads) {
       const int pos = atomicAdd(&cnt[sId[e]], 1);
       sA[pos] = (uint16_t)e;
     }
   } else {
     for (int g = tid; g < groups; g += kPermThreads) {
-      uint4 w = philox4x32_10(make_uint4((uint32_t)g, perm, A.pair_id, tagB), k0, k1);
-      const uint32_t wv[4] = {w.x, w.y, w.z, w.w};
+      const uint4 w = philox4x32_10(make_uint4((uint32_t)g, perm, A.pair_id, tagB), k0, k1);
 #pragma unroll
-      for (int q = 0; q < 4; ++q) {
-        const int e = 4 * g + q;
+      for (int q = 0; q < 8; ++q) {
+        const int e = 8 * g + q;
         if (e < L) {
-          const int pos = atomicAdd(&cnt[wv[q] >> kLowBits], 1);
+          const int pos = atomicAdd(&cnt[bucket_in(w, e)], 1);
           sA[pos] = (uint16_t)e;
         }
       }
@@ -200,7 +195,8 @@ __device__ __forceinline__ void perm_body(const PermArgs& A, int* cnt, uint16_t*
   }
   __syncthreads();
   // cnt[b] now holds the end of bucket b.  Canonical (increasing) order
-  // inside bucket b, then the forward Fisher-Yates pass.
+  // inside bucket b, then the forward Fisher-Yates pass from the bucket's
+  // own stream.
   auto shuffle_bucket = [&](int b, int s0, int sz) {
     uint16_t* a = sA + s0;
     for (int i = 1; i < sz; ++i) {
@@ -218,11 +214,7 @@ __device__ __forceinline__ void perm_body(const PermArgs& A, int* cnt, uint16_t*
     st.k1 = k1;
     st.used = 4;
     for (int i = 1; i < sz; ++i) {
-      const uint32_t n = (uint32_t)(i + 1);
-      const unsigned long long m = (unsigned long long)(word_of(a[i]) & kLowMask) * n;
-      uint32_t j = (uint32_t)(m >> kLowBits);
-      const uint32_t l = (uint32_t)m & kLowMask;
-      if (l < n && l < (kLowMask + 1u) % n) j = st.bounded(n);
+      const uint32_t j = st.bounded((uint32_t)(i + 1));
       const uint16_t tmp = a[i];
       a[i] = a[j];
       a[j] = tmp;
@@ -240,7 +232,7 @@ __device__ __forceinline__ void perm_body(const PermArgs& A, int* cnt, uint16_t*
     auto claim = [&](int r, int u) -> int2 {
       const int p = u == 0 ? rs0 : u == 1 ? rs1 : __ldg(A.rowstart + r);
       if (p <= 0 || p >= L) return make_int2(-1, 0);
-      const int lo = ids ? (int)sId[sA[p]] : (int)(word_of(sA[p]) >> kLowBits);
+      const int lo = ids ? (int)sId[sA[p]] : bucket_of(sA[p]);
       const int s0 = lo == 0 ? 0 : cnt[lo - 1];
       if (s0 >= p) return make_int2(-1, 0);  // p starts the bucket
       const int prev = u == 0 ? rsPrev0 : u == 1 ? rsPrev1 : __ldg(A.rowstart + r - 1);
@@ -260,14 +252,17 @@ __device__ __forceinline__ void perm_body(const PermArgs& A, int* cnt, uint16_t*
       if (c.x >= 0) shuffle_bucket(c.x, c.y, cnt[c.x] - c.y);
     }
   } else {
-    if (ids) stage_labels();
+    if (ids) {
+      __syncthreads();  // every scatter has read the buckets
+      stage_labels();
+    }
     for (int b = tid; b < kBuckets; b += kPermThreads) {
       const int s0 = b == 0 ? 0 : cnt[b - 1];
       const int sz = cnt[b] - s0;
       if (sz >= 2) shuffle_bucket(b, s0, sz);
     }
   }
-  if (asyncY) asm volatile("cp.async.wait_all;\n" ::: "memory");
+  if (asyncY && A.X) asm volatile("cp.async.wait_all;\n" ::: "memory");
   __syncthreads();
   if (A.X) {
     int16_t* xo = A.X + (long long)blockIdx.x * A.xstride;
@@ -305,13 +300,8 @@ __global__ void __launch_bounds__(kPermThreads) perm_kernel(const PermArgs A) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   int* cnt = reinterpret_cast<int*>(smem_raw);
   uint16_t* sA = reinterpret_cast<uint16_t*>(cnt + kBuckets);
-  int16_t* sY = A.stage ? reinterpret_cast<int16_t*>(smem_raw + perm_base_smem(A.L, A.words)) : nullptr;
-  if (A.words) {
-    uint32_t* sW = reinterpret_cast<uint32_t*>(reinterpret_cast<unsigned char*>(sA) + perm_round16((size_t)A.L * 2));
-    perm_body<true, kPermThreads>(A, cnt, sA, sW, sY);
-  } else {
-    perm_body<false, kPermThreads>(A, cnt, sA, nullptr, sY);
-  }
+  int16_t* sY = A.stage ? reinterpret_cast<int16_t*>(smem_raw + perm_base_smem(A.L)) : nullptr;
+  perm_body<kPermThreads>(A, cnt, sA, sY);
 }
 
 // X[p1] = label of the list-2 position holding the feature at list-1 position
@@ -410,43 +400,20 @@ cudaError_t raise_smem_limit(const void* kernel, size_t bytes) {
   return e;
 }
 
-// Shared-memory layout of a permutation launch.  Keeping the words saves
-// recomputing a Philox block per element in the scatter pass; dropping them
-// is worth it only where that lets a second CTA share the SM (the phases of
-// one CTA, separated by barriers, then overlap with the other's).  `ctas`
-// gives the resident CTAs per SM for a dynamic shared-memory size.
-template <class Ctas>
-void perm_layout(int L, bool labels, Ctas ctas, int* words, int* stage, size_t* smem) {
-  auto bytes = [&](bool w, bool* st) {
-    *st = labels && perm_stage_ylab(L, w);
-    return perm_base_smem(L, w) + (*st ? perm_round16((size_t)L * 2) : 0);
-  };
-  bool stW = false, stN = false;
-  const size_t bW = bytes(true, &stW), bN = bytes(false, &stN);
-  const bool keep = L <= kPermWordsMaxL && (ctas(bW) >= 2 || ctas(bN) < 2);
-  *words = keep ? 1 : 0;
-  *stage = (keep ? stW : stN) ? 1 : 0;
-  *smem = keep ? bW : bN;
-}
-
+// Shared memory of a permutation launch: the counters and the indices, and
+// the bucket / label area where it fits.  CTAs of 512 threads, two to an SM
+// where the shared memory allows; where only one fits, CTAs of 1024 threads
+// keep the SM's warps busy.
 cudaError_t launch_perm(const PermArgs& a0, int count, cudaStream_t s) {
   if (count <= 0) return cudaSuccess;
   PermArgs a = a0;
-  size_t smem = 0;
-  cudaError_t e = cudaSuccess;
-  // CTAs of 512 threads, two to an SM where the shared memory allows; where
-  // only one fits, CTAs of 1024 threads keep the SM's warps busy
-  auto ctas = [&](size_t bytes) {
-    int n = 0;
-    if (e == cudaSuccess) e = raise_smem_limit((const void*)perm_kernel<512>, bytes);
-    if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, perm_kernel<512>, 512, bytes);
-    return n;
-  };
-  perm_layout(a.L, a.X != nullptr, ctas, &a.words, &a.stage, &smem);
+  a.stage = perm_stage_area(a.L) ? 1 : 0;
+  const size_t smem = perm_base_smem(a.L) + (a.stage ? perm_round16((size_t)a.L * 2) : 0);
+  cudaError_t e = raise_smem_limit((const void*)perm_kernel<512>, smem);
+  int n = 0;
+  if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, perm_kernel<512>, 512, smem);
   if (e != cudaSuccess) return e;
-  const bool pairs = ctas(smem) >= 2;
-  if (e != cudaSuccess) return e;
-  if (pairs) {
+  if (n >= 2) {
     perm_kernel<512><<<count, 512, smem, s>>>(a);
   } else {
     e = raise_smem_limit((const void*)perm_kernel<1024>, smem);

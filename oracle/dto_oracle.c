@@ -414,9 +414,10 @@ OR_EXPORT double or_empirical(double p_obs, const double* p_perm, int64_t n_perm
 /* Philox4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11) and the permutation       */
 /* specification used by the GPU's on-device permutations:                     */
 /*   one level of Rao-Sandelius bucketing (4096 buckets, bucket = top 12 bits  */
-/*   of one Philox word per element), elements in each bucket kept in index    */
-/*   order, then a Fisher-Yates shuffle of each bucket with Lemire's unbiased  */
-/*   bounded integers.  The result is an exactly uniform permutation.          */
+/*   of one 16-bit half of a Philox word per element), elements in each bucket */
+/*   kept in index order, then a Fisher-Yates shuffle of each bucket from its  */
+/*   own Philox stream with Lemire's unbiased bounded integers.  The result is */
+/*   an exactly uniform permutation.                                           */
 /* ------------------------------------------------------------------------- */
 OR_EXPORT void or_philox4x32_10(const uint32_t* ctr_in, const uint32_t* key_in, uint32_t* out) {
     uint32_t c0 = ctr_in[0], c1 = ctr_in[1], c2 = ctr_in[2], c3 = ctr_in[3];
@@ -467,31 +468,38 @@ static uint32_t bounded(or_stream_t* s, uint32_t range) {
     return (uint32_t)(m >> 32);
 }
 
+/* The bucket of element e: the low (e even) or high (e odd) 16 bits of word
+ * (e / 2) % 4 of the Philox block at counter (e / 8, perm, pair,
+ * 0x10000000 | tag<<24), and of those 16 bits the top 12. */
+static uint32_t bucket_of(const uint32_t w[4], int32_t e) {
+    const uint32_t word = w[(e >> 1) & 3];
+    return (e & 1) ? (word >> 20) : ((word >> 4) & 0xFFFu);
+}
+
 /* sigma[p] for p in [0, L): the index placed at position p.
- * Element e draws one Philox word W[e] (counter (e/4, perm, pair,
- * 0x10000000 | tag<<24), word e%4).  Its top 12 bits pick a bucket; elements
- * are grouped by bucket in increasing e.  Each bucket is then shuffled by the
- * forward Fisher-Yates pass (i = 1..sz-1: swap positions i and j, j uniform in
- * [0, i]); draw i takes the low 20 bits r of W of the element at position i
- * (that position is untouched before step i), j = (r (i+1)) >> 20 unless the
- * low 20 bits of r (i+1) fall below 2^20 mod (i+1) (Lemire's rejection), in
- * which case j comes from the bucket's own Philox stream (counter (call, perm,
- * pair, 0x20000000 | tag<<24 | bucket)) by 32-bit Lemire with rejection. */
+ * Every element draws a bucket in [0, 4096) (bucket_of); elements are grouped
+ * by bucket in increasing e.  Each bucket is then shuffled by the forward
+ * Fisher-Yates pass (i = 1..sz-1: swap positions i and j, j uniform in
+ * [0, i]) whose draws come from the bucket's own Philox stream (counter
+ * (call, perm, pair, 0x20000000 | tag<<24 | bucket), the four words of each
+ * call in order) by Lemire's multiply-shift with rejection.  Independent
+ * uniform buckets followed by uniform shuffles of the buckets give an exactly
+ * uniform permutation (one level of Rao-Sandelius). */
 OR_EXPORT void or_shuffle(uint64_t seed, uint32_t pair_id, uint32_t perm_id, uint32_t list_tag, int32_t L, int32_t* sigma) {
     uint32_t key[2] = {(uint32_t)seed, (uint32_t)(seed >> 32)};
-    uint32_t* word = (uint32_t*)malloc((size_t)(L > 0 ? L : 1) * 4);
+    uint32_t* bucket = (uint32_t*)malloc((size_t)(L > 0 ? L : 1) * 4);
     int64_t* cnt = (int64_t*)calloc(OR_NBUCKET + 1, sizeof(int64_t));
     int64_t* fill = (int64_t*)malloc(OR_NBUCKET * sizeof(int64_t));
     for (int32_t e = 0; e < L; ++e) {
-        uint32_t ctr[4] = {(uint32_t)e >> 2, perm_id, pair_id, 0x10000000u | (list_tag << 24)};
+        uint32_t ctr[4] = {(uint32_t)e >> 3, perm_id, pair_id, 0x10000000u | (list_tag << 24)};
         uint32_t w[4];
         or_philox4x32_10(ctr, key, w);
-        word[e] = w[e & 3];
-        cnt[(word[e] >> 20) + 1] += 1;
+        bucket[e] = bucket_of(w, e);
+        cnt[bucket[e] + 1] += 1;
     }
     for (int b = 0; b < OR_NBUCKET; ++b) cnt[b + 1] += cnt[b];
     for (int b = 0; b < OR_NBUCKET; ++b) fill[b] = cnt[b];
-    for (int32_t e = 0; e < L; ++e) sigma[fill[word[e] >> 20]++] = e;
+    for (int32_t e = 0; e < L; ++e) sigma[fill[bucket[e]]++] = e;
     for (int b = 0; b < OR_NBUCKET; ++b) {
         int64_t s0 = cnt[b], sz = cnt[b + 1] - cnt[b];
         or_stream_t st;
@@ -500,16 +508,13 @@ OR_EXPORT void or_shuffle(uint64_t seed, uint32_t pair_id, uint32_t perm_id, uin
         st.ctr[3] = 0x20000000u | (list_tag << 24) | (uint32_t)b;
         st.used = 4;
         for (int64_t i = 1; i < sz; ++i) {
-            const uint32_t n = (uint32_t)(i + 1);
-            const uint64_t m = (uint64_t)(word[sigma[s0 + i]] & 0xFFFFFu) * n;
-            uint32_t j = (uint32_t)(m >> 20);
-            if ((uint32_t)(m & 0xFFFFFu) < (0x100000u % n)) j = bounded(&st, n);
+            const uint32_t j = bounded(&st, (uint32_t)(i + 1));
             int32_t tmp = sigma[s0 + i];
             sigma[s0 + i] = sigma[s0 + j];
             sigma[s0 + j] = tmp;
         }
     }
-    free(word);
+    free(bucket);
     free(cnt);
     free(fill);
 }

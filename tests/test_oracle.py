@@ -213,20 +213,21 @@ def test_shuffle_position_marginals():
 
 def test_shuffle_within_bucket_orders_are_uniform():
     # Lists long enough that buckets hold several elements: recompute each
-    # element's Philox word and bucket, and check that every bucket of size 3
-    # comes out in each of its 6 orders equally often (the forward
-    # Fisher-Yates pass on the words' low 20 bits) and every bucket of size 2
-    # swapped half the time.
+    # element's bucket from the Philox blocks (8 elements a block, a 16-bit
+    # half each, its top 12 bits), check that every bucket holds exactly its
+    # elements, and that every bucket of size 3 comes out in each of its 6
+    # orders equally often (the Fisher-Yates pass on the bucket's own stream)
+    # and every bucket of size 2 swapped half the time.
     L, n = 12288, 40
     seed, pair, tag = 77, 0, 1
-    words = np.zeros(L, np.uint32)
+    bucket = np.zeros(L, np.uint32)
     c3 = {}
     swaps2 = tot2 = 0
     for t in range(1, n + 1):
-        for g in range((L + 3) // 4):
+        for g in range((L + 7) // 8):
             w = O.philox4x32_10([g, t, pair, 0x10000000 | (tag << 24)], [seed & 0xFFFFFFFF, seed >> 32])
-            words[4 * g:4 * g + 4] = w[:min(4, L - 4 * g)]
-        bucket = words >> 20
+            halves = np.array([(x >> (16 * h)) & 0xFFFF for x in w for h in (0, 1)], np.uint32)
+            bucket[8 * g:8 * g + 8] = (halves >> 4)[:min(8, L - 8 * g)]
         s = O.shuffle(seed, pair, t, tag, L)
         starts = np.searchsorted(np.sort(bucket), np.arange(4097))
         for b in range(4096):
