@@ -124,19 +124,21 @@ __device__ __forceinline__ void perm_body(const PermArgs& A, int* cnt, uint16_t*
   const int rsPrev1 = (rows && r1 <= A.n1) ? __ldg(A.rowstart + r1 - 1) : 0;
   const int rs1 = (rows && r1 <= A.n1) ? __ldg(A.rowstart + r1) : 0;
   __syncthreads();
-  // counting: one Philox block per eight elements
+  // counting: one Philox block per eight elements; their eight buckets go to
+  // the bucket area as one 16-byte store (the area is a whole number of
+  // 16-byte chunks, so the padding past L takes the last group's spare ids)
   const int groups = (L + 7) >> 3;
   for (int g = tid; g < groups; g += kPermThreads) {
     const uint4 w = philox4x32_10(make_uint4((uint32_t)g, perm, A.pair_id, tagB), k0, k1);
     const uint32_t wv[4] = {w.x, w.y, w.z, w.w};
+    uint32_t packed[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) packed[q] = ((wv[q] >> 4) & 0xFFFu) | ((wv[q] >> 20) << 16);
+    if (ids) reinterpret_cast<uint4*>(sId)[g] = make_uint4(packed[0], packed[1], packed[2], packed[3]);
 #pragma unroll
     for (int q = 0; q < 8; ++q) {
       const int e = 8 * g + q;
-      if (e < L) {
-        const int b = (int)((q & 1) ? (wv[q >> 1] >> 20) : ((wv[q >> 1] >> 4) & 0xFFFu));
-        if (ids) sId[e] = (uint16_t)b;
-        atomicAdd(&cnt[b], 1);
-      }
+      if (e < L) atomicAdd(&cnt[(int)((q & 1) ? (wv[q >> 1] >> 20) : ((wv[q >> 1] >> 4) & 0xFFFu))], 1);
     }
   }
   __syncthreads();

@@ -900,8 +900,10 @@ __global__ void __launch_bounds__(kTableWarps * 32, 1) table_hw_kernel(const Tab
             if (w < NW) {
               const uint32_t o = v[w] + Eg[w / GW];
               const uint32_t d = o + tv[c];
-              if (d & 0x8000u) push_hit(i, 2 * w, (int)(o & 0xFFFFu));
-              if (d & 0x80000000u) push_hit(i, 2 * w + 1, (int)(o >> 16));
+              if (d & 0x80008000u) {  // one test a word; the halves only for words with a hit
+                if (d & 0x8000u) push_hit(i, 2 * w, (int)(o & 0xFFFFu));
+                if (d & 0x80000000u) push_hit(i, 2 * w + 1, (int)(o >> 16));
+              }
             }
           }
         }
