@@ -253,10 +253,60 @@ def cpu_fast_oracle_rate(pair, seconds=3.0):
 
 
 # ---------------------------------------------------------------------------
+def run_reference_config1(args):
+    """Config 1 as stated (N = 6,000, ~10 % list-2 ties, 1,000 permutations)
+    through the reference algorithm restated in C, every task in full
+    (string hash-set intersection per cell, FP64 tail, tasks over all host
+    threads).  Permutations: numpy's seeded generator (the reference's own
+    generator is unseeded)."""
+    import numpy as np
+    from oracle import oracle as O
+    from dual_threshold_optimization_gb300 import synth
+    pair = synth.config1()
+    (r1, f1), (r2, f2) = pair.sorted_lists()
+    names = pair.feature_names()
+    g1 = [names[f] for f in f1]
+    g2 = [names[f] for f in f2]
+    P = args.ref_tasks
+    rng = np.random.default_rng(1)
+    idx1 = np.empty((P + 1, len(r1)), np.int32)
+    idx2 = np.empty((P + 1, len(r2)), np.int32)
+    idx1[0], idx2[0] = np.arange(len(r1)), np.arange(len(r2))
+    for t in range(1, P + 1):
+        idx1[t] = rng.permutation(len(r1))
+        idx2[t] = rng.permutation(len(r2))
+    threads = host_threads()
+    t0 = time.perf_counter()
+    recs, cells = O.ref_run(g1, r1, g2, r2, pair.population, idx1, idx2, P + 1, 1, threads)
+    dt = time.perf_counter() - t0
+    p_obs = recs[0]["pvalue"]
+    emp = O.empirical(p_obs, [r["pvalue"] for r in recs[1:]])
+    line = {
+        "impl": "reference", "metric": "perms/s, config 1 (N=6000, ties, 1000 permutations)",
+        "value": P / dt, "unit": "perms/s", "n_gpus": 0, "steps": 1, "warmup": 0,
+        "ms_per_step": dt * 1e3, "higher_is_better": True, "dtype": "f64",
+        "data": "synthetic (synth.config1: seeded Gaussian-copula lists, rho 0.3, min-method ties)",
+        "config": {"workload": "config 1: N=6000, ~10% of list-2 features in tie blocks of 2-5, "
+                               "%d permutations + the unpermuted task, every task in full" % P,
+                   "grid": [len(O.thresholds(int(r1[-1]))), len(O.thresholds(int(r2[-1])))]},
+        "cpu_baseline": {"value": P / dt, "unit": "perms/s", "cores": threads, "kind": "port",
+                         "sample": "all %d tasks, %d grid cells" % (P + 1, cells)},
+        "result": {"rank1": recs[0]["rank1"], "rank2": recs[0]["rank2"],
+                   "unpermuted_intersection_size": recs[0]["intersection_size"],
+                   "unpermuted_pvalue": p_obs, "empirical_pvalue": emp,
+                   "fdr": O.fdr(recs[0]["set1_len"], recs[0]["set2_len"], recs[0]["intersection_size"],
+                                pair.population)},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def run_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
         return 0
+    if args.workload == "config1":
+        return run_reference_config1(args)
     from dual_threshold_optimization_gb300 import synth
     pair = synth.copula_pair(N_FEATURES, RHO, seed=2)
     threads = host_threads()
@@ -301,8 +351,26 @@ def run_gpu(args):
     eng = Engine(dev)
     dp = eng.pair(pair.ranks1, pair.feat1, pair.ranks2, pair.feat2, pair.n_features, pair.population)
     P = args.perms
-    seed = 0x5EED0000 + rank  # disjoint streams per rank (weak scaling)
     stream = torch.cuda.ExternalStream(eng.stream)
+    from dual_threshold_optimization_gb300.run import shard_range
+
+    def null_step(q, s):
+        """One step: one null of world * P permutations of seed s, split over
+        the ranks by contiguous id ranges (P each: weak scaling).  Rank 0 runs
+        the unpermuted task; the one exchange broadcasts its p and sums the
+        ranks' counts of permutations at or below it."""
+        first, count = shard_range(world * P, rank, world)
+        r = q.run(count, seed=s, first=first, precision="screen", unpermuted=(rank == 0))
+        if world > 1:
+            p_obs = torch.tensor([r.unpermuted["pvalue"] if rank == 0 else 0.0], dtype=torch.float64,
+                                 device="cuda")
+            torch.distributed.broadcast(p_obs, 0)
+            le = torch.tensor([int(np.count_nonzero(r.minp <= float(p_obs.item())))], dtype=torch.int64,
+                              device="cuda")
+            torch.distributed.all_reduce(le)
+            r.summary["count_le_all_ranks"] = int(le.item())
+        return r
+    seed = 0x5EED0000
 
     def barrier():
         if world > 1:
@@ -313,7 +381,7 @@ def run_gpu(args):
     sampler = ClockSampler(dev)
     sampler.start()  # before the warm-up, so that it samples from the timed region's start
     for w in range(args.warmup):
-        dp.run(P, seed=seed + 1000 + w, precision="screen")
+        null_step(dp, seed + 1000 + w)
     barrier()
     sampler.begin()
     e0 = torch.cuda.Event(enable_timing=True)
@@ -322,7 +390,7 @@ def run_gpu(args):
     step_ms, grid_ms, launches, summaries = [], [], 0, []
     for s in range(args.steps):
         t0 = time.perf_counter()
-        r = dp.run(P, seed=seed + s, precision="screen")
+        r = null_step(dp, seed + s)
         step_ms.append((time.perf_counter() - t0) * 1e3)
         grid_ms.append(r.summary["grid_ms"])
         launches += r.summary["n_launches"]
@@ -345,7 +413,7 @@ def run_gpu(args):
     for s in range(args.e2e_steps):
         t0 = time.perf_counter()
         dq = eng.pair(pair.ranks1, pair.feat1, pair.ranks2, pair.feat2, pair.n_features, pair.population)
-        rr = dq.run(P, seed=seed + 500 + s, precision="screen")
+        rr = null_step(dq, seed + 500 + s)
         h2d = dq.upload_bytes + rr.summary["h2d_bytes"]
         d2h = rr.summary["d2h_bytes"]
         dq.close()
@@ -397,6 +465,10 @@ def run_gpu(args):
                 "same_argmin_as_screen": bool(np.array_equal(r64.minp, r32.minp)
                                               and r64.unpermuted == r32.unpermuted)}
 
+    extras = None
+    if world == 1 and not args.no_extras:
+        extras = extra_configs(eng, args, torch)
+
     # ---- CPU baseline (reference algorithm restated) ----
     cpu = None
     if not args.no_cpu:
@@ -427,6 +499,7 @@ def run_gpu(args):
         "fp64_gpu": fp64,
         "clocks": clocks,
         "gpu_launches": launches,
+        "other_configs": extras,
         "screen": {"fp64_refines_per_task": s0["n_refined"] / (P + 1),
                    "stage2_per_task": s0["n_stage2"] / (P + 1),
                    "logp_err_bound_screen": s0["logp_err_bound_screen"],
@@ -439,6 +512,74 @@ def run_gpu(args):
     if world > 1:
         torch.distributed.destroy_process_group()
     return 0
+
+
+# ---------------------------------------------------------------------------
+# the other benchmark configurations, as short extra keys of the N=1 line
+# ---------------------------------------------------------------------------
+def _timed_runs(dp, P, seeds, torch):
+    """Device-resident perms/s of dp.run(P) over the given seeds (one run each,
+    CUDA events on the library's stream)."""
+    ms = []
+    res = None
+    for sd in seeds:
+        torch.cuda.synchronize()
+        res = dp.run(P, seed=sd, precision="screen")
+        ms.append(res.summary["device_ms"])
+    return P / (statistics.mean(ms) * 1e-3), statistics.mean(ms), res
+
+
+def extra_configs(eng, args, torch):
+    """Configs 1, 3, 4 and 5 of the benchmark set, each short: perms/s with the
+    pair resident (warm ladder after one untimed run), its statistics, and
+    the batch and serving numbers."""
+    from dual_threshold_optimization_gb300 import synth
+    out = {}
+    # config 1: N = 6,000, ~10 % ties; 1,000 permutations as stated, and 100,000
+    p1 = synth.config1()
+    d1 = eng.pair(p1.ranks1, p1.feat1, p1.ranks2, p1.feat2, p1.n_features, p1.population)
+    d1.run(1000, seed=1)
+    v1000, ms1000, r1k = _timed_runs(d1, 1000, [11, 12, 13], torch)
+    d1.run(100000, seed=2)
+    v1e5, ms1e5, _ = _timed_runs(d1, 100000, [21, 22, 23], torch)
+    out["config1"] = {"workload": "N=6000, rho 0.3, ~10% of list-2 features in tie blocks of 2-5",
+                      "perms_1000": {"value": v1000, "unit": "perms/s", "ms_per_run": ms1000},
+                      "perms_100000": {"value": v1e5, "unit": "perms/s", "ms_per_run": ms1e5},
+                      "unpermuted_pvalue": r1k.unpermuted["pvalue"],
+                      "empirical_pvalue": r1k.summary["empirical_pvalue"], "fdr": r1k.summary["fdr"]}
+    d1.close()
+    # config 4: 25,000-feature rankings on an 18,000-feature background,
+    # geometric ties, 10^6 permutations
+    p4 = synth.config4()
+    d4 = eng.pair(p4.ranks1, p4.feat1, p4.ranks2, p4.feat2, p4.n_features, p4.population)
+    d4.run(1_000_000, seed=41)
+    v4, ms4, r4 = _timed_runs(d4, 1_000_000, [42], torch)
+    out["config4"] = {"workload": "25000-feature rankings restricted to an 18000-feature background, "
+                                  "geometric tie blocks (mean 5), rho 0.1, 1000000 permutations",
+                      "value": v4, "unit": "perms/s", "ms_per_run": ms4,
+                      "unpermuted_pvalue": r4.unpermuted["pvalue"],
+                      "empirical_pvalue": r4.summary["empirical_pvalue"],
+                      "count_le": r4.summary["count_le"], "fdr": r4.summary["fdr"],
+                      "routes": r4.summary["n_route"]}
+    d4.close()
+    # config 3: 512 uneven pairs x 10,000 permutations (seeds differ per run)
+    pairs = synth.batch_pairs(512, 2000, 30000, 0.0, 0.4, seed=3)
+    dps = [eng.pair(p.ranks1, p.feat1, p.ranks2, p.feat2, p.n_features, p.population) for p in pairs]
+    eng.batch_run(dps, 10000, [0xBA7C0000 + q for q in range(512)], lanes=args.lanes)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    eng.batch_run(dps, 10000, [0xBA7D0000 + q for q in range(512)], lanes=args.lanes)
+    dtb = time.perf_counter() - t0
+    out["config3_batch"] = {"workload": "512 pairs, N ~ U[2000, 30000], rho ~ U[0, 0.4], 10000 "
+                                        "permutations each, %d lanes" % args.lanes,
+                            "value": 512 * 10000 / dtb, "unit": "perms/s", "ms_per_batch": dtb * 1e3}
+    for d in dps:
+        d.close()
+    # config 5: a short serving run (60 requests)
+    sv = serve_measure(eng, 60, args.lanes, [0.5])
+    sv.pop("lists"), sv.pop("Ps")
+    out["config5_serve"] = sv
+    return out
 
 
 # ---------------------------------------------------------------------------
@@ -459,17 +600,20 @@ def run_batch(args):
     npairs, P = args.batch_pairs, args.batch_perms
     pairs = synth.batch_pairs(npairs, 2000, 30000, 0.0, 0.4, seed=3)
     eng = Engine(dev)
-    seeds = [0xBA7C0000 + q for q in range(npairs)]
     dps = [eng.pair(p.ranks1, p.feat1, p.ranks2, p.feat2, p.n_features, p.population) for p in pairs]
     cells = sum(dp.n1 * dp.n2 for dp in dps)
-    for _ in range(args.warmup):
-        eng.batch_run(dps, P, seeds, lanes=args.lanes)
+    # every run takes seeds of its own: a pair's stored ladder never comes from
+    # the very permutations it then screens
+    def step_seeds(k):
+        return [0xBA7C0000 + 0x10000 * k + q for q in range(npairs)]
+    for w in range(args.warmup):
+        eng.batch_run(dps, P, step_seeds(1000 + w), lanes=args.lanes)
     torch.cuda.synchronize()
     sampler = ClockSampler(dev)
     sampler.start()
     t0 = time.perf_counter()
-    for _ in range(args.steps):
-        res = eng.batch_run(dps, P, seeds, lanes=args.lanes)
+    for k in range(args.steps):
+        res = eng.batch_run(dps, P, step_seeds(k), lanes=args.lanes)
     dt = (time.perf_counter() - t0) / max(args.steps, 1)
     clocks = sampler.stop()
     value = npairs * P / dt
@@ -478,7 +622,7 @@ def run_batch(args):
     for _ in range(args.e2e_steps):
         t0 = time.perf_counter()
         dq = [eng.pair(p.ranks1, p.feat1, p.ranks2, p.feat2, p.n_features, p.population) for p in pairs]
-        rr = eng.batch_run(dq, P, seeds, lanes=args.lanes)
+        rr = eng.batch_run(dq, P, step_seeds(2000), lanes=args.lanes)
         e2e_t.append(time.perf_counter() - t0)
         h2d = sum(d.upload_bytes for d in dq)
         for d in dq:
@@ -504,26 +648,23 @@ def run_batch(args):
     return 0
 
 
-def run_serve(args):
+def serve_measure(eng, M, lanes, loads, rng_seed=5):
+    """Config 5: M requests (N log-uniform in [1,000, 60,000], permutations
+    log-uniform in [1,000, 100,000], rho uniform in [0, 0.4]), each creating its
+    pair from host arrays at arrival and submitted to a server of `lanes`
+    lanes: all at once (saturated), then Poisson arrivals at each fraction of
+    the saturated rate.  Latency = arrival to completion (host clock)."""
     import numpy as np
-    import torch
-    from dual_threshold_optimization_gb300 import Engine, synth
-    rank, world, local = dist_env()
-    dev = local if torch.cuda.device_count() > local else 0
-    torch.cuda.set_device(dev)
-    rng = np.random.default_rng(5)
-    M = args.serve_requests
+    from dual_threshold_optimization_gb300 import synth
+    rng = np.random.default_rng(rng_seed)
     Ns = np.exp(rng.uniform(np.log(1000), np.log(60000), M)).astype(int)
     Ps = np.exp(rng.uniform(np.log(1000), np.log(100000), M)).astype(int)
     rhos = rng.uniform(0.0, 0.4, M)
     lists = [synth.copula_pair(int(n), float(r), seed=500 + q) for q, (n, r) in enumerate(zip(Ns, rhos))]
-    eng = Engine(dev)
     total_perms = int(Ps.sum())
 
-    def play(srv, arrivals):
-        """Submit request q at arrivals[q] seconds (pair created from host
-        arrays at arrival); returns per-request latency (s) and makespan."""
-        jobs, t_arr = [], []
+    def play(srv, arrivals, seed0):
+        jobs = []
         t0 = time.perf_counter()
         for q in range(M):
             now = time.perf_counter() - t0
@@ -533,7 +674,7 @@ def run_serve(args):
             p = lists[q]
             dp = eng.pair(p.ranks1, p.feat1, p.ranks2, p.feat2, p.n_features, p.population)
             ts = time.perf_counter()
-            jobs.append((srv.submit(dp, int(Ps[q]), seed=900 + q), dp, ta, ts))
+            jobs.append((srv.submit(dp, int(Ps[q]), seed=seed0 + q), dp, ta, ts))
         lat, t_end = [], 0.0
         for job, dp, ta, ts in jobs:
             job.wait()
@@ -543,21 +684,38 @@ def run_serve(args):
             dp.close()
         return np.array(lat), t_end - t0
 
-    with eng.server(lanes=args.lanes) as srv:
-        play(srv, np.zeros(M))  # warm-up: every request at once
-        sampler = ClockSampler(dev)
-        sampler.start()
-        lat0, span = play(srv, np.zeros(M))
-        clocks = sampler.stop()
+    with eng.server(lanes=lanes) as srv:
+        play(srv, np.zeros(M), 900)  # warm-up: every request at once
+        lat0, span = play(srv, np.zeros(M), 1900)
         cap_rps = M / span
         rates = []
-        for frac in args.serve_loads:
+        for k, frac in enumerate(loads):
             lam = frac * cap_rps
             arr = np.cumsum(rng.exponential(1.0 / lam, M))
-            lat, span_r = play(srv, arr)
+            lat, span_r = play(srv, arr, 2900 + 1000 * k)
             rates.append({"load": frac, "rate_rps": lam, "p50_ms": float(np.median(lat) * 1e3),
                           "p99_ms": float(np.quantile(lat, 0.99) * 1e3),
                           "perms_per_s": total_perms / span_r})
+    return {"requests": M, "lanes": lanes, "permutations_total": total_perms,
+            "n_range": [int(Ns.min()), int(Ns.max())], "perm_range": [int(Ps.min()), int(Ps.max())],
+            "saturated": {"perms_per_s": total_perms / span, "requests_per_s": cap_rps,
+                          "p50_ms": float(np.median(lat0) * 1e3), "p99_ms": float(np.quantile(lat0, 0.99) * 1e3)},
+            "poisson": rates, "lists": lists, "Ps": Ps}
+
+
+def run_serve(args):
+    import torch
+    from dual_threshold_optimization_gb300 import Engine
+    rank, world, local = dist_env()
+    dev = local if torch.cuda.device_count() > local else 0
+    torch.cuda.set_device(dev)
+    eng = Engine(dev)
+    sampler = ClockSampler(dev)
+    sampler.start()
+    sv = serve_measure(eng, args.serve_requests, args.lanes, args.serve_loads)
+    clocks = sampler.stop()
+    lists, Ps = sv.pop("lists"), sv.pop("Ps")
+    M = sv["requests"]
     # the plain FP64 GPU path on a sample of the same requests (256 permutations each)
     fp64_perms, fp64_s, nreq = 0, 0.0, 0
     for q in range(0, M, max(1, M // 4)):
@@ -568,17 +726,17 @@ def run_serve(args):
         fp64_s += r.summary["device_ms"] * 1e-3
         nreq += 1
         dp.close()
+    sat = sv["saturated"]
     line = {
-        "metric": SERVE_METRIC, "value": total_perms / span, "unit": "perms/s", "n_gpus": 1,
-        "steps": 1, "warmup": 1, "ms_per_step": span * 1e3, "higher_is_better": True, "scaling": "weak",
+        "metric": SERVE_METRIC, "value": sat["perms_per_s"], "unit": "perms/s", "n_gpus": 1,
+        "steps": 1, "warmup": 1, "ms_per_step": sv["permutations_total"] / sat["perms_per_s"] * 1e3,
+        "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "int32+f32 screen, f64 refine",
         "data": "synthetic (seeded Gaussian-copula lists)",
         "config": {"workload": "serve: %d requests, %d lanes" % (M, args.lanes), "requests": M,
-                   "lanes": args.lanes, "permutations_total": total_perms,
-                   "n_range": [int(Ns.min()), int(Ns.max())], "perm_range": [int(Ps.min()), int(Ps.max())]},
-        "saturated": {"requests_per_s": cap_rps, "p50_ms": float(np.median(lat0) * 1e3),
-                      "p99_ms": float(np.quantile(lat0, 0.99) * 1e3)},
-        "poisson": rates,
+                   "lanes": args.lanes, "permutations_total": sv["permutations_total"],
+                   "n_range": sv["n_range"], "perm_range": sv["perm_range"]},
+        "saturated": sat, "poisson": sv["poisson"],
         "fp64_gpu": {"value": fp64_perms / fp64_s, "unit": "perms/s",
                      "sample": "%d permutations over %d of the requests" % (fp64_perms, nreq)},
         "clocks": clocks,
@@ -600,7 +758,11 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--traffic", type=float, default=None,
                     help="DRAM bytes per grid-kernel launch from an ncu capture")
-    ap.add_argument("--workload", default="single", choices=["single", "batch", "serve"],
+    ap.add_argument("--no-extras", action="store_true",
+                    help="leave out the short runs of configs 1, 3 and 4 from the N=1 line")
+    ap.add_argument("--ref-tasks", type=int, default=1000,
+                    help="--impl reference --workload config1: permutations run in full")
+    ap.add_argument("--workload", default="single", choices=["single", "batch", "serve", "config1"],
                     help="single: the headline pair; batch: 512 uneven pairs; serve: Poisson request loop")
     ap.add_argument("--lanes", type=int, default=4)
     ap.add_argument("--batch-pairs", type=int, default=512)
