@@ -17,10 +17,22 @@
 #include <string>
 #include <vector>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include "../../include/dto.h"
 #include "dto_internal.h"
 
 namespace dto {
+
+// An NVTX range over a stage of a run (header-only NVTX: without a profiler
+// attached the push and pop cost a branch).  The ranges mark the host-side
+// enqueue of each stage; the device work follows on the lane's streams.
+struct NvtxRange {
+  explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+  ~NvtxRange() { nvtxRangePop(); }
+  NvtxRange(const NvtxRange&) = delete;
+  NvtxRange& operator=(const NvtxRange&) = delete;
+};
 
 // Buffers of one in-flight batch of the table-screen pipeline.
 struct BatchSlot {

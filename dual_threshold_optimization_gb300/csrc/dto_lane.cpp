@@ -321,6 +321,7 @@ int ensure_table(Lane* L, dto_pair* P, int level, int tau, cudaStream_t stream, 
 // below `tight_levels` switch to their tighter tables.
 int table_levels(Lane* L, dto_pair* P, const int16_t* X, long long xstride, int ntask, TaskResult* dOut,
                  int lev_begin, int lev_end, int* fall, int* cnts, cudaStream_t stream, int hb, int tight_levels) {
+  NvtxRange range(lev_begin == 0 ? "dto: table level 0" : "dto: table levels 1-2");
   const int cap = std::max(ntask, 1);
   const int hitcap = kTableWarpHits;
   const bool packed = P->ncommon <= kPackedMaxCommon;
@@ -368,6 +369,7 @@ int table_levels(Lane* L, dto_pair* P, const int16_t* X, long long xstride, int 
 // The exhaustive screen of what the last table level left, on `stream`.
 int table_exhaustive(Lane* L, dto_pair* P, const int16_t* X, long long xstride, int ntask, TaskResult* dOut,
                      int nlev, const int* fall, int* cnts, cudaStream_t stream) {
+  NvtxRange range("dto: exhaustive fallback");
   const int cap = std::max(ntask, 1);
   GridArgs g{};
   g.P = P->dev;
@@ -400,6 +402,7 @@ int make_labels_launch(Lane* L, dto_pair* P, uint64_t seed, uint32_t first, int 
 
 int lane_make_labels(Lane* L, dto_pair* P, uint64_t seed, uint32_t first, int count,
                      const int32_t* dIdx /* nullable: test mode, [count][N1+N2] */, int row0) {
+  NvtxRange range("dto: labels");
   long long xs = xstride_of(P->N1);
   int rc = lane_grow(L, &L->dX, &L->xBytes, (size_t)(count + row0) * xs * 2);
   if (rc) return rc;
@@ -530,6 +533,7 @@ int lane_run_range(Lane* L, dto_pair* P, uint32_t perm_first, int64_t n_perm, ui
     return lane_err(L, DTO_ERR_INVALID, "n_perm out of range");
   if (precision != DTO_PRECISION_FP64 && precision != DTO_PRECISION_SCREEN)
     return lane_err(L, DTO_ERR_INVALID, "unknown precision");
+  NvtxRange run_range("dto: run");
   LCK(cudaSetDevice(L->ctx->device));
   const long long L12 = P->N1 + P->N2;
   if (perm_idx) {
@@ -710,6 +714,7 @@ int lane_run_range(Lane* L, dto_pair* P, uint32_t perm_first, int64_t n_perm, ui
       const int32_t* dI = nullptr;
       r = upload_idx(&sl.dIdx, &sl.idxBytes, b0, cnt, &dI);
       if (r) return r;
+      NvtxRange range("dto: labels");
       LCK(cudaEventRecord(sl.ev[0], L->stream));
       r = make_labels_launch(L, P, seed, (uint32_t)(perm_first + b0), cnt, dI, (int16_t*)sl.dX, xs);
       if (r) return r;
@@ -761,6 +766,7 @@ int lane_run_range(Lane* L, dto_pair* P, uint32_t perm_first, int64_t n_perm, ui
     // fallback and result copy run on its slot's side stream, the next
     // batches' labels and level-0 table sweeps run on the main stream.
     auto harvest = [&](BatchSlot& sl) -> int {
+      NvtxRange range("dto: result copy");
       LCK(cudaEventSynchronize(sl.ev[7]));
       float ms = 0.f;
       if (cudaEventElapsedTime(&ms, sl.ev[0], sl.ev[1]) == cudaSuccess) L->acc_perm_ms += ms;

@@ -74,3 +74,23 @@ def test_no_oracle_in_product():
             if f.endswith((".py", ".cu", ".cuh", ".cpp", ".h")):
                 txt = open(os.path.join(dp, f), errors="ignore").read()
                 assert not pat.search(txt), f
+
+
+def test_rust_binding_matches_the_header():
+    # the Rust crate (not compiled in this image: no cargo) declares every
+    # entry point of include/dto.h, and its structs list the fields in the
+    # order of the ctypes binding
+    import re
+    from dual_threshold_optimization_gb300._lib import DtoResult, DtoSummary
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    hdr = open(os.path.join(root, "include", "dto.h")).read()
+    rs = open(os.path.join(root, "dual_threshold_optimization_gb300", "rust", "src", "ffi.rs")).read()
+    declared = set(re.findall(r"DTO_API[^(]*?\b(dto_\w+)\(", hdr))
+    bound = set(re.findall(r"pub fn (dto_\w+)\(", rs))
+    assert declared == bound, (declared ^ bound)
+
+    def fields(struct):
+        body = re.search(r"pub struct %s \{(.*?)\n\}" % struct, rs, re.S).group(1)
+        return re.findall(r"pub (\w+):", body)
+    assert fields("dto_result") == [f for f, _ in DtoResult._fields_]
+    assert fields("dto_summary") == [f for f, _ in DtoSummary._fields_]
