@@ -656,14 +656,22 @@ def serve_measure(eng, M, lanes, loads, rng_seed=5):
     the saturated rate.  Latency = arrival to completion (host clock)."""
     import numpy as np
     from dual_threshold_optimization_gb300 import synth
-    rng = np.random.default_rng(rng_seed)
-    Ns = np.exp(rng.uniform(np.log(1000), np.log(60000), M)).astype(int)
-    Ps = np.exp(rng.uniform(np.log(1000), np.log(100000), M)).astype(int)
-    rhos = rng.uniform(0.0, 0.4, M)
-    lists = [synth.copula_pair(int(n), float(r), seed=500 + q) for q, (n, r) in enumerate(zip(Ns, rhos))]
+    def requests(seed, pair_seed0):
+        rng = np.random.default_rng(seed)
+        Ns = np.exp(rng.uniform(np.log(1000), np.log(60000), M)).astype(int)
+        Ps = np.exp(rng.uniform(np.log(1000), np.log(100000), M)).astype(int)
+        rhos = rng.uniform(0.0, 0.4, M)
+        lists = [synth.copula_pair(int(n), float(r), seed=pair_seed0 + q) for q, (n, r) in enumerate(zip(Ns, rhos))]
+        return Ns, Ps, lists
+
+    # the warm-up plays requests of its own (other sizes, other lists): the
+    # timed requests find only what earlier timed requests left
+    _, Ps_w, lists_w = requests(rng_seed + 1000, 50_000)
+    Ns, Ps, lists = requests(rng_seed, 500)
+    rng = np.random.default_rng(rng_seed + 1)
     total_perms = int(Ps.sum())
 
-    def play(srv, arrivals, seed0):
+    def play(srv, arrivals, seed0, lists=lists, Ps=Ps):
         jobs = []
         t0 = time.perf_counter()
         for q in range(M):
@@ -685,7 +693,7 @@ def serve_measure(eng, M, lanes, loads, rng_seed=5):
         return np.array(lat), t_end - t0
 
     with eng.server(lanes=lanes) as srv:
-        play(srv, np.zeros(M), 900)  # warm-up: every request at once
+        play(srv, np.zeros(M), 900, lists_w, Ps_w)  # warm-up: every request at once
         lat0, span = play(srv, np.zeros(M), 1900)
         cap_rps = M / span
         rates = []

@@ -75,6 +75,10 @@ struct Lane {
   // that share the GPU with other runs take the warp-per-task screen, whose
   // throughput is higher
   bool coop_first = true;
+  // a pair without a ladder of its own starts from the ladder of an earlier
+  // pair of the same shape (LadderModel), skipping its first batch (server
+  // and batch lanes: many pairs, each run once)
+  bool use_model = false;
   cudaStream_t stream = nullptr;
   cudaStream_t side = nullptr;  // first batch, later table levels and fallbacks
   cudaEvent_t evSide = nullptr;
@@ -121,6 +125,28 @@ struct Lane {
   int kthr_tau[kTables] = {};
 };
 
+// Ladders of the pairs a context has run, by shape, in nats of ln p.  The
+// null distribution of the minimum p-value depends on the pair's shape (list
+// lengths, shared features, population, grid) and hardly on its ranks, and a
+// ladder decides only which path settles each permutation, never a result:
+// so a pair of nearly the same shape as an earlier one can start from that
+// pair's ladder instead of measuring its own from an exhaustive first batch.
+struct LadderShape {
+  long long npop, N1, N2, ncommon;
+  int n1, n2;
+  bool same_set;
+  double nats[kLadderTaus];
+};
+
+struct LadderModel {
+  std::mutex mu;
+  std::vector<LadderShape> shapes;  // most recent last
+  static constexpr size_t kMaxShapes = 4096;
+  static constexpr double kTol = 0.05;  // relative difference accepted per size
+  void record(const LadderShape& x);
+  bool lookup(const LadderShape& want, double nats[kLadderTaus]);
+};
+
 }  // namespace dto
 
 struct dto_ctx {
@@ -139,6 +165,7 @@ struct dto_ctx {
   std::vector<double2*> lf_old;
   std::atomic<unsigned long long> next_serial{1};
   dto::Lane* lane0 = nullptr;
+  dto::LadderModel ladders;
 };
 
 struct dto_pair {

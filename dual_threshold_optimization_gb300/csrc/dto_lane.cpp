@@ -391,6 +391,56 @@ int table_exhaustive(Lane* L, dto_pair* P, const int16_t* X, long long xstride, 
   return DTO_OK;
 }
 
+void LadderModel::record(const LadderShape& x) {
+  std::lock_guard<std::mutex> g(mu);
+  for (auto it = shapes.begin(); it != shapes.end(); ++it)
+    if (it->npop == x.npop && it->N1 == x.N1 && it->N2 == x.N2 && it->ncommon == x.ncommon && it->n1 == x.n1 &&
+        it->n2 == x.n2 && it->same_set == x.same_set) {
+      shapes.erase(it);
+      break;
+    }
+  if (shapes.size() >= kMaxShapes) shapes.erase(shapes.begin());
+  shapes.push_back(x);
+}
+
+bool LadderModel::lookup(const LadderShape& want, double nats[kLadderTaus]) {
+  auto rel = [](double a, double b) { return std::fabs(a - b) / std::max(1.0, std::max(a, b)); };
+  std::lock_guard<std::mutex> g(mu);
+  const LadderShape* best = nullptr;
+  double best_d = 1e300;
+  for (const LadderShape& x : shapes) {
+    if (x.same_set != want.same_set) continue;
+    const double d[6] = {rel((double)x.npop, (double)want.npop), rel((double)x.N1, (double)want.N1),
+                         rel((double)x.N2, (double)want.N2), rel((double)x.ncommon, (double)want.ncommon),
+                         rel(x.n1, want.n1), rel(x.n2, want.n2)};
+    double sum = 0.0;
+    bool ok = true;
+    for (double v : d) {
+      ok = ok && v <= kTol;
+      sum += v;
+    }
+    if (ok && sum < best_d) {
+      best_d = sum;
+      best = &x;
+    }
+  }
+  if (!best) return false;
+  for (int l = 0; l < kLadderTaus; ++l) nats[l] = best->nats[l];
+  return true;
+}
+
+static LadderShape shape_of(const dto_pair* P) {
+  LadderShape x{};
+  x.npop = P->npop;
+  x.N1 = P->N1;
+  x.N2 = P->N2;
+  x.ncommon = P->ncommon;
+  x.n1 = (int)P->T1.size();
+  x.n2 = (int)P->T2.size();
+  x.same_set = P->same_set;
+  return x;
+}
+
 int fixed_log(double p, int fshift) {
   double t = std::floor(std::log(p) * std::ldexp(1.0, fshift));
   return (int)std::max(-2.0e9, std::min(0.0, t));
@@ -667,6 +717,15 @@ int lane_run_range(Lane* L, dto_pair* P, uint32_t perm_first, int64_t n_perm, ui
         for (int l = 0; l < kLadderTaus; ++l) tau[l] = P->ladder_tau[l];
       }
     }
+    double model_nats[kLadderTaus];
+    if (!warm && L->use_model && L->ctx->ladders.lookup(shape_of(P), model_nats)) {
+      // a pair of the same shape has run: start from its ladder
+      warm = true;
+      const double scale = std::ldexp(1.0, P->fshift);
+      for (int l = 0; l < kLadderTaus; ++l)
+        tau[l] = (int)std::max(-2.0e9, std::min(0.0, std::floor(model_nats[l] * scale)));
+      ladder_order(tau);
+    }
     const int cnt0 = warm ? 0 : (int)first_batch;
     if (warm) {
       rc = lane_grow(L, &L->dX, &L->xBytes, (size_t)xs * 2);
@@ -847,6 +906,9 @@ int lane_run_range(Lane* L, dto_pair* P, uint32_t perm_first, int64_t n_perm, ui
         if (!P->ladder_ok || std::llabs((long long)t[l] - P->ladder_tau[l]) > slack) P->ladder_tau[l] = t[l];
       ladder_order(P->ladder_tau);
       P->ladder_ok = true;
+      LadderShape x = shape_of(P);
+      for (int l = 0; l < kLadderTaus; ++l) x.nats[l] = std::ldexp((double)P->ladder_tau[l], -P->fshift);
+      L->ctx->ladders.record(x);
     }
     // the main stream's timing event follows the side streams' last work
     LCK(cudaEventRecord(L->evSide, L->side));

@@ -143,6 +143,7 @@ int dto_serve_create(dto_ctx* ctx, int lanes, int64_t mem_budget, dto_server** o
       return rc;
     }
     L->coop_first = false;  // requests share the GPU: throughput first
+    L->use_model = true;    // many pairs, each run once: start from similar pairs' ladders
     s->lanes.push_back(L);
   }
   for (int w = 0; w < lanes; ++w) s->workers.emplace_back(worker, s, w);
