@@ -286,8 +286,8 @@ def run_reference_config1(args):
         "value": P / dt, "unit": "perms/s", "n_gpus": 0, "steps": 1, "warmup": 0,
         "ms_per_step": dt * 1e3, "higher_is_better": True, "dtype": "f64",
         "data": "synthetic (synth.config1: seeded Gaussian-copula lists, rho 0.3, min-method ties)",
-        "config": {"workload": "config 1: N=6000, ~10% of list-2 features in tie blocks of 2-5, "
-                               "%d permutations + the unpermuted task, every task in full" % P,
+        "config": {"workload": ("config 1: N=6000, ~10 percent of list-2 features in tie blocks of 2-5, "
+                                "%d permutations + the unpermuted task, every task in full" % P),
                    "grid": [len(O.thresholds(int(r1[-1]))), len(O.thresholds(int(r2[-1])))]},
         "cpu_baseline": {"value": P / dt, "unit": "perms/s", "cores": threads, "kind": "port",
                          "sample": "all %d tasks, %d grid cells" % (P + 1, cells)},
@@ -488,6 +488,12 @@ def run_gpu(args):
         "config": single_config(P),
         "ladder": "value: the pair keeps the table ladder its warm-up runs measured; e2e: a new "
                   "pair each step, so its first run measures the ladder",
+        "timeline_ms_per_step": {
+            "permutations": statistics.mean(s_["perm_ms"] for s_ in summaries),
+            "level0_sweeps": statistics.mean(s_["sweep0_ms"] for s_ in summaries),
+            "after_last_level0": statistics.mean(s_["tail_ms"] for s_ in summaries),
+            "note": "device times of the library's CUDA events; the permutations and level-0 sweeps run "
+                    "one after another on the main stream, later levels on side streams"},
         "routes_per_step": {k: v / args.steps for k, v in
                             ((k, sum(s_["n_route"][k] for s_ in summaries)) for k in summaries[0]["n_route"])},
         "latency_ms": {"p50": statistics.median(step_ms),

@@ -69,7 +69,7 @@ class DtoSummary(C.Structure):
                 ("device_ms", C.c_double), ("grid_ms", C.c_double), ("perm_ms", C.c_double),
                 ("n_launches", C.c_int64), ("h2d_bytes", C.c_int64), ("d2h_bytes", C.c_int64),
                 ("sweep0_ms", C.c_double), ("sweep0_launches", C.c_int64), ("sweep0_tasks", C.c_int64),
-                ("n_route", C.c_int64 * 8)]
+                ("n_route", C.c_int64 * 8), ("tail_ms", C.c_double)]
 
     def as_dict(self):
         d = {k: getattr(self, k) for k, _ in self._fields_ if k != "n_route"}

@@ -626,6 +626,7 @@ int lane_run_range(Lane* L, dto_pair* P, uint32_t perm_first, int64_t n_perm, ui
   };
   std::vector<double> minp((size_t)n_perm);
   long long nroute[DTO_ROUTES] = {};
+  cudaEvent_t last_l0_end = nullptr;  // end of the last level-0 sweep (main stream)
   TaskResult unperm{};
   // Short runs (and FP64 runs) go through the exhaustive screen in batches,
   // the unpermuted task (task 0) in row 0 of the first.  Long runs go through
@@ -860,6 +861,7 @@ int lane_run_range(Lane* L, dto_pair* P, uint32_t perm_first, int64_t n_perm, ui
       rc = table_levels(L, P, X, xs, cnt, dR, 0, 1, (int*)sl.dFall, sl.dCnt, L->stream, 0, tight_levels);
       if (rc) return rc;
       LCK(cudaEventRecord(sl.ev[6], L->stream));
+      last_l0_end = sl.ev[6];
       const int si = (int)(it % Lane::kSlots);
       LCK(cudaStreamWaitEvent(sl.side, sl.ev[6], 0));
       if (built_late) LCK(cudaStreamWaitEvent(sl.side, L->evTables, 0));
@@ -959,6 +961,8 @@ int lane_run_range(Lane* L, dto_pair* P, uint32_t perm_first, int64_t n_perm, ui
     s.sweep0_ms = L->acc_sweep0_ms;
     s.sweep0_launches = L->acc_sweep0_launches;
     s.sweep0_tasks = L->acc_sweep0_tasks;
+    s.tail_ms = 0.0;
+    if (last_l0_end && cudaEventElapsedTime(&ms, last_l0_end, L->ev1) == cudaSuccess) s.tail_ms = ms;
     for (int q = 0; q < DTO_ROUTES; ++q) s.n_route[q] = nroute[q];
   }
   return DTO_OK;

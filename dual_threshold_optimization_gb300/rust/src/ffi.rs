@@ -73,6 +73,7 @@ pub struct dto_summary {
     pub sweep0_launches: i64,
     pub sweep0_tasks: i64,
     pub n_route: [i64; DTO_ROUTES],
+    pub tail_ms: f64,
 }
 
 extern "C" {

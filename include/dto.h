@@ -98,6 +98,8 @@ typedef struct {
     int64_t sweep0_launches;       /* their launches */
     int64_t sweep0_tasks;          /* permutations they took */
     int64_t n_route[DTO_ROUTES];   /* tasks (unpermuted included) settled by each DTO_ROUTE_* */
+    double tail_ms;                /* device time from the end of the last level-0 sweep to the end
+                                      of the run (0 when no table sweep ran) */
 } dto_summary;
 
 DTO_API int dto_version(void);
