@@ -46,7 +46,7 @@ PERMS_PER_STEP = 100000
 # DRAM bytes per task of the level-0 table sweep at N = 20,000, from an ncu
 # capture of one level-0 launch (dram__bytes_read.sum + dram__bytes_write.sum
 # over its tasks): labels read once, hit buffer written and re-read.
-SWEEP0_DRAM_BYTES_PER_TASK = 51900.0
+SWEEP0_DRAM_BYTES_PER_TASK = 43100.0
 WORKLOAD = ("single pair, N=20000 features, list 2 Gaussian copula rho=0.2 to list 1, no ties, "
             "100000 on-device Philox permutations per step + the unpermuted task, "
             "FP32 screen + FP64 refine")
@@ -345,7 +345,7 @@ def run_gpu(args):
         import torch.distributed as dist
         dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
     from dual_threshold_optimization_gb300 import Engine, synth
-    from dual_threshold_optimization_gb300._lib import RESULT_DTYPE  # noqa: F401
+    from dual_threshold_optimization_gb300._lib import OPTIMUM_FIELDS
 
     pair = synth.copula_pair(N_FEATURES, RHO, seed=2)
     eng = Engine(dev)
@@ -462,8 +462,10 @@ def run_gpu(args):
         r32 = dp.run(args.fp64_perms, seed=seed + 777, precision="screen")
         fp64 = {"value": args.fp64_perms / (r64.summary["device_ms"] * 1e-3), "unit": "perms/s",
                 "perms": args.fp64_perms,
-                "same_argmin_as_screen": bool(np.array_equal(r64.minp, r32.minp)
-                                              and r64.unpermuted == r32.unpermuted)}
+                # the optimum fields (the route code differs by design)
+                "same_argmin_as_screen": bool(np.array_equal(r64.minp, r32.minp) and all(
+                    r64.unpermuted[k] == r32.unpermuted[k] for k in OPTIMUM_FIELDS)),
+                "same_minp": bool(np.array_equal(r64.minp, r32.minp))}
 
     extras = None
     if world == 1 and not args.no_extras:
@@ -478,6 +480,11 @@ def run_gpu(args):
         cpu = {"value": rate, "unit": "perms/s", "cores": threads, "kind": "port", "sample": sample,
                "fast_oracle_1thread": {"value": fast, "unit": "perms/s", "tasks": ndone,
                                        "note": "histogram-formulation FP64 oracle"}}
+        if extras is not None:
+            from dual_threshold_optimization_gb300 import synth
+            for key, make in (("config1", synth.config1), ("config4", synth.config4)):
+                f, n = cpu_fast_oracle_rate(make())
+                extras[key]["fast_oracle_1thread"] = {"value": f, "unit": "perms/s", "tasks": n}
 
     s0 = summaries[-1]
     line = {
@@ -535,6 +542,19 @@ def _timed_runs(dp, P, seeds, torch):
     return P / (statistics.mean(ms) * 1e-3), statistics.mean(ms), res
 
 
+def fp64_rate(dp, perms, seed):
+    """The plain FP64 GPU path on `perms` permutations (device time), and
+    whether its optima equal the screen path's."""
+    import numpy as np
+    from dual_threshold_optimization_gb300._lib import OPTIMUM_FIELDS
+    r64 = dp.run(perms, seed=seed, precision="fp64")
+    r32 = dp.run(perms, seed=seed, precision="screen")
+    same = bool(np.array_equal(r64.minp, r32.minp)
+                and all(r64.unpermuted[k] == r32.unpermuted[k] for k in OPTIMUM_FIELDS))
+    return {"value": perms / (r64.summary["device_ms"] * 1e-3), "unit": "perms/s", "perms": perms,
+            "same_optima_as_screen": same}
+
+
 def extra_configs(eng, args, torch):
     """Configs 1, 3, 4 and 5 of the benchmark set, each short: perms/s with the
     pair resident (warm ladder after one untimed run), its statistics, and
@@ -552,7 +572,8 @@ def extra_configs(eng, args, torch):
                       "perms_1000": {"value": v1000, "unit": "perms/s", "ms_per_run": ms1000},
                       "perms_100000": {"value": v1e5, "unit": "perms/s", "ms_per_run": ms1e5},
                       "unpermuted_pvalue": r1k.unpermuted["pvalue"],
-                      "empirical_pvalue": r1k.summary["empirical_pvalue"], "fdr": r1k.summary["fdr"]}
+                      "empirical_pvalue": r1k.summary["empirical_pvalue"], "fdr": r1k.summary["fdr"],
+                      "fp64_gpu": fp64_rate(d1, 512, 31)}
     d1.close()
     # config 4: 25,000-feature rankings on an 18,000-feature background,
     # geometric ties, 10^6 permutations
@@ -566,7 +587,7 @@ def extra_configs(eng, args, torch):
                       "unpermuted_pvalue": r4.unpermuted["pvalue"],
                       "empirical_pvalue": r4.summary["empirical_pvalue"],
                       "count_le": r4.summary["count_le"], "fdr": r4.summary["fdr"],
-                      "routes": r4.summary["n_route"]}
+                      "routes": r4.summary["n_route"], "fp64_gpu": fp64_rate(d4, 256, 43)}
     d4.close()
     # config 3: 512 uneven pairs x 10,000 permutations (seeds differ per run)
     pairs = synth.batch_pairs(512, 2000, 30000, 0.0, 0.4, seed=3)
@@ -576,9 +597,14 @@ def extra_configs(eng, args, torch):
     t0 = time.perf_counter()
     eng.batch_run(dps, 10000, [0xBA7D0000 + q for q in range(512)], lanes=args.lanes)
     dtb = time.perf_counter() - t0
+    f64 = [fp64_rate(dps[q], 256, 44) for q in range(0, 512, 128)]
     out["config3_batch"] = {"workload": "512 pairs, N ~ U[2000, 30000], rho ~ U[0, 0.4], 10000 "
                                         "permutations each, %d lanes" % args.lanes,
-                            "value": 512 * 10000 / dtb, "unit": "perms/s", "ms_per_batch": dtb * 1e3}
+                            "value": 512 * 10000 / dtb, "unit": "perms/s", "ms_per_batch": dtb * 1e3,
+                            "fp64_gpu": {"value": 4 * 256 / sum(256 / f["value"] for f in f64),
+                                         "unit": "perms/s", "sample": "256 permutations of pairs 0, 128, "
+                                                                     "256, 384",
+                                         "same_optima_as_screen": all(f["same_optima_as_screen"] for f in f64)}}
     for d in dps:
         d.close()
     # config 5: a short serving run (60 requests)
