@@ -177,6 +177,17 @@ struct TableGridArgs {
   const uint16_t* tight[3];
   int tight_tau[3];
   int ntight;
+  // The half-warp sweep cascades: a task with no hit at level l is swept
+  // again at level l + 1 by the same half-warp, up to nlev levels (the level
+  // above sits in kthr, tau, tight*, ntight; levels 1 and 2 below).  Tasks
+  // of the last level with no hit go to the fallback list.  nlev = 1: one
+  // level, as the 32-bit sweep always runs.
+  int nlev;
+  const uint16_t* kthr_up[2];
+  int tau_up[2];
+  const uint16_t* tight_up[2][3];
+  int tight_tau_up[2][3];
+  int ntight_up[2];
   int packed;             // 16-bit overlap sweep (every overlap <= 0x7FFF)
   int route;              // DTO_ROUTE_* written with each result
   int smemF;              // the ln m! table is copied to shared memory

@@ -320,7 +320,8 @@ int ensure_table(Lane* L, dto_pair* P, int level, int tau, cudaStream_t stream, 
 // counters then 4 list counts (zeroed by the launch of level 0).  Levels
 // below `tight_levels` switch to their tighter tables.
 int table_levels(Lane* L, dto_pair* P, const int16_t* X, long long xstride, int ntask, TaskResult* dOut,
-                 int lev_begin, int lev_end, int* fall, int* cnts, cudaStream_t stream, int hb, int tight_levels) {
+                 int lev_begin, int lev_end, int* fall, int* cnts, cudaStream_t stream, int hb, int tight_levels,
+                 bool cascade) {
   NvtxRange range(lev_begin == 0 ? "dto: table level 0" : "dto: table levels 1-2");
   const int cap = std::max(ntask, 1);
   const int hitcap = kTableWarpHits;
@@ -328,6 +329,48 @@ int table_levels(Lane* L, dto_pair* P, const int16_t* X, long long xstride, int 
   int rc = lane_grow(L, &L->dHits[hb], &L->hitBytes[hb], (size_t)kTableCtasPerSm * L->ctx->nsm * kTableWarps * hitcap * 8);
   if (rc) return rc;
   if (lev_begin == 0) LCK(cudaMemsetAsync(cnts, 0, 12 * sizeof(int), stream));
+  if (cascade) {
+    // one launch over levels [0, lev_end): a task with no hit at a level is
+    // swept at the next by the same half-warp; the last level's misses go to
+    // the exhaustive screen's list (level lev_end - 1's fallback list)
+    TableGridArgs a{};
+    a.P = P->dev;
+    a.P.LF = L->ctx->dLF.load();
+    a.X = X;
+    a.xstride = xstride;
+    a.ntask = ntask;
+    a.tau = L->kthr_tau[0];
+    a.kthr = L->dKthr[0];
+    a.ntight = 0 < tight_levels ? kTightTables : 0;
+    for (int q = 0; q < a.ntight; ++q) {
+      a.tight[q] = L->dKthr[tight_slot(0, q)];
+      a.tight_tau[q] = L->kthr_tau[tight_slot(0, q)];
+    }
+    a.nlev = lev_end;
+    for (int l = 1; l < lev_end; ++l) {
+      a.kthr_up[l - 1] = L->dKthr[l];
+      a.tau_up[l - 1] = L->kthr_tau[l];
+      a.ntight_up[l - 1] = l < tight_levels ? kTightTables : 0;
+      for (int q = 0; q < a.ntight_up[l - 1]; ++q) {
+        a.tight_up[l - 1][q] = L->dKthr[tight_slot(l, q)];
+        a.tight_tau_up[l - 1][q] = L->kthr_tau[tight_slot(l, q)];
+      }
+    }
+    a.packed = 1;
+    a.route = DTO_ROUTE_LEVEL0;
+    a.smemF = table_smem_bytes(P->C, P->dev.n1, P->dev.n2, P->npop, 1, true) <= L->ctx->smem_optin ? 1 : 0;
+    a.out = dOut;
+    a.work = cnts;
+    a.n_refined = L->dRefined;
+    a.fallback = fall + (size_t)(lev_end - 1) * cap;
+    a.nfallback = cnts + 8 + lev_end - 1;
+    a.hitbuf = (int2*)L->dHits[hb];
+    a.hitcap = hitcap;
+    const int ctas = std::max(1, std::min(kTableCtasPerSm * L->ctx->nsm, ntask / (kTableWarps * 2) + 1));
+    LCK(launch_table_grid(a, P->C, ctas, stream));
+    L->acc_launches += 1;
+    return DTO_OK;
+  }
   for (int level = lev_begin; level < lev_end; ++level) {
     TableGridArgs a{};
     a.P = P->dev;
@@ -343,6 +386,7 @@ int table_levels(Lane* L, dto_pair* P, const int16_t* X, long long xstride, int 
       a.tight_tau[q] = L->kthr_tau[tight_slot(level, q)];
     }
     a.packed = packed ? 1 : 0;
+    a.nlev = 1;
     a.route = DTO_ROUTE_LEVEL0 + level;
     a.smemF = table_smem_bytes(P->C, P->dev.n1, P->dev.n2, P->npop, 1, packed) <= L->ctx->smem_optin ? 1 : 0;
     a.out = dOut;
@@ -809,15 +853,20 @@ int lane_run_range(Lane* L, dto_pair* P, uint32_t perm_first, int64_t n_perm, ui
     // first batch (their first sweeps come a level-0 sweep later; each
     // slot's side stream waits for them).
     const int tight_levels = std::min(n_perm >= kTightAllMin ? kTightLevels : 1, kLadderLevels);
+    // packed pairs sweep all levels in one cascade launch on the main stream,
+    // which needs every level's tables first
+    const bool cascade = P->ncommon <= kPackedMaxCommon;
     bool built0 = false, built_late = false;
     for (int l = 0; l < kLadderLevels; ++l) {
-      rc = ensure_table(L, P, l, tau[l], l == 0 ? L->stream : L->side, l == 0 ? &built0 : &built_late);
+      const bool main = l == 0 || cascade;
+      rc = ensure_table(L, P, l, tau[l], main ? L->stream : L->side, main ? &built0 : &built_late);
       if (rc) return rc;
     }
     for (int l = 0; l < tight_levels; ++l)
       for (int q = 0; q < kTightTables; ++q) {
-        rc = ensure_table(L, P, tight_slot(l, q), tau[tight_slot(l, q)], l == 0 ? L->stream : L->side,
-                          l == 0 ? &built0 : &built_late);
+        const bool main = l == 0 || cascade;
+        rc = ensure_table(L, P, tight_slot(l, q), tau[tight_slot(l, q)], main ? L->stream : L->side,
+                          main ? &built0 : &built_late);
         if (rc) return rc;
       }
     if (built_late) LCK(cudaEventRecord(L->evTables, L->side));
@@ -858,7 +907,8 @@ int lane_run_range(Lane* L, dto_pair* P, uint32_t perm_first, int64_t n_perm, ui
       int16_t* X = (int16_t*)sl.dX;
       TaskResult* dR = (TaskResult*)sl.dRes;
       LCK(cudaEventRecord(sl.ev[2], L->stream));
-      rc = table_levels(L, P, X, xs, cnt, dR, 0, 1, (int*)sl.dFall, sl.dCnt, L->stream, 0, tight_levels);
+      rc = table_levels(L, P, X, xs, cnt, dR, 0, cascade ? nlev : 1, (int*)sl.dFall, sl.dCnt, L->stream, 0,
+                        tight_levels, cascade);
       if (rc) return rc;
       LCK(cudaEventRecord(sl.ev[6], L->stream));
       last_l0_end = sl.ev[6];
@@ -866,9 +916,11 @@ int lane_run_range(Lane* L, dto_pair* P, uint32_t perm_first, int64_t n_perm, ui
       LCK(cudaStreamWaitEvent(sl.side, sl.ev[6], 0));
       if (built_late) LCK(cudaStreamWaitEvent(sl.side, L->evTables, 0));
       LCK(cudaEventRecord(sl.ev[4], sl.side));
-      const int nl = it + 1 == npipe ? std::min(nlev, kLastLevels) : nlev;
-      rc = table_levels(L, P, X, xs, cnt, dR, 1, nl, (int*)sl.dFall, sl.dCnt, sl.side, 1 + si, tight_levels);
-      if (rc) return rc;
+      const int nl = cascade ? nlev : (it + 1 == npipe ? std::min(nlev, kLastLevels) : nlev);
+      if (!cascade) {
+        rc = table_levels(L, P, X, xs, cnt, dR, 1, nl, (int*)sl.dFall, sl.dCnt, sl.side, 1 + si, tight_levels, false);
+        if (rc) return rc;
+      }
       rc = table_exhaustive(L, P, X, xs, cnt, dR, nl, (const int*)sl.dFall, sl.dCnt, sl.side);
       if (rc) return rc;
       LCK(cudaEventRecord(sl.ev[5], sl.side));

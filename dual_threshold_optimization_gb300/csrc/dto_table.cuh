@@ -201,12 +201,12 @@ static __device__ __forceinline__ void table_pending_flush(const TableGridArgs& 
   }
   __syncwarp();
   for (int q = lane; q < np; q += 32) {
-    const int task = m.pendTask[q];
-    if (q == 0 || m.pendTask[q - 1] != task) {
+    const int tw = m.pendTask[q];  // task | route << 28
+    if (q == 0 || m.pendTask[q - 1] != tw) {
       Best b = best_init();
-      for (int r = q; r < np && m.pendTask[r] == task; ++r)
+      for (int r = q; r < np && m.pendTask[r] == tw; ++r)
         best_take(b, m.pendP[r], m.pendK[r], m.pendCell[r] >> 16, m.pendCell[r] & 0xffff);
-      A.out[task] = TaskResult{b.p, b.i, b.j, b.k, A.route};
+      A.out[tw & 0x0FFFFFFF] = TaskResult{b.p, b.i, b.j, b.k, (int)((unsigned)tw >> 28)};
     }
   }
   __syncwarp();
@@ -220,7 +220,7 @@ static __device__ __forceinline__ void table_pending_flush(const TableGridArgs& 
 // Queue the task's survivors that the final B admits, without duplicates
 // (a cell can reach stage 2 twice: as a seed and as a hit).
 static __device__ __forceinline__ void table_defer(const TableGridArgs& A, const TabGrid& g, const TableWarpMem& m,
-                                                int lane, int task) {
+                                                int lane, int task, int route) {
   __syncwarp();
   const int B = m.st->B;
   const int ns = m.st->nsurv;
@@ -240,7 +240,7 @@ static __device__ __forceinline__ void table_defer(const TableGridArgs& A, const
     const unsigned msk = __ballot_sync(kFull, keep);
     if (keep) {
       const int pos = npend + __popc(msk & ((1u << lane) - 1u));
-      m.pendTask[pos] = task;
+      m.pendTask[pos] = task | (route << 28);  // task ids stay below 2^28
       m.pendCell[pos] = m.survCell[q];
       m.pendK[pos] = m.survK[q];
     }
@@ -382,6 +382,26 @@ __device__ __forceinline__ const uint16_t* tight_of(const TableGridArgs& A, int 
 }
 __device__ __forceinline__ int tight_tau_of(const TableGridArgs& A, int q) {
   return q == 0 ? A.tight_tau[0] : q == 1 ? A.tight_tau[1] : A.tight_tau[2];
+}
+// The same per cascade level l (0: the fields above; 1, 2: the *_up fields).
+__device__ __forceinline__ const uint16_t* lv_kthr(const TableGridArgs& A, int l) {
+  return l == 0 ? A.kthr : l == 1 ? A.kthr_up[0] : A.kthr_up[1];
+}
+__device__ __forceinline__ int lv_tau(const TableGridArgs& A, int l) {
+  return l == 0 ? A.tau : l == 1 ? A.tau_up[0] : A.tau_up[1];
+}
+__device__ __forceinline__ int lv_ntight(const TableGridArgs& A, int l) {
+  return l == 0 ? A.ntight : l == 1 ? A.ntight_up[0] : A.ntight_up[1];
+}
+__device__ __forceinline__ const uint16_t* lv_tight(const TableGridArgs& A, int l, int q) {
+  if (l == 0) return tight_of(A, q);
+  if (l == 1) return q == 0 ? A.tight_up[0][0] : q == 1 ? A.tight_up[0][1] : A.tight_up[0][2];
+  return q == 0 ? A.tight_up[1][0] : q == 1 ? A.tight_up[1][1] : A.tight_up[1][2];
+}
+__device__ __forceinline__ int lv_tight_tau(const TableGridArgs& A, int l, int q) {
+  if (l == 0) return tight_tau_of(A, q);
+  if (l == 1) return q == 0 ? A.tight_tau_up[0][0] : q == 1 ? A.tight_tau_up[0][1] : A.tight_tau_up[0][2];
+  return q == 0 ? A.tight_tau_up[1][0] : q == 1 ? A.tight_tau_up[1][1] : A.tight_tau_up[1][2];
 }
 
 template <int C, bool Packed>
@@ -649,7 +669,7 @@ __global__ void __launch_bounds__(kTableWarps * 32, kTableCtasPerSm) table_grid_
       if ((nh > 0 || anyhits[t]) && mt.st->B_valid) {
         if (isinf(mt.st->bp)) {
           // no FP64 tail evaluated yet for this task: queue its survivors
-          table_defer(A, g, mt, lane, bt[t]);
+          table_defer(A, g, mt, lane, bt[t], A.route);
         } else {
           table_refine(A, g, mt, lane);
           if (lane == 0) A.out[bt[t]] = TaskResult{mt.st->bp, mt.st->bi, mt.st->bj, mt.st->bk, A.route};
@@ -757,6 +777,22 @@ __global__ void __launch_bounds__(kTableWarps * 32, 1) table_hw_kernel(const Tab
     sLut[q] = (uint16_t)((4 * (hh * Wp + (tc2 >> 1))) | ((tc2 & 1) << 15));
   }
   const TabGrid g{sRow, sNcnt, A.smemF ? sF : A.P.F};
+  // the cascade levels' tables and bounds, indexed by level from shared
+  // memory (selecting among the kernel's arguments at run time kept them
+  // all in registers and slowed the row loop by a fifth)
+  __shared__ const uint16_t* sLvTab[3][4];  // [level][0: the level's table, 1..3: its tighter tables]
+  __shared__ int sLvTau[3][4];              // [level][0: its bound, 1..3: the tighter tables' bounds]
+  __shared__ int sLvNtight[3];
+  if (threadIdx.x < 3) {
+    const int l = threadIdx.x;
+    sLvTab[l][0] = lv_kthr(A, l);
+    sLvTau[l][0] = lv_tau(A, l);
+    sLvNtight[l] = lv_ntight(A, l);
+    for (int q = 0; q < 3; ++q) {
+      sLvTab[l][1 + q] = lv_tight(A, l, q);
+      sLvTau[l][1 + q] = lv_tight_tau(A, l, q);
+    }
+  }
   int* const cnt_t = wb + half * TI;  // this lane's task's counters
   WarpTask* const st_me = reinterpret_cast<WarpTask*>(cnt_t + 16 * Wp);
   auto st_of = [&](int t) { return reinterpret_cast<WarpTask*>(wb + t * TI + 16 * Wp); };
@@ -766,22 +802,42 @@ __global__ void __launch_bounds__(kTableWarps * 32, 1) table_hw_kernel(const Tab
     st_of(0)->npend = 0;
   }
   __syncthreads();
-  const uint4* ktab0 = reinterpret_cast<const uint4*>(A.kthr);
   const int hcap = A.hitcap / 2;  // per task
   int2* const hbw = A.hitbuf + (size_t)(blockIdx.x * kTableWarps + warp) * A.hitcap;
   int2* const hb_me = hbw + half * hcap;
   unsigned long long nfall = 0;
   const int ntask = A.ntask_dev ? *((volatile const int*)A.ntask_dev) : A.ntask;
+  // Each half-warp holds one task and its cascade level (warp-uniform
+  // copies in every lane); a free half takes the next level-0 task, a task
+  // with no hit at level l is swept again at level l + 1 by the same half.
+  int tb[2] = {-1, -1}, tl[2] = {0, 0};
+  bool drained = false;
   for (;;) {
-    int b0 = 0;
-    if (lane == 0) b0 = atomicAdd(A.work, 2);
-    b0 = __shfl_sync(kFull, b0, 0);
-    if (b0 >= ntask) break;
-    const bool live = b0 + half < ntask;
-    const int bt_me = live ? (A.task_list ? A.task_list[b0 + half] : b0 + half) : -1;
+    const int want = (tb[0] < 0 ? 1 : 0) + (tb[1] < 0 ? 1 : 0);
+    if (want && !drained) {
+      int b = 0;
+      if (lane == 0) b = atomicAdd(A.work, want);
+      b = __shfl_sync(kFull, b, 0);
+#pragma unroll
+      for (int t = 0; t < 2; ++t) {
+        if (tb[t] < 0) {
+          if (b < ntask) {
+            tb[t] = A.task_list ? A.task_list[b] : b;
+            tl[t] = 0;
+          } else {
+            drained = true;
+          }
+          ++b;
+        }
+      }
+    }
+    if (tb[0] < 0 && tb[1] < 0) break;
+    const int bt_me = half ? tb[1] : tb[0];
+    const int lv_me = half ? tl[1] : tl[0];
+    const bool live = bt_me >= 0;
     const int* const x32 = reinterpret_cast<const int*>(A.X + (long long)(live ? bt_me : 0) * A.xstride);
     if (h == 0) {
-      st_me->B = A.tau;
+      st_me->B = sLvTau[lv_me][0];
       st_me->B_valid = 0;
       st_me->ncand = 0;
       st_me->nsurv = 0;
@@ -805,7 +861,7 @@ __global__ void __launch_bounds__(kTableWarps * 32, 1) table_hw_kernel(const Tab
     }
     bool anyhits[2] = {false, false};
     int cur_tight[2] = {-1, -1};  // the table each task's rows are compared with (uniform)
-    const uint4* ktab_me = ktab0;
+    const uint4* ktab_me = reinterpret_cast<const uint4*>(sLvTab[lv_me][0]);
     auto add_lab = [&](int lab) {
       const uint32_t v = sLut[lab];
       atomicAdd(reinterpret_cast<uint32_t*>(reinterpret_cast<unsigned char*>(cnt_t) + (v & 0x7FFFu)),
@@ -821,7 +877,13 @@ __global__ void __launch_bounds__(kTableWarps * 32, 1) table_hw_kernel(const Tab
       const int pos = atomicAdd(&st_me->nhits, 1);
       if (pos < hcap) hb_me[pos] = make_int2((i << 16) | (h * C2 + col), k);
     };
-    for (int i = 0; i < n1; ++i) {
+    // The row loop breaks out every fourth row when a task needs an early
+    // resolve, resolves after it and resumes at the next row: the resolve
+    // code stays out of the loop's body.
+    int i = 0;
+    for (;;) {
+    bool resolve_now = false;
+    for (; i < n1; ++i) {
       const int c0 = w0, c1 = w1;
       const int sN = e;
       const int eN = (i + 2 <= n1) ? sRow[i + 2] : e;
@@ -910,59 +972,80 @@ __global__ void __launch_bounds__(kTableWarps * 32, 1) table_hw_kernel(const Tab
       }
       // the next row's counter updates wait for every lane's reads of this row
       __syncwarp();
+      s = sN;
+      e = eN;
       // every fourth row: could a task's buffer overflow within the next four
       // rows, or has it gathered kEarlyHits hits while a tighter table is
-      // left?  Then resolve what it holds; the bound B it sets lets its
-      // remaining rows be compared with the tightest table whose bound is
-      // still >= B (every cell with ln p <= B stays a hit).
+      // left?  Then resolve what it holds (below); the bound B it sets lets
+      // its remaining rows be compared with the tightest table whose bound
+      // is still >= B (every cell with ln p <= B stays a hit).
       if ((i & 3) == 3) {
+        bool need = false;
 #pragma unroll
         for (int t = 0; t < 2; ++t) {
           const int nh = st_of(t)->nhits;
-          if (nh > hcap - 4 * 16 * C2 || (cur_tight[t] + 1 < A.ntight && nh >= kEarlyHits)) {
-            table_resolve(A, g, hw_warp_mem(wb, C2, t), lane, hbw + t * hcap, min(nh, hcap));
-            anyhits[t] = true;
-            __syncwarp();
-            if (lane == 0) st_of(t)->nhits = 0;
-            if (st_of(t)->B_valid) {
-              const int B = st_of(t)->B;
-              for (int q = A.ntight - 1; q > cur_tight[t]; --q) {
-                if (tight_tau_of(A, q) >= B) {
-                  cur_tight[t] = q;
-                  break;
-                }
-              }
+          need = need || nh > hcap - 4 * 16 * C2 || (cur_tight[t] + 1 < sLvNtight[tl[t]] && nh >= kEarlyHits);
+        }
+        if (need) {
+          ++i;
+          resolve_now = true;
+          break;
+        }
+      }
+    }
+    if (!resolve_now) break;
+#pragma unroll
+    for (int t = 0; t < 2; ++t) {
+      const int nh = st_of(t)->nhits;
+      if (nh > hcap - 4 * 16 * C2 || (cur_tight[t] + 1 < sLvNtight[tl[t]] && nh >= kEarlyHits)) {
+        table_resolve(A, g, hw_warp_mem(wb, C2, t), lane, hbw + t * hcap, min(nh, hcap));
+        anyhits[t] = true;
+        __syncwarp();
+        if (lane == 0) st_of(t)->nhits = 0;
+        if (st_of(t)->B_valid) {
+          const int B = st_of(t)->B;
+          for (int q = sLvNtight[tl[t]] - 1; q > cur_tight[t]; --q) {
+            if (sLvTau[tl[t]][1 + q] >= B) {
+              cur_tight[t] = q;
+              break;
             }
-            __syncwarp();
           }
         }
-        const int ct = half ? cur_tight[1] : cur_tight[0];
-        ktab_me = ct < 0 ? ktab0 : reinterpret_cast<const uint4*>(tight_of(A, ct));
+        __syncwarp();
       }
-      s = sN;
-      e = eN;
+    }
+    const int ct = half ? cur_tight[1] : cur_tight[0];
+    ktab_me = reinterpret_cast<const uint4*>(sLvTab[lv_me][1 + ct]);  // ct = -1: the level's own table
     }
     __syncwarp();
 #pragma unroll
     for (int t = 0; t < 2; ++t) {
-      if (b0 + t >= ntask) continue;
-      const int bt = A.task_list ? A.task_list[b0 + t] : b0 + t;
+      if (tb[t] < 0) continue;
+      const int bt = tb[t];
+      const int route = A.route + tl[t];  // DTO_ROUTE_LEVEL0 + level
       const TableWarpMem mt = hw_warp_mem(wb, C2, t);
       const int nh = min(mt.st->nhits, hcap);
       if (nh > 0) table_resolve(A, g, mt, lane, hbw + t * hcap, nh);
       if ((nh > 0 || anyhits[t]) && mt.st->B_valid) {
         if (isinf(mt.st->bp)) {
           // no FP64 tail evaluated yet for this task: queue its survivors
-          table_defer(A, g, mt, lane, bt);
+          table_defer(A, g, mt, lane, bt, route);
         } else {
           table_refine(A, g, mt, lane);
-          if (lane == 0) A.out[bt] = TaskResult{mt.st->bp, mt.st->bi, mt.st->bj, mt.st->bk, A.route};
+          if (lane == 0) A.out[bt] = TaskResult{mt.st->bp, mt.st->bi, mt.st->bj, mt.st->bk, route};
         }
+        tb[t] = -1;
       } else {
-        // no cell reaches the guess: the next level (or the exhaustive
-        // screen) takes the task
-        if (lane == 0) A.fallback[atomicAdd(A.nfallback, 1)] = bt;
+        // no cell reaches the level's bound: the next level takes the task
+        // in this half-warp's next sweep, or after the last level the
+        // exhaustive screen
         ++nfall;
+        if (tl[t] + 1 < A.nlev) {
+          tl[t] += 1;
+        } else {
+          if (lane == 0) A.fallback[atomicAdd(A.nfallback, 1)] = bt;
+          tb[t] = -1;
+        }
       }
       __syncwarp();
     }
