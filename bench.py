@@ -43,10 +43,11 @@ METRIC = "perms/s on 1 GB300 at N=20k (FP32-screen vs plain FP64, same argmin); 
 N_FEATURES = 20000
 RHO = 0.2
 PERMS_PER_STEP = 100000
-# DRAM bytes per task of the level-0 table sweep at N = 20,000, from an ncu
-# capture of one level-0 launch (dram__bytes_read.sum + dram__bytes_write.sum
-# over its tasks): labels read once, hit buffer written and re-read.
-SWEEP0_DRAM_BYTES_PER_TASK = 43100.0
+# DRAM bytes per permutation of the table sweep at N = 20,000, from an ncu
+# capture of one launch (dram__bytes_read.sum + dram__bytes_write.sum over its
+# permutations, levels 1 and 2 of the ones that cascade included): labels read
+# once (again by a cascading task), hit buffer written and re-read.
+SWEEP0_DRAM_BYTES_PER_TASK = 48500.0
 WORKLOAD = ("single pair, N=20000 features, list 2 Gaussian copula rho=0.2 to list 1, no ties, "
             "100000 on-device Philox permutations per step + the unpermuted task, "
             "FP32 screen + FP64 refine")
@@ -442,7 +443,8 @@ def run_gpu(args):
     roofline = {"bound": "fp32", "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
                 "frac": (achieved / fp32_peak) if (fp32_peak and achieved) else None,
                 "traffic": traffic,
-                "kernel": "table_grid_kernel<%d, packed> level-0 sweep (main stream)" % (20 if cells == 589 * 589 else 0),
+                "kernel": "table_hw_kernel<40>: the table sweep, level 0 with levels 1 and 2 cascaded in the "
+                          "same launch (main stream)",
                 "work_per_task": "8 FP32-class ops x %d cells (the nine-term log-pmf sum per cell)" % cells,
                 "launch_ms": s0_ms / s0_launches if s0_launches else None,
                 "tasks_per_launch": s0_tasks / s0_launches if s0_launches else None,
