@@ -309,7 +309,6 @@ __device__ __forceinline__ void sweep(const int16_t* __restrict__ x, const int* 
 
 template <int C>
 __global__ void __launch_bounds__(kGridWarps * 32, 1) grid_kernel(const GridArgs A) {
-  constexpr int Cp = C | 1;
   constexpr int kCntInts = grid_cnt_ints(C);
   constexpr int kWarpInts = grid_warp_ints(C);
   extern __shared__ __align__(16) unsigned char smem_raw[];

@@ -109,10 +109,7 @@ struct Lane {
   // draws the next batch's labels while the side stream still resolves the
   // batch before last (its later levels get SMs only as the level-0 sweep
   // on the main stream lets go of them).
-#ifndef DTO_SLOTS
-#define DTO_SLOTS 3
-#endif
-  static constexpr int kSlots = DTO_SLOTS;
+  static constexpr int kSlots = 3;
   static_assert(kSlots >= 2 && kSlots <= kSlotsMax, "two to four batch slots");
   BatchSlot slot[kSlots];
   // table screens of the pair this lane last ran: the ladder's levels 0..2,

@@ -5,10 +5,7 @@
 
 namespace dto {
 
-#ifndef DTO_GRID_WARPS
-#define DTO_GRID_WARPS 12
-#endif
-constexpr int kGridWarps = DTO_GRID_WARPS;  // warps per CTA of the grid kernel (one task per warp)
+constexpr int kGridWarps = 12;       // warps per CTA of the grid kernel (one task per warp)
 constexpr int kCandCap = 64;         // per-warp candidate buffer of the screen
 constexpr int kBucketBits = 12;
 constexpr int kBuckets = 1 << kBucketBits;  // Rao-Sandelius buckets
@@ -121,24 +118,15 @@ struct ComposeArgs {
 // registers, which keeps the row sweep free of register spills; at 2 CTAs
 // (64 registers) spilled state reloads from L2 inside the sweep and the
 // kernel runs about 25 % slower.
-#ifndef DTO_TABLE_WARPS
-#define DTO_TABLE_WARPS 16
-#endif
-#ifndef DTO_TABLE_MINB
-#define DTO_TABLE_MINB 1
-#endif
-constexpr int kTableWarps = DTO_TABLE_WARPS;
-constexpr int kTableCtasPerSm = DTO_TABLE_MINB;
-// Tasks one warp of the table screen sweeps side by side (sharing the
+constexpr int kTableWarps = 16;
+constexpr int kTableCtasPerSm = 1;
+// Tasks one warp of the 32-bit table sweep runs side by side (sharing the
 // table-row loads and the loop control, interleaving their dependent
 // instruction chains).  Two measured slower than one at N = 20,000 (1.72 M
 // against 2.04 M permutations/s: the two tasks' state does not fit 128
-// registers without spilling), so one is the default.  Each task has
-// kTableHitCap hit slots.
-#ifndef DTO_TABLE_TASKS
-#define DTO_TABLE_TASKS 1
-#endif
-constexpr int kTableTasks = DTO_TABLE_TASKS;
+// registers without spilling); the half-warp packed sweep is the layout that
+// does run two tasks per warp.  Each task has kTableHitCap hit slots.
+constexpr int kTableTasks = 1;
 static_assert(kTableTasks == 1 || kTableTasks == 2, "one or two tasks per warp");
 constexpr int kTableHitCap = 8192;  // hit slots per task
 // hit slots per warp of a table sweep (the half-warp sweep runs two tasks)
@@ -147,10 +135,7 @@ constexpr int kTableWarpHits = 2 * kTableHitCap;
 // The packed table sweep holds overlaps in 16-bit halves and tests
 // k >= kthr as the sign bit of k + (0x8000 - kthr): it needs every overlap,
 // hence the number of features the two lists share, to be <= 0x7FFF.
-#ifndef DTO_TABLE_PACKED
-#define DTO_TABLE_PACKED 1
-#endif
-constexpr long long kPackedMaxCommon = DTO_TABLE_PACKED ? 0x7FFF : -1;
+constexpr long long kPackedMaxCommon = 0x7FFF;
 
 struct TableArgs {
   int n1, n2, N, C;      // C: columns per lane

@@ -20,59 +20,37 @@
 namespace dto {
 
 // Quantile of a sample of minimum p-values (a run's first batch, or the
-// pair's previous run) that sets the level-0 table.
-#ifndef DTO_L0_QUANTILE
-#define DTO_L0_QUANTILE 0.90
-#endif
-constexpr double kLevel0Quantile = DTO_L0_QUANTILE;
+// pair's previous run) that sets the level-0 table.  With the later levels
+// cascaded in the same sweep, 100,000 permutations measured (N = 20,000 /
+// 6,000): 0.75 -> 24.2 / 14.4 ms, 0.80 -> 23.8 / 14.2, 0.85 -> 23.7 / 14.5,
+// 0.90 -> 23.9 / 15.3, 0.95 -> 26.8 / 18.1.
+constexpr double kLevel0Quantile = 0.85;
 // Permutations of the first batch, whose minimum p-values set the ladder
 // (cold runs at 100,000 permutations, N = 20,000: 256 -> 47.8 ms, 512 -> 46.9,
 // 1,024 -> 49.3; its slowest tasks and its size both delay the pipeline).
-#ifndef DTO_FIRST_BATCH
-#define DTO_FIRST_BATCH 512
-#endif
-constexpr long long kFirstBatch = DTO_FIRST_BATCH;
-// Levels of the table ladder: 3 (90th, 99th percentile, maximum + 1 nat) or
-// 2 (90th percentile, maximum + 1 nat).
-#ifndef DTO_LADDER_LEVELS
-#define DTO_LADDER_LEVELS 3
-#endif
-constexpr int kLadderLevels = DTO_LADDER_LEVELS;
-static_assert(kLadderLevels == 2 || kLadderLevels == 3, "two or three table levels");
-// Tighter tables a sweep may switch to (0 to 3), for the levels below
-// kTightLevels.
-#ifndef DTO_TIGHT_TABLES
-#define DTO_TIGHT_TABLES 3
-#endif
-constexpr int kTightTables = DTO_TIGHT_TABLES;
+constexpr long long kFirstBatch = 512;
+// Levels of the table ladder: the level-0 quantile, the 99th percentile and
+// the maximum + 1 nat (a two-level ladder measured much slower).
+constexpr int kLadderLevels = 3;
+// Tighter tables a sweep may switch to, for the levels below kTightLevels.
+constexpr int kTightTables = 3;
 static_assert(kTightTables >= 0 && kTightTables <= 3, "at most three tighter tables");
-#ifndef DTO_TIGHT_LEVELS
-#define DTO_TIGHT_LEVELS 3
-#endif
-constexpr int kTightLevels = DTO_TIGHT_LEVELS;
+constexpr int kTightLevels = 3;
 // The first batch's screen with a CTA per task (see grid_kernel).
-#ifndef DTO_FIRST_COOP
-#define DTO_FIRST_COOP 1
-#endif
-constexpr bool kFirstBatchCoop = DTO_FIRST_COOP != 0;
-#ifndef DTO_SIDE_PRIORITY
-#define DTO_SIDE_PRIORITY 0
-#endif
-constexpr bool kSidePriority = DTO_SIDE_PRIORITY != 0;
-// Table levels of the last pipelined batch before its exhaustive screen
-// (a CTA per task).  Nothing runs beside that batch's later levels, but the
-// table sweeps still beat the exhaustive screen on its hardest tasks: 3
+constexpr bool kFirstBatchCoop = true;
+// Table levels of the last pipelined batch of the 32-bit sweep (whose levels
+// run as separate launches) before its exhaustive screen (a CTA per task):
+// the table sweeps still beat the exhaustive screen on the hardest tasks (3
 // levels measured 36.9 ms per 100,000 permutations at N = 20,000, 2 levels
-// 38.7 ms, 1 level 44.6 ms.
-#ifndef DTO_LAST_LEVELS
-#define DTO_LAST_LEVELS 3
-#endif
-constexpr int kLastLevels = DTO_LAST_LEVELS;
+// 38.7 ms, 1 level 44.6 ms).
+constexpr int kLastLevels = 3;
 // How far (in nats of ln p) a run's ladder bound may lie from the pair's
 // stored one before it replaces it.
 constexpr double kLadderSlack = 0.25;
-// Runs shorter than this build the tighter tables of level 0 only: the
-// later levels of a short run see too few tasks to repay six more builds.
+// Runs shorter than this build no tighter tables: a short run (most pairs of
+// a batch, most served requests) does not repay their builds (the 512-pair
+// batch of 10,000 permutations each: 3.00 M perms/s with level 0's three,
+// 3.12 M without).
 constexpr long long kTightAllMin = 32768;
 
 int set_err(dto_ctx* ctx, int code, const std::string& msg) {
@@ -130,14 +108,14 @@ int lane_create(dto_ctx* ctx, Lane** out, std::string* err_sink) {
   };
   cudaError_t e;
   if ((e = cudaStreamCreateWithFlags(&L->stream, cudaStreamNonBlocking)) != cudaSuccess) return fail(e, "stream");
-  // The side stream runs the later table levels and the fallbacks of a batch
-  // while the main stream sweeps the next one.  With DTO_SIDE_PRIORITY its
-  // CTAs go first whenever SMs free up (the level-0 sweep is a persistent
-  // kernel that keeps its SMs until its queue drains); measured neutral at
-  // N = 20,000 (the side levels finish sooner, the next labels later), so off.
+  // The side stream runs the fallbacks (and, for the 32-bit sweep, the later
+  // table levels) of a batch while the main stream sweeps the next one, at
+  // the lowest priority: the highest, which lets its CTAs go first whenever
+  // SMs free up, measured neutral at N = 20,000 (the side levels finished
+  // sooner, the next labels later).
   int prio_least = 0, prio_greatest = 0;
   if ((e = cudaDeviceGetStreamPriorityRange(&prio_least, &prio_greatest)) != cudaSuccess) return fail(e, "stream");
-  if ((e = cudaStreamCreateWithPriority(&L->side, cudaStreamNonBlocking, kSidePriority ? prio_greatest : prio_least)) !=
+  if ((e = cudaStreamCreateWithPriority(&L->side, cudaStreamNonBlocking, prio_least)) !=
       cudaSuccess)
     return fail(e, "stream");
   if ((e = cudaEventCreateWithFlags(&L->evSide, cudaEventDisableTiming)) != cudaSuccess) return fail(e, "event");
@@ -220,19 +198,17 @@ void fill_result(const dto_pair* P, const TaskResult& r, int permuted, dto_resul
   o->reserved = 0;
 }
 
-// Batch size of a run: 2^DTO_BATCH_SHIFT bytes of labels (2 GiB), and at
+// Batch size of a run: 2^31 bytes of labels (2 GiB), and at
 // most 1 GiB of index scratch for test mode and for pairs whose lists hold
-// different features.  Every batch's later levels pay a latency floor (their
-// slowest tasks), so fewer, larger batches win: per 100,000 permutations
-// 2 GiB measured 36.2 ms at N = 20,000 and 39.6 ms on the 18,000-feature
-// background pair, 1 GiB 36.2-36.8 and 43.1 ms, 512 MiB 40-41 ms and 46 ms.
-#ifndef DTO_BATCH_SHIFT
-#define DTO_BATCH_SHIFT 31
-#endif
+// different features.  Every launch pays a tail (its slowest tasks), so
+// fewer, larger batches win: per 100,000 permutations 2 GiB measured 36.2 ms
+// at N = 20,000 and 39.6 ms on the 18,000-feature background pair, 1 GiB
+// 36.2-36.8 and 43.1 ms, 512 MiB 40-41 ms and 46 ms (before the cascade).
+
 long long batch_of(const dto_pair* P, int64_t n_perm, bool test_mode) {
   const long long xs = xstride_of(P->N1);
   const long long L12 = P->N1 + P->N2;
-  long long batch = std::max(1LL, std::min<long long>((1LL << DTO_BATCH_SHIFT) / (xs * 2), 1LL << 20));
+  long long batch = std::max(1LL, std::min<long long>((1LL << 31) / (xs * 2), 1LL << 20));
   if (test_mode || !P->same_set) batch = std::min(batch, std::max(1LL, (1LL << 30) / (L12 * 4)));
   return std::min<long long>(batch, std::max<long long>(n_perm, 1));
 }
@@ -572,7 +548,7 @@ int make_labels_launch(Lane* L, dto_pair* P, uint64_t seed, uint32_t first, int 
 }
 
 // Bounds of the table levels from a sample of minimum p-values: the
-// 90th percentile (level 0), the 99th (level 1), one nat above the maximum
+// kLevel0Quantile quantile (level 0), the 99th percentile (level 1), one nat above the maximum
 // (level 2), as fixed-point ln p, each above the one before; then each
 // level's three tighter tables (kLadderTaus entries in all).
 // The ladder's order: each level's bound above the one before, each level's
@@ -852,7 +828,7 @@ int lane_run_range(Lane* L, dto_pair* P, uint32_t perm_first, int64_t n_perm, ui
     // sweep needs them), the later levels' on the side stream behind the
     // first batch (their first sweeps come a level-0 sweep later; each
     // slot's side stream waits for them).
-    const int tight_levels = std::min(n_perm >= kTightAllMin ? kTightLevels : 1, kLadderLevels);
+    const int tight_levels = std::min(n_perm >= kTightAllMin ? kTightLevels : 0, kLadderLevels);
     // packed pairs sweep all levels in one cascade launch on the main stream,
     // which needs every level's tables first
     const bool cascade = P->ncommon <= kPackedMaxCommon;
