@@ -404,6 +404,7 @@ int dto_pair_create(dto_ctx* ctx, const uint32_t* ranks1, const int32_t* feat1, 
 int dto_pair_destroy(dto_pair* P) {
   if (!P) return DTO_ERR_INVALID;
   cudaFree(P->dBase);
+  for (uint16_t* t : P->dWaveKthr) cudaFree(t);
   delete P;
   return DTO_OK;
 }

@@ -120,6 +120,25 @@ struct Lane {
   size_t kthrBytes[kTables] = {};
   unsigned long long kthr_pair[kTables] = {};  // pair serial the table was built for (0: none)
   int kthr_tau[kTables] = {};
+  // dto_batch_run's waves (lane_wave), two in flight: labels, results,
+  // fallback lists and counters, and the segment arguments of the
+  // multi-pair sweep
+  struct WaveBuf {
+    void* dX = nullptr;
+    size_t xBytes = 0;
+    void* dRes = nullptr;
+    size_t resBytes = 0;
+    void* hRes = nullptr;  // pinned
+    size_t hResBytes = 0;
+    void* dAux = nullptr;
+    size_t auxBytes = 0;
+    void* dSegs = nullptr;
+    size_t segsBytes = 0;
+    void* hSegs = nullptr;  // pinned
+    size_t hSegsBytes = 0;
+    cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};  // start, labels done, sweep done, end
+  };
+  WaveBuf wave[2];
 };
 
 // Ladders of the pairs a context has run, by shape, in nats of ln p.  The
@@ -192,6 +211,12 @@ struct dto_pair {
   std::mutex ladder_mu;
   bool ladder_ok = false;
   int ladder_tau[dto::kLadderTaus] = {};
+  // The table screens of levels 0..2 that dto_batch_run's waves built for
+  // this pair, kept with it (a wave sweeps several pairs at once, so each
+  // needs its own; the next batch finds them).  Guarded by the context mutex.
+  uint16_t* dWaveKthr[3] = {};
+  int wave_tau[3] = {};
+  bool wave_ok[3] = {};
 };
 
 namespace dto {
@@ -240,6 +265,40 @@ int lane_run_range(Lane* L, dto_pair* P, uint32_t perm_first, int64_t n_perm, ui
 // The table ladder's bounds (fixed-point ln p, kLadderTaus of them) from a
 // sample of minimum p-values, in ladder order.
 void ladder_of(const std::vector<double>& all, int fshift, int tau[kLadderTaus]);
+void ladder_order(int tau[kLadderTaus]);
+LadderShape shape_of(const dto_pair* P);
+// A run's ladder after it: bounds that moved by more than the slack replace
+// the pair's, and the context's model records the pair's shape.
+void ladder_update(dto_ctx* ctx, dto_pair* P, const std::vector<double>& minp);
+// Labels of `count` permutations from perm id `first` (or of uploaded index
+// rows dIdx) into X (row stride xs) on the lane's main stream.
+int make_labels_launch(Lane* L, dto_pair* P, uint64_t seed, uint32_t first, int count, const int32_t* dIdx,
+                       int16_t* X, long long xs);
+// The exhaustive screen of what the last table level left, on `stream`.
+int table_exhaustive(Lane* L, dto_pair* P, const int16_t* X, long long xstride, int ntask, TaskResult* dOut,
+                     int nlev, const int* fall, int* cnts, cudaStream_t stream,
+                     unsigned long long* refined = nullptr);
+
+// One pair's run inside a wave of dto_batch_run.
+struct WaveJob {
+  dto_pair* P = nullptr;
+  int64_t n_perm = 0;
+  uint64_t seed = 0;
+  dto_result* out_unpermuted = nullptr;
+  double* out_minp = nullptr;  // nullable
+  dto_summary* out_summary = nullptr;  // nullable
+  int tau[3] = {};  // the levels' bounds (set by lane_wave)
+};
+// Runs that a wave takes: the screen, lists over one feature set sharing at
+// most 0x7FFF features (the packed sweep), kWaveMinPerm..kWaveMaxPerm
+// permutations, and a ladder (the pair's own, or the context's model's).
+bool wave_eligible(dto_ctx* ctx, dto_pair* P, int64_t n_perm, int precision);
+// The runs of `jobs` (all eligible, permutation ids 1..n_perm) in waves: per
+// wave the pairs' labels, then one cascade sweep over all their tasks, then
+// their exhaustive fallbacks; each pair's unpermuted task through the
+// exhaustive screen on the side stream.  The results equal lane_run_range's
+// bit for bit.  Returns the first failure.
+int lane_wave(Lane* L, std::vector<WaveJob>& jobs);
 
 // Bytes of device scratch a run of the pair holds at its peak (labels of the
 // batches in flight, results, hit buffers, table screens).

@@ -185,6 +185,11 @@ struct TableGridArgs {
   const int* ntask_dev;   // nullable: the task count, read on the device
   int2* hitbuf;           // [gridDim.x * kTableWarps][hitcap] hits (packed cell, overlap)
   int hitcap;
+  // nullable: a cascade sweep over several packed pairs of the same C, one
+  // TableGridArgs per pair (segment, in device memory); the launch's own
+  // fields then give only C, hitbuf and hitcap
+  const TableGridArgs* segs;
+  int nseg;
 };
 
 // Raises a kernel's dynamic shared-memory limit to at least `bytes` on the

@@ -136,6 +136,16 @@ void lane_destroy(Lane* L) {
   if (L->stream) cudaStreamSynchronize(L->stream);
   if (L->side) cudaStreamSynchronize(L->side);
   cudaFree(L->dX);
+  for (Lane::WaveBuf& wb : L->wave) {
+    cudaFree(wb.dX);
+    cudaFree(wb.dRes);
+    cudaFreeHost(wb.hRes);
+    cudaFree(wb.dAux);
+    cudaFree(wb.dSegs);
+    cudaFreeHost(wb.hSegs);
+    for (cudaEvent_t e : wb.ev)
+      if (e) cudaEventDestroy(e);
+  }
   cudaFree(L->dSig);
   cudaFree(L->dRes);
   cudaFreeHost(L->hRes);
@@ -388,7 +398,7 @@ int table_levels(Lane* L, dto_pair* P, const int16_t* X, long long xstride, int 
 
 // The exhaustive screen of what the last table level left, on `stream`.
 int table_exhaustive(Lane* L, dto_pair* P, const int16_t* X, long long xstride, int ntask, TaskResult* dOut,
-                     int nlev, const int* fall, int* cnts, cudaStream_t stream) {
+                     int nlev, const int* fall, int* cnts, cudaStream_t stream, unsigned long long* refined) {
   NvtxRange range("dto: exhaustive fallback");
   const int cap = std::max(ntask, 1);
   GridArgs g{};
@@ -403,7 +413,7 @@ int table_exhaustive(Lane* L, dto_pair* P, const int16_t* X, long long xstride, 
   g.coop = 1;  // the few tasks left here are the hard ones: a CTA each
   g.out = dOut;
   g.work = cnts + nlev;
-  g.n_refined = L->dRefined;
+  g.n_refined = refined ? refined : L->dRefined;
   g.task_list = fall + (size_t)(nlev - 1) * cap;
   g.ntask_dev = cnts + 8 + nlev - 1;
   LCK(launch_grid(g, L->ctx->nsm, stream));
@@ -449,7 +459,7 @@ bool LadderModel::lookup(const LadderShape& want, double nats[kLadderTaus]) {
   return true;
 }
 
-static LadderShape shape_of(const dto_pair* P) {
+LadderShape shape_of(const dto_pair* P) {
   LadderShape x{};
   x.npop = P->npop;
   x.N1 = P->N1;
@@ -592,6 +602,20 @@ void ladder_of(const std::vector<double>& all, int fshift, int tau[kLadderTaus])
   for (int l = 0; l < 3; ++l)
     for (int t = 0; t < 3; ++t) tau[tight_slot(l, t)] = fixed_log(ptight[l][t], fshift);
   ladder_order(tau);
+}
+
+void ladder_update(dto_ctx* ctx, dto_pair* P, const std::vector<double>& minp) {
+  int t[kLadderTaus];
+  ladder_of(minp, P->fshift, t);
+  const long long slack = (long long)std::ldexp(kLadderSlack, P->fshift);
+  std::lock_guard<std::mutex> g(P->ladder_mu);
+  for (int l = 0; l < kLadderTaus; ++l)
+    if (!P->ladder_ok || std::llabs((long long)t[l] - P->ladder_tau[l]) > slack) P->ladder_tau[l] = t[l];
+  ladder_order(P->ladder_tau);
+  P->ladder_ok = true;
+  LadderShape x = shape_of(P);
+  for (int l = 0; l < kLadderTaus; ++l) x.nats[l] = std::ldexp((double)P->ladder_tau[l], -P->fshift);
+  ctx->ladders.record(x);
 }
 
 int lane_run_range(Lane* L, dto_pair* P, uint32_t perm_first, int64_t n_perm, uint64_t seed,
@@ -927,19 +951,7 @@ int lane_run_range(Lane* L, dto_pair* P, uint32_t perm_first, int64_t n_perm, ui
     // by more than kLadderSlack nats, which spares the next run the rebuild
     // of that table screen (they are screens: any bounds give the same
     // results).
-    {
-      int t[kLadderTaus];
-      ladder_of(minp, P->fshift, t);
-      const long long slack = (long long)std::ldexp(kLadderSlack, P->fshift);
-      std::lock_guard<std::mutex> g(P->ladder_mu);
-      for (int l = 0; l < kLadderTaus; ++l)
-        if (!P->ladder_ok || std::llabs((long long)t[l] - P->ladder_tau[l]) > slack) P->ladder_tau[l] = t[l];
-      ladder_order(P->ladder_tau);
-      P->ladder_ok = true;
-      LadderShape x = shape_of(P);
-      for (int l = 0; l < kLadderTaus; ++l) x.nats[l] = std::ldexp((double)P->ladder_tau[l], -P->fshift);
-      L->ctx->ladders.record(x);
-    }
+    ladder_update(L->ctx, P, minp);
     // the main stream's timing event follows the side streams' last work
     LCK(cudaEventRecord(L->evSide, L->side));
     LCK(cudaStreamWaitEvent(L->stream, L->evSide, 0));

@@ -302,12 +302,33 @@ int dto_batch_run(dto_ctx* ctx, int npairs, dto_pair* const* pairs, const int64_
   if (!ctx || npairs < 0 || (npairs > 0 && (!pairs || !n_perm || !seeds || !out_unpermuted)))
     return set_err(ctx, DTO_ERR_INVALID, "dto_batch_run: null argument");
   if (npairs == 0) return DTO_OK;
+  // Runs that a wave takes (dto_wave.cpp: short screen runs of pairs with a
+  // ladder) go through waves on the context's own lane in this thread; the
+  // others through a server's lanes meanwhile.
+  std::vector<dto::WaveJob> wave;
+  std::vector<char> in_wave((size_t)npairs, 0);
+  for (int q = 0; q < npairs; ++q) {
+    if (!dto::wave_eligible(ctx, pairs[q], n_perm[q], precision)) continue;
+    dto::WaveJob j;
+    j.P = pairs[q];
+    j.n_perm = n_perm[q];
+    j.seed = seeds[q];
+    j.out_unpermuted = &out_unpermuted[q];
+    j.out_minp = out_minp ? out_minp[q] : nullptr;
+    j.out_summary = out_summary ? &out_summary[q] : nullptr;
+    wave.push_back(j);
+    in_wave[(size_t)q] = 1;
+  }
   dto_server* s = nullptr;
-  int rc = dto_serve_create(ctx, lanes > 0 ? lanes : 4, 0, &s);
-  if (rc) return rc;
+  int rc = DTO_OK;
+  if (wave.size() < (size_t)npairs) {
+    rc = dto_serve_create(ctx, lanes > 0 ? lanes : 4, 0, &s);
+    if (rc) return rc;
+  }
   std::vector<dto_job> ids((size_t)npairs, 0);
   int first_bad = DTO_OK;
-  for (int q = 0; q < npairs; ++q) {
+  for (int q = 0; q < npairs && s; ++q) {
+    if (in_wave[(size_t)q]) continue;
     rc = dto_serve_submit(s, pairs[q], 1u, n_perm[q], seeds[q], precision, &out_unpermuted[q],
                           out_minp ? out_minp[q] : nullptr, out_summary ? &out_summary[q] : nullptr, &ids[(size_t)q]);
     if (rc) {
@@ -316,7 +337,20 @@ int dto_batch_run(dto_ctx* ctx, int npairs, dto_pair* const* pairs, const int64_
       break;
     }
   }
-  for (int q = 0; q < npairs; ++q) {
+  if (!wave.empty() && !first_bad) {
+    std::lock_guard<std::mutex> g(ctx->mu);
+    dto::Lane* L = ctx->lane0;
+    std::string err;
+    std::string* prev = L->err;
+    L->err = &err;
+    rc = dto::lane_wave(L, wave);
+    L->err = prev;
+    if (rc) {
+      ctx->err = "dto_batch_run: " + err;
+      first_bad = rc;
+    }
+  }
+  for (int q = 0; q < npairs && s; ++q) {
     if (!ids[(size_t)q]) continue;
     rc = dto_serve_wait(s, ids[(size_t)q], nullptr, nullptr);
     if (rc && !first_bad) {
@@ -324,7 +358,7 @@ int dto_batch_run(dto_ctx* ctx, int npairs, dto_pair* const* pairs, const int64_
       first_bad = rc;
     }
   }
-  dto_serve_destroy(s);
+  if (s) dto_serve_destroy(s);
   return first_bad;
 }
 

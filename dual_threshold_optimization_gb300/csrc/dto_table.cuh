@@ -742,8 +742,14 @@ __device__ __forceinline__ TableWarpMem hw_warp_mem(int* base, int C2, int t) {
   return m;
 }
 
-template <int C2>
-__global__ void __launch_bounds__(kTableWarps * 32, 1) table_hw_kernel(const TableGridArgs A) {
+// Multi: the launch sweeps the tasks of several pairs (segments; Ain.segs
+// holds one TableGridArgs per pair, all of the same C).  A warp works through
+// the segments in order, both its half-warps on tasks of one segment, with
+// that segment's arguments copied to shared memory; the pairs' tables (row
+// bounds, set sizes, ln m!) are read from global memory.  A segment's tail
+// is filled by the warps that have moved on to the next.
+template <int C2, bool Multi>
+__global__ void __launch_bounds__(kTableWarps * 32, 1) table_hw_kernel(const TableGridArgs Ain) {
   constexpr int C = C2 / 2;        // columns per lane of the 32-lane label encoding
   constexpr int Cp = C | 1;
   constexpr int NQ = hw_cq(C2) / 8;  // 16-byte table chunks per lane per row
@@ -756,41 +762,73 @@ __global__ void __launch_bounds__(kTableWarps * 32, 1) table_hw_kernel(const Tab
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int h = lane & 15, half = lane >> 4;
-  const int n1 = A.P.n1;
-  const int Npop = (int)A.P.Npop;
+  __shared__ TableGridArgs sSeg[Multi ? kTableWarps : 1];  // the warp's segment (Multi)
+  const TableGridArgs& A = Multi ? sSeg[warp] : Ain;
+  // one pair: its row bounds, set sizes and (where it fits) ln m! table in
+  // shared memory; Multi: none (each pair's are read from global memory)
+  const int Npop0 = (int)Ain.P.Npop;
   uint32_t* sF = reinterpret_cast<uint32_t*>(smem_raw);
-  int* sRow = reinterpret_cast<int*>(sF + (A.smemF ? ((Npop + 1 + 3) & ~3) : 0));
-  int* sNcnt = sRow + ((n1 + 1 + 3) & ~3);
-  uint16_t* sLut = reinterpret_cast<uint16_t*>(sNcnt + ((A.P.n2 + 3) & ~3));
+  int* sRow = reinterpret_cast<int*>(sF + ((!Multi && Ain.smemF) ? ((Npop0 + 1 + 3) & ~3) : 0));
+  int* sNcnt = sRow + (Multi ? 0 : ((Ain.P.n1 + 1 + 3) & ~3));
+  uint16_t* sLut = reinterpret_cast<uint16_t*>(sNcnt + (Multi ? 0 : ((Ain.P.n2 + 3) & ~3)));
   int* sWarp = reinterpret_cast<int*>(sLut + ((hw_lut_entries(C) + 7) & ~7));
   int* const wb = sWarp + warp * hw_warp_ints(C2);
-  for (int q = threadIdx.x; q <= n1; q += blockDim.x) sRow[q] = __ldg(A.P.rowstart + q);
-  for (int q = threadIdx.x; q < A.P.n2; q += blockDim.x) sNcnt[q] = __ldg(A.P.ncnt + q);
-  if (A.smemF)
-    for (int q = threadIdx.x; q <= Npop; q += blockDim.x) sF[q] = __ldg(A.P.F + q);
+  if constexpr (!Multi) {
+    for (int q = threadIdx.x; q <= Ain.P.n1; q += blockDim.x) sRow[q] = __ldg(Ain.P.rowstart + q);
+    for (int q = threadIdx.x; q < Ain.P.n2; q += blockDim.x) sNcnt[q] = __ldg(Ain.P.ncnt + q);
+    if (Ain.smemF)
+      for (int q = threadIdx.x; q <= Npop0; q += blockDim.x) sF[q] = __ldg(Ain.P.F + q);
+  }
   for (int q = threadIdx.x; q < hw_lut_entries(C); q += blockDim.x) {
     const int l = q / Cp, tcol = q - (q / Cp) * Cp;
     const int j = l * C + min(tcol, C - 1);
     const int hh = j / C2, tc2 = j - (j / C2) * C2;
     sLut[q] = (uint16_t)((4 * (hh * Wp + (tc2 >> 1))) | ((tc2 & 1) << 15));
   }
-  const TabGrid g{sRow, sNcnt, A.smemF ? sF : A.P.F};
-  // the cascade levels' tables and bounds, indexed by level from shared
-  // memory (selecting among the kernel's arguments at run time kept them
-  // all in registers and slowed the row loop by a fifth)
-  __shared__ const uint16_t* sLvTab[3][4];  // [level][0: the level's table, 1..3: its tighter tables]
-  __shared__ int sLvTau[3][4];              // [level][0: its bound, 1..3: the tighter tables' bounds]
-  __shared__ int sLvNtight[3];
-  if (threadIdx.x < 3) {
-    const int l = threadIdx.x;
-    sLvTab[l][0] = lv_kthr(A, l);
-    sLvTau[l][0] = lv_tau(A, l);
-    sLvNtight[l] = lv_ntight(A, l);
-    for (int q = 0; q < 3; ++q) {
-      sLvTab[l][1 + q] = lv_tight(A, l, q);
-      sLvTau[l][1 + q] = lv_tight_tau(A, l, q);
+  // the cascade levels' tables and bounds, per warp, indexed by level from
+  // shared memory (selecting among the kernel's arguments at run time kept
+  // them all in registers and slowed the row loop by a fifth)
+  // (one copy per CTA for one pair, per warp for several)
+  constexpr int kLv = Multi ? kTableWarps : 1;
+  __shared__ const uint16_t* sLvTabW[kLv][3][4];  // [level][0: the level's table, 1..3: its tighter tables]
+  __shared__ int sLvTauW[kLv][3][4];              // [level][0: its bound, 1..3: the tighter tables' bounds]
+  __shared__ int sLvNtightW[kLv][3];
+  const uint16_t* (*const sLvTab)[4] = sLvTabW[Multi ? warp : 0];
+  int (*const sLvTau)[4] = sLvTauW[Multi ? warp : 0];
+  int* const sLvNtight = sLvNtightW[Multi ? warp : 0];
+  // the segment-dependent state: the pair's grid rows, its tables, the task count
+  int n1 = 0, ntask = 0;
+  const int* rowp = sRow;
+  TabGrid g{sRow, sNcnt, Ain.smemF ? sF : Ain.P.F};
+  auto bind_seg = [&]() {
+    if (lane < 3 && (Multi || warp == 0)) {  // one pair: read after the barrier below
+      const int l = lane;
+      sLvTab[l][0] = lv_kthr(A, l);
+      sLvTau[l][0] = lv_tau(A, l);
+      sLvNtight[l] = lv_ntight(A, l);
+      for (int q = 0; q < 3; ++q) {
+        sLvTab[l][1 + q] = lv_tight(A, l, q);
+        sLvTau[l][1 + q] = lv_tight_tau(A, l, q);
+      }
     }
-  }
+    n1 = A.P.n1;
+    ntask = A.ntask_dev ? *((volatile const int*)A.ntask_dev) : A.ntask;
+    if constexpr (Multi) {
+      rowp = A.P.rowstart;
+      g = TabGrid{A.P.rowstart, A.P.ncnt, A.P.F};
+    }
+    __syncwarp();
+  };
+  int seg = 0;
+  auto load_seg = [&](int sgi) {  // Multi: copy segment sgi's arguments
+    __syncwarp();
+    const int* src = reinterpret_cast<const int*>(Ain.segs + sgi);
+    int* dst = reinterpret_cast<int*>(&sSeg[Multi ? warp : 0]);
+    for (int q = lane; q < (int)(sizeof(TableGridArgs) / 4); q += 32) dst[q] = __ldg(src + q);
+    __syncwarp();
+  };
+  if constexpr (Multi) load_seg(0);
+  bind_seg();
   int* const cnt_t = wb + half * TI;  // this lane's task's counters
   WarpTask* const st_me = reinterpret_cast<WarpTask*>(cnt_t + 16 * Wp);
   auto st_of = [&](int t) { return reinterpret_cast<WarpTask*>(wb + t * TI + 16 * Wp); };
@@ -800,11 +838,10 @@ __global__ void __launch_bounds__(kTableWarps * 32, 1) table_hw_kernel(const Tab
     st_of(0)->npend = 0;
   }
   __syncthreads();
-  const int hcap = A.hitcap / 2;  // per task
-  int2* const hbw = A.hitbuf + (size_t)(blockIdx.x * kTableWarps + warp) * A.hitcap;
+  const int hcap = Ain.hitcap / 2;  // per task
+  int2* const hbw = Ain.hitbuf + (size_t)(blockIdx.x * kTableWarps + warp) * Ain.hitcap;
   int2* const hb_me = hbw + half * hcap;
   unsigned long long nfall = 0;
-  const int ntask = A.ntask_dev ? *((volatile const int*)A.ntask_dev) : A.ntask;
   // Each half-warp holds one task and its cascade level (warp-uniform
   // copies in every lane); a free half takes the next level-0 task, a task
   // with no hit at level l is swept again at level l + 1 by the same half.
@@ -829,7 +866,29 @@ __global__ void __launch_bounds__(kTableWarps * 32, 1) table_hw_kernel(const Tab
         }
       }
     }
-    if (tb[0] < 0 && tb[1] < 0) break;
+    if (tb[0] < 0 && tb[1] < 0) {
+      if constexpr (Multi) {
+        if (seg + 1 < Ain.nseg) {
+          // the deferred FP64 evaluations belong to this segment's tasks
+          if (st_of(0)->npend > 0) table_pending_flush(A, g, hw_warp_mem(wb, C2, 0), lane);
+          __syncwarp();
+          // and so do the refine and fall-through counts so far
+          if (lane == 0 && A.n_refined) {
+            atomicAdd(A.n_refined, st_of(0)->n64);
+            atomicAdd(A.n_refined + 1, st_of(0)->n32);
+            atomicAdd(A.n_refined + 2, nfall);
+            st_of(0)->n64 = 0;
+            st_of(0)->n32 = 0;
+          }
+          nfall = 0;
+          load_seg(++seg);
+          bind_seg();
+          drained = false;
+          continue;
+        }
+      }
+      break;
+    }
     const int bt_me = half ? tb[1] : tb[0];
     const int lv_me = half ? tl[1] : tl[0];
     const bool live = bt_me >= 0;
@@ -850,7 +909,7 @@ __global__ void __launch_bounds__(kTableWarps * 32, 1) table_hw_kernel(const Tab
     __syncwarp();
     // labels as 32-bit words (two each), a row's words prefetched one row
     // ahead: 16 words (32 labels) per task, and 16 more for rows that long
-    int s = sRow[0], e = sRow[1];
+    int s = rowp[0], e = rowp[1];
     int w0, w1;
     {
       const int q0 = (s >> 1) + h;
@@ -884,7 +943,7 @@ __global__ void __launch_bounds__(kTableWarps * 32, 1) table_hw_kernel(const Tab
     for (; i < n1; ++i) {
       const int c0 = w0, c1 = w1;
       const int sN = e;
-      const int eN = (i + 2 <= n1) ? sRow[i + 2] : e;
+      const int eN = (i + 2 <= n1) ? rowp[i + 2] : e;
       {
         const int q0 = (sN >> 1) + h;
         w0 = (live && 2 * q0 < eN) ? __ldg(x32 + q0) : -1;
@@ -1056,11 +1115,11 @@ __global__ void __launch_bounds__(kTableWarps * 32, 1) table_hw_kernel(const Tab
   }
 }
 
-template <int C2>
+template <int C2, bool Multi>
 cudaError_t launch_table_hw_kernel(const TableGridArgs& a, int ctas, size_t smem, cudaStream_t s) {
-  cudaError_t e = raise_smem_limit((const void*)table_hw_kernel<C2>, smem);
+  cudaError_t e = raise_smem_limit((const void*)table_hw_kernel<C2, Multi>, smem);
   if (e != cudaSuccess) return e;
-  table_hw_kernel<C2><<<ctas, kTableWarps * 32, smem, s>>>(a);
+  table_hw_kernel<C2, Multi><<<ctas, kTableWarps * 32, smem, s>>>(a);
   return cudaGetLastError();
 }
 
@@ -1076,7 +1135,8 @@ cudaError_t launch_table_grid_kernel(const TableGridArgs& a, int ctas, size_t sm
 // the 32-bit sweep of table_grid_kernel.
 template <int C>
 cudaError_t launch_table_grid_impl(const TableGridArgs& a, int ctas, size_t smem, cudaStream_t s) {
-  return a.packed ? launch_table_hw_kernel<2 * C>(a, ctas, smem, s)
+  if (a.segs) return launch_table_hw_kernel<2 * C, true>(a, ctas, smem, s);
+  return a.packed ? launch_table_hw_kernel<2 * C, false>(a, ctas, smem, s)
                   : launch_table_grid_kernel<C, false>(a, ctas, smem, s);
 }
 

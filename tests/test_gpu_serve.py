@@ -69,6 +69,49 @@ def test_batch_run_equals_single_runs(engine):
         dp.close()
 
 
+def test_batch_waves_equal_single_runs(engine):
+    # Pairs that have run before (so they have a ladder) and short screen
+    # runs go through waves: the tasks of several pairs in one multi-pair
+    # sweep, grouped by grid width.  Each pair's results equal its own run's
+    # bit for bit; the same pair twice (other seeds) shares its table
+    # screens; the long run, the run of lists over different features and the
+    # short one take a server lane beside the waves.
+    specs = [(synth.copula_pair(2000, 0.1, seed=90), 2500, 21),
+             (synth.copula_pair(9000, 0.3, seed=91), 4000, 22),
+             (synth.copula_pair(15000, 0.0, seed=92), 1500, 23),
+             (synth.copula_pair(20000, 0.2, seed=93), 10000, 24),
+             (synth.copula_pair(6000, 0.3, seed=94, frac_tied2=0.1), 3000, 25),
+             (None, 6000, 26),  # the pair before again
+             (synth.copula_pair(12000, 0.2, seed=95), 40000, 27),  # long: a lane
+             (synth.small_pair(4000, 0.2, seed=96, subset1=3600, subset2=3800), 3000, 28),  # a lane
+             (synth.copula_pair(5000, 0.2, seed=97), 600, 29)]  # short: a lane
+    dps = [engine.pair(p.ranks1, p.feat1, p.ranks2, p.feat2, p.n_features, p.population) if p else None
+           for p, _, _ in specs]
+    dps[5] = dps[3]
+    for dp, (_, n, _) in zip(dps, specs):
+        dp.run(n, seed=99)  # each pair's ladder
+    n_perm = [n for _, n, _ in specs]
+    seeds = [s for _, _, s in specs]
+    got = engine.batch_run(dps, n_perm, seeds)
+    # six runs in waves: one sweep launch per wave, counted with its first run
+    launches = [g.summary["sweep0_launches"] for g in got]
+    assert sum(launches[:6]) < 6, launches
+    for dp, n, s, g in zip(dps, n_perm, seeds, got):
+        a = dp.run(n, seed=s)
+        assert optimum(g.unpermuted) == optimum(a.unpermuted), (n, s)
+        assert np.array_equal(g.minp, a.minp), (n, s)
+        assert g.summary["count_le"] == a.summary["count_le"]
+        assert g.summary["empirical_pvalue"] == a.summary["empirical_pvalue"]
+        assert sum(g.summary["n_route"].values()) == n + 1
+    # a second batch finds the pairs' table screens and ladders
+    again = engine.batch_run(dps[:6], n_perm[:6], seeds[:6])
+    for g, h in zip(got, again):
+        assert np.array_equal(g.minp, h.minp)
+    for q, dp in enumerate(dps):
+        if q != 5:
+            dp.close()
+
+
 def test_memory_admission_and_errors(engine):
     from dual_threshold_optimization_gb300._lib import lib
     p = synth.copula_pair(8000, 0.2, seed=90)
