@@ -601,7 +601,8 @@ def extra_configs(eng, args, torch):
     dtb = time.perf_counter() - t0
     f64 = [fp64_rate(dps[q], 256, 44) for q in range(0, 512, 128)]
     out["config3_batch"] = {"workload": "512 pairs, N ~ U[2000, 30000], rho ~ U[0, 0.4], 10000 "
-                                        "permutations each, %d lanes" % args.lanes,
+                                        "permutations each: waves of pairs per multi-pair sweep (pairs "
+                                        "without a ladder on %d lanes)" % args.lanes,
                             "value": 512 * 10000 / dtb, "unit": "perms/s", "ms_per_batch": dtb * 1e3,
                             "fp64_gpu": {"value": 4 * 256 / sum(256 / f["value"] for f in f64),
                                          "unit": "perms/s", "sample": "256 permutations of pairs 0, 128, "
@@ -668,7 +669,8 @@ def run_batch(args):
         "warmup": args.warmup, "ms_per_step": dt * 1e3, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "int32+f32 screen, f64 refine",
         "data": "synthetic (seeded Gaussian-copula lists, N ~ U[2000, 30000], rho ~ U[0, 0.4])",
-        "config": {"workload": "batch: %d pairs x %d permutations, %d lanes" % (npairs, P, args.lanes),
+        "config": {"workload": "batch: %d pairs x %d permutations, waves of pairs per multi-pair sweep "
+                               "(pairs without a ladder on %d lanes)" % (npairs, P, args.lanes),
                    "pairs": npairs, "permutations_per_pair": P, "lanes": args.lanes,
                    "grid_cells_total": cells,
                    "l2": "inputs larger than L2: each step streams %d MB of permutation labels"

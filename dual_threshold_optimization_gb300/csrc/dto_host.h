@@ -282,6 +282,7 @@ int table_exhaustive(Lane* L, dto_pair* P, const int16_t* X, long long xstride, 
 // One pair's run inside a wave of dto_batch_run.
 struct WaveJob {
   dto_pair* P = nullptr;
+  uint32_t first = 1;  // permutation ids first .. first + n_perm - 1
   int64_t n_perm = 0;
   uint64_t seed = 0;
   dto_result* out_unpermuted = nullptr;
@@ -293,7 +294,9 @@ struct WaveJob {
 // most 0x7FFF features (the packed sweep), kWaveMinPerm..kWaveMaxPerm
 // permutations, and a ladder (the pair's own, or the context's model's).
 bool wave_eligible(dto_ctx* ctx, dto_pair* P, int64_t n_perm, int precision);
-// The runs of `jobs` (all eligible, permutation ids 1..n_perm) in waves: per
+// Device bytes of labels a wave holds for a job.
+long long wave_label_bytes(const dto_pair* P, int64_t n_perm);
+// The runs of `jobs` (all eligible) in waves: per
 // wave the pairs' labels, then one cascade sweep over all their tasks, then
 // their exhaustive fallbacks; each pair's unpermuted task through the
 // exhaustive screen on the side stream.  The results equal lane_run_range's

@@ -76,11 +76,16 @@ bool admissible(const dto_server* s, const Job* j) {
   return s->running == 0 || s->reserved + j->need <= s->budget;
 }
 
+// Labels of the requests a worker takes into one wave (continuous batching:
+// short screen requests queued together share one multi-pair sweep).
+constexpr long long kGroupLabelBytes = 4LL << 30;
+
 void worker(dto_server* s, int w) {
   Lane* L = s->lanes[(size_t)w];
   cudaSetDevice(s->ctx->device);
   for (;;) {
-    Job* j = nullptr;
+    std::vector<Job*> group;
+    bool wave = false;
     {
       std::unique_lock<std::mutex> lk(s->mu);
       s->cv_work.wait(lk, [&] { return s->stop || (!s->queue.empty() && admissible(s, s->queue.front())); });
@@ -88,29 +93,75 @@ void worker(dto_server* s, int w) {
         if (s->stop) return;
         continue;
       }
-      j = s->queue.front();
+      Job* j = s->queue.front();
       s->queue.pop_front();
-      s->reserved += j->need;
-      s->running += 1;
-      j->started = true;
-      j->t_start = Clock::now();
+      group.push_back(j);
+      // a request that a wave takes brings the queued requests a wave also
+      // takes, in arrival order, while their labels fit and memory admits them
+      wave = wave_eligible(s->ctx, j->pair, j->n_perm, j->precision);
+      if (wave) {
+        long long bytes = wave_label_bytes(j->pair, j->n_perm);
+        s->reserved += j->need;
+        s->running += 1;
+        for (auto it = s->queue.begin(); it != s->queue.end() && bytes < kGroupLabelBytes;) {
+          Job* x = *it;
+          const long long b = wave_label_bytes(x->pair, x->n_perm);
+          if (bytes + b <= kGroupLabelBytes && admissible(s, x) &&
+              wave_eligible(s->ctx, x->pair, x->n_perm, x->precision)) {
+            group.push_back(x);
+            bytes += b;
+            s->reserved += x->need;
+            s->running += 1;
+            it = s->queue.erase(it);
+          } else {
+            ++it;
+          }
+        }
+      } else {
+        s->reserved += j->need;
+        s->running += 1;
+      }
+      for (Job* x : group) {
+        x->started = true;
+        x->t_start = Clock::now();
+      }
     }
     s->lane_err[(size_t)w].clear();
-    dto_result unperm{};
-    L->cancel = &j->cancel;
-    const int rc = lane_run_range(L, j->pair, j->first, j->n_perm, j->seed, nullptr, j->precision,
-                                  j->out_unpermuted ? j->out_unpermuted : &unperm, j->out_minp, nullptr,
-                                  j->out_summary);
-    L->cancel = nullptr;
+    int rc = DTO_OK;
+    std::vector<dto_result> unperm(group.size());
+    if (wave) {
+      // the group's runs in waves (requests in a wave run to the end: a
+      // cancel reaches only requests still queued)
+      std::vector<WaveJob> wj(group.size());
+      for (size_t q = 0; q < group.size(); ++q) {
+        Job* x = group[q];
+        wj[q].P = x->pair;
+        wj[q].first = x->first;
+        wj[q].n_perm = x->n_perm;
+        wj[q].seed = x->seed;
+        wj[q].out_unpermuted = x->out_unpermuted ? x->out_unpermuted : &unperm[q];
+        wj[q].out_minp = x->out_minp;
+        wj[q].out_summary = x->out_summary;
+      }
+      rc = lane_wave(L, wj);
+    } else {
+      Job* j = group[0];
+      L->cancel = &j->cancel;
+      rc = lane_run_range(L, j->pair, j->first, j->n_perm, j->seed, nullptr, j->precision,
+                          j->out_unpermuted ? j->out_unpermuted : &unperm[0], j->out_minp, nullptr, j->out_summary);
+      L->cancel = nullptr;
+    }
     {
       std::lock_guard<std::mutex> lk(s->mu);
-      j->status = rc;
-      if (rc) j->err = s->lane_err[(size_t)w];
-      j->t_end = Clock::now();
-      j->done = true;
-      s->reserved -= j->need;
-      s->running -= 1;
-      s->completed += 1;
+      for (Job* x : group) {
+        x->status = rc;
+        if (rc) x->err = s->lane_err[(size_t)w];
+        x->t_end = Clock::now();
+        x->done = true;
+        s->reserved -= x->need;
+        s->running -= 1;
+        s->completed += 1;
+      }
     }
     s->cv_done.notify_all();
     s->cv_work.notify_all();  // memory freed: the head may now fit

@@ -27,7 +27,7 @@ namespace {
 
 constexpr int64_t kWaveMinPerm = 1025;   // shorter runs: the exhaustive screen (a lane's run)
 constexpr int64_t kWaveMaxPerm = 32767;  // longer runs: a lane's pipeline with its tighter tables
-constexpr size_t kWaveLabelBytes = size_t(4) << 30;  // labels of one wave (two in flight)
+constexpr size_t kWaveLabelBytes = size_t(8) << 30;  // labels of one wave (two in flight)
 constexpr int kWaveLevels = 3;
 
 // The pair's ladder (levels 0..2): its own from an earlier run, else the
@@ -145,7 +145,8 @@ int enqueue_wave(Lane* L, std::vector<WaveJob>& jobs, Wave& wv) {
     NvtxRange lr("dto: labels");
     for (int k = 0; k < nj; ++k) {
       const long long xs = xstride_of(job(k).P->N1);
-      rc = make_labels_launch(L, job(k).P, job(k).seed, 1u, (int)job(k).n_perm, nullptr, X + xoff[(size_t)k] + xs, xs);
+      rc = make_labels_launch(L, job(k).P, job(k).seed, job(k).first, (int)job(k).n_perm, nullptr,
+                              X + xoff[(size_t)k] + xs, xs);
       if (rc) return rc;
       wv.launches[(size_t)k] += 1;
     }
@@ -304,6 +305,8 @@ int finish_wave(Lane* L, std::vector<WaveJob>& jobs, Wave& wv) {
 
 }  // namespace
 
+long long wave_label_bytes(const dto_pair* P, int64_t n_perm) { return (n_perm + 1) * xstride_of(P->N1) * 2; }
+
 bool wave_eligible(dto_ctx* ctx, dto_pair* P, int64_t n_perm, int precision) {
   if (!ctx || !P || P->ctx != ctx) return false;
   if (precision != DTO_PRECISION_SCREEN || !P->same_set || P->ncommon > kPackedMaxCommon) return false;
@@ -331,7 +334,7 @@ int lane_wave(Lane* L, std::vector<WaveJob>& jobs) {
     size_t bytes = 0;
     while (q < order.size() && jobs[(size_t)order[q]].P->C == C) {
       const WaveJob& j = jobs[(size_t)order[q]];
-      const size_t b = (size_t)(j.n_perm + 1) * (size_t)xstride_of(j.P->N1) * 2;
+      const size_t b = (size_t)wave_label_bytes(j.P, j.n_perm);
       if (!wv.w.empty() && bytes + b > kWaveLabelBytes) break;
       wv.w.push_back(order[q]);
       bytes += b;
