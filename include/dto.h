@@ -244,8 +244,13 @@ DTO_API double dto_fdr(int64_t set1_len, int64_t set2_len, int64_t overlap, int6
  * in arrival order; the head is admitted when a lane is free and its device
  * working set (dto_run_device_bytes) fits under mem_budget bytes next to the
  * requests running (mem_budget 0: no budget; a request larger than the budget
- * runs alone).  A request's results equal dto_run_range's for the same
- * arguments, whatever runs beside it. */
+ * runs alone).  A worker that admits a short screen request (1,025 to 32,767
+ * permutations of lists over one feature set that share at most 32,767
+ * features, with a ladder from an earlier run of the pair or of a pair of its
+ * shape) also takes the queued requests of that kind that fit, in arrival
+ * order, and sweeps their tasks together in waves (one launch over several
+ * pairs).  A request's results equal dto_run_range's for the same arguments,
+ * whatever runs beside it. */
 typedef struct dto_server dto_server;
 typedef int64_t dto_job;
 
@@ -275,7 +280,8 @@ DTO_API int dto_serve_wait_for(dto_server* srv, dto_job job, double timeout_ms, 
  * queue at once, a running one stops at its next batch boundary once its
  * kernels in flight have finished (they are not interrupted).  Its wait then
  * returns DTO_ERR_CANCELLED and its outputs are undefined; a request that had
- * already finished keeps its results. */
+ * already finished, or that runs in a wave (which runs to its end), keeps its
+ * results. */
 DTO_API int dto_serve_cancel(dto_server* srv, dto_job job);
 DTO_API const char* dto_serve_last_error(dto_server* srv);
 DTO_API int dto_serve_stats(dto_server* srv, int64_t* queued, int64_t* running, int64_t* completed,
@@ -284,8 +290,13 @@ DTO_API int dto_serve_stats(dto_server* srv, int64_t* queued, int64_t* running, 
  * its peak (the admission size of a request). */
 DTO_API int64_t dto_run_device_bytes(const dto_pair* pair, int64_t n_perm);
 /* The permutation null of npairs pairs (pair q: n_perm[q] permutations from
- * id 1 of seeds[q]) over `lanes` lanes (<= 0: 4); per-pair outputs as in
- * dto_run_range (out_minp[q] and out_summary nullable). */
+ * id 1 of seeds[q]); per-pair outputs as in dto_run_range (out_minp[q] and
+ * out_summary nullable).  Short screen runs of pairs with a ladder (as for a
+ * server's waves) go in waves on the context's own stream: each wave draws
+ * the labels of several pairs and sweeps all their tasks in one launch, and
+ * each pair keeps the table screens built for it; the other runs go over
+ * `lanes` lanes (<= 0: 4) meanwhile.  A wave's summary times are the wave's,
+ * shared by its pairs in proportion to their tasks. */
 DTO_API int dto_batch_run(dto_ctx* ctx, int npairs, dto_pair* const* pairs, const int64_t* n_perm,
                           const uint64_t* seeds, int precision, int lanes, dto_result* out_unpermuted,
                           double* const* out_minp, dto_summary* out_summary);
