@@ -501,8 +501,10 @@ def run_gpu(args):
             "permutations": statistics.mean(s_["perm_ms"] for s_ in summaries),
             "level0_sweeps": statistics.mean(s_["sweep0_ms"] for s_ in summaries),
             "after_last_level0": statistics.mean(s_["tail_ms"] for s_ in summaries),
-            "note": "device times of the library's CUDA events; the permutations and level-0 sweeps run "
-                    "one after another on the main stream, later levels on side streams"},
+            "note": "device times of the library's CUDA events; the permutations and the table sweeps "
+                    "(level 0, with levels 1 and 2 cascaded in the same launch) run one after another on "
+                    "the main stream; after_last_level0 is what follows the last sweep (fallbacks, result "
+                    "copy)"},
         "routes_per_step": {k: v / args.steps for k, v in
                             ((k, sum(s_["n_route"][k] for s_ in summaries)) for k in summaries[0]["n_route"])},
         "latency_ms": {"p50": statistics.median(step_ms),

@@ -208,17 +208,19 @@ void fill_result(const dto_pair* P, const TaskResult& r, int permuted, dto_resul
   o->reserved = 0;
 }
 
-// Batch size of a run: 2^31 bytes of labels (2 GiB), and at
+// Batch size of a run: 2^32 bytes of labels (4 GiB), and at
 // most 1 GiB of index scratch for test mode and for pairs whose lists hold
 // different features.  Every launch pays a tail (its slowest tasks), so
-// fewer, larger batches win: per 100,000 permutations 2 GiB measured 36.2 ms
-// at N = 20,000 and 39.6 ms on the 18,000-feature background pair, 1 GiB
-// 36.2-36.8 and 43.1 ms, 512 MiB 40-41 ms and 46 ms (before the cascade).
+// fewer, larger batches win: per 100,000 permutations at N = 20,000, 4 GiB
+// (one batch) measured 22.6 ms against 23.8 ms for 2 GiB (two); before the
+// cascade 2 GiB measured 36.2 ms at N = 20,000 and 39.6 ms on the
+// 18,000-feature background pair, 1 GiB 36.2-36.8 and 43.1 ms, 512 MiB
+// 40-41 ms and 46 ms.
 
 long long batch_of(const dto_pair* P, int64_t n_perm, bool test_mode) {
   const long long xs = xstride_of(P->N1);
   const long long L12 = P->N1 + P->N2;
-  long long batch = std::max(1LL, std::min<long long>((1LL << 31) / (xs * 2), 1LL << 20));
+  long long batch = std::max(1LL, std::min<long long>((1LL << 32) / (xs * 2), 1LL << 20));
   if (test_mode || !P->same_set) batch = std::min(batch, std::max(1LL, (1LL << 30) / (L12 * 4)));
   return std::min<long long>(batch, std::max<long long>(n_perm, 1));
 }
