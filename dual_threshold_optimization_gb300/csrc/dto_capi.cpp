@@ -331,11 +331,19 @@ int dto_pair_create(dto_ctx* ctx, const uint32_t* ranks1, const int32_t* feat1, 
   P->map12.assign((size_t)n1, -1);
   P->ylab.assign((size_t)n1, -1);
   long long common = 0;
+  // m_j: list-1 positions whose feature sits in list 2 at a rank <= T2[j]
+  std::vector<int> mcnt((size_t)nt2, 0);
   for (int64_t p = 0; p < n1; ++p) {
     int q = pos2[(size_t)P->f1[(size_t)p]];
     P->map12[(size_t)p] = q;
-    if (q >= 0) { ++common; P->ylab[(size_t)p] = P->lab2[(size_t)q]; }
+    if (q >= 0) {
+      ++common;
+      P->ylab[(size_t)p] = P->lab2[(size_t)q];
+      const int16_t l = P->lab2[(size_t)q];
+      if (l >= 0) ++mcnt[(size_t)((l / Cp) * P->C + (l % Cp))];
+    }
   }
+  for (int j = 1; j < nt2; ++j) mcnt[(size_t)j] += mcnt[(size_t)j - 1];
   P->ncommon = common;
   P->same_set = (common == n1 && common == n2);
   // fixed-point fraction bits: |ln pmf| <= N ln 2 must fit in int32 with slack
@@ -357,24 +365,26 @@ int dto_pair_create(dto_ctx* ctx, const uint32_t* ranks1, const int32_t* feat1, 
     size_t bytes;
     void** d;
   };
-  const Part parts[6] = {{row.data(), row.size() * 4, (void**)&P->dRow},
+  const Part parts[7] = {{row.data(), row.size() * 4, (void**)&P->dRow},
                          {P->c2.data(), P->c2.size() * 4, (void**)&P->dNcnt},
                          {F.data(), F.size() * 4, (void**)&P->dF},
                          {P->ylab.data(), P->ylab.size() * 2, (void**)&P->dYlab},
                          {P->lab2.data(), P->lab2.size() * 2, (void**)&P->dLab2},
-                         {P->map12.data(), P->map12.size() * 4, (void**)&P->dMap12}};
-  size_t off[6], total = 0;
-  for (int k = 0; k < 6; ++k) {
+                         {P->map12.data(), P->map12.size() * 4, (void**)&P->dMap12},
+                         {mcnt.data(), mcnt.size() * 4, (void**)&P->dMcnt}};
+  constexpr int kParts = (int)(sizeof(parts) / sizeof(parts[0]));
+  size_t off[kParts], total = 0;
+  for (int k = 0; k < kParts; ++k) {
     off[k] = total;
     total += (parts[k].bytes + 255) & ~(size_t)255;
     P->upload_bytes += (long long)parts[k].bytes;
   }
   std::vector<unsigned char> host(total, 0);
-  for (int k = 0; k < 6; ++k)
+  for (int k = 0; k < kParts; ++k)
     if (parts[k].bytes) std::memcpy(host.data() + off[k], parts[k].h, parts[k].bytes);
   cudaError_t e = cudaMalloc(&P->dBase, std::max(total, (size_t)256));
   if (e == cudaSuccess) {
-    for (int k = 0; k < 6; ++k) *parts[k].d = static_cast<unsigned char*>(P->dBase) + off[k];
+    for (int k = 0; k < kParts; ++k) *parts[k].d = static_cast<unsigned char*>(P->dBase) + off[k];
     e = cudaMemcpyAsync(P->dBase, host.data(), total, cudaMemcpyHostToDevice, ctx->lane0->stream);
   }
   if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->lane0->stream);

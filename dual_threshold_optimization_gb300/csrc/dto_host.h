@@ -204,6 +204,7 @@ struct dto_pair {
   int16_t* dYlab = nullptr;
   int16_t* dLab2 = nullptr;
   int* dMap12 = nullptr;
+  int* dMcnt = nullptr;  // [n2]: list-1 positions whose label's column is <= j
   dto::PairDev dev{};
   // The table ladder (fixed-point bounds of levels 0..2) from the last long
   // run of this pair: a property of the pair's null distribution, so a later

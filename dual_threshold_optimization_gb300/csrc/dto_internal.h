@@ -135,13 +135,18 @@ constexpr int kTableWarpHits = 2 * kTableHitCap;
 // The packed table sweep holds overlaps in 16-bit halves and tests
 // k >= kthr as the sign bit of k + (0x8000 - kthr): it needs every overlap,
 // hence the number of features the two lists share, to be <= 0x7FFF.
-constexpr long long kPackedMaxCommon = 0x7FFF;
+constexpr long long kPackedMaxCommon = 0xFFFF;
 
 struct TableArgs {
   int n1, n2, N, C;      // C: columns per lane
   int lanes;             // 32 (32-bit sweep) or 16 (half-warp packed sweep)
   const int* rowstart;   // K_i = rowstart[i+1]
   const int* ncnt;
+  // packed entries: m_j = list-1 positions whose label is <= j (any
+  // permutation: the labels are only moved), and N1 = all list-1 positions;
+  // a cell's overlap lies in [max(0, K_i + m_j - N1), min(K_i, m_j)]
+  const int* mcnt;
+  int N1;
   const uint32_t* F;
   int fshift;
   int tau;               // fixed-point ln p guess

@@ -292,6 +292,8 @@ int ensure_table(Lane* L, dto_pair* P, int level, int tau, cudaStream_t stream, 
   t.fshift = P->fshift;
   t.tau = tau;
   t.packed = packed ? 1 : 0;
+  t.mcnt = P->dMcnt;
+  t.N1 = (int)P->N1;
   t.kthr = L->dKthr[level];
   LCK(launch_table_build(t, L->ctx->nsm, stream));
   L->acc_launches += 1;

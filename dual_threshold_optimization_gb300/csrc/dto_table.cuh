@@ -31,13 +31,45 @@ __host__ __device__ constexpr int table_cq(int C) { return (C + 7) & ~7; }
 // chunks so that a quarter-warp's 128-bit loads hit distinct banks.
 __host__ __device__ constexpr int table_wp(int C) { return 4 * ((table_cq(C) / 8) | 1); }
 
-// One thread per entry: binary search for the first overlap that passes.
+// The first overlap k of cell (i, j) whose LBT(k) is <= tauT (binary search
+// over k), 0 when every k passes, min(K, n) + 1 when none does.
+__device__ __forceinline__ int table_thr(const TableArgs& A, uint32_t FN, double scale, int tauT, int i, int j) {
+  const int K = __ldg(A.rowstart + i + 1);
+  const int n = __ldg(A.ncnt + j);
+  const int a = min(K, n), b = max(K, n);
+  const long long mode = ((long long)(a + 1) * (long long)(b + 1)) / (long long)(A.N + 2);
+  if (lbt_fix(A.F, A.N, FN, K, n, (int)mode, mode, scale) <= tauT) return 0;
+  // invariant: pred(lo) false, pred(hi) true or hi = a + 1
+  int lo = (int)mode, hi = a + 1;
+  while (hi - lo > 1) {
+    const int mid = lo + (hi - lo) / 2;
+    if (lbt_fix(A.F, A.N, FN, K, n, mid, mode, scale) <= tauT) hi = mid;
+    else lo = mid;
+  }
+  return hi;
+}
+
 // Layout [i][q][lane][8] for A.lanes lanes of A.C columns each (32 lanes of C
 // for the 32-bit sweep, 16 lanes of 2 C for the half-warp packed sweep):
 // entry t of a lane's row is in its q = t / 8-th 16-byte chunk, so a load of
 // chunk q by the lanes reads lanes x 16 contiguous bytes.
-// Plain entries hold kthr (0xFFFF: never); packed entries hold
-// 0x8000 - min(kthr, 0x8000) (0: never).
+//
+// Plain entries (one thread each) hold kthr (0xFFFF: never).
+//
+// Packed entries come in pairs, the two 16-bit halves of one word of the
+// sweep (columns t, t + 1, t even; one thread a pair).  The sweep holds a
+// cell's overlap o in a 16-bit half (o <= N1 <= 65534) and adds the entry
+// with one 32-bit add to both halves at once; bit 15 (31) of the sum must
+// be set exactly when o >= kthr.  A cell's overlap lies in
+// [L, U] = [max(0, K_i + m_j - N1), min(K_i, m_j)] whatever the permutation
+// (m_j: the list-1 positions whose label is <= j), and U - L <= N1 / 2 <=
+// 32767.  With kthr clamped to [L, U + 1] (which changes no hit),
+// o - kthr lies in [-32768, 32767], so the half's sum 0x8000 + o - kthr
+// lies in [0, 0xFFFF] and its bit 15 is the test.  The entry is
+// 0x8000 - kthr modulo 2^16: when kthr > 0x8000 that wraps, and the lower
+// half's sum then always carries one into the upper half, which the upper
+// entry takes back (it is one less).  A column past the grid (padding) has
+// the overlap of the last column and the entry "never" (kthr = U + 1).
 static __global__ void table_build_kernel(const TableArgs A) {
   const int Cq = table_cq(A.C);
   const int lanes = A.lanes;
@@ -45,33 +77,31 @@ static __global__ void table_build_kernel(const TableArgs A) {
   const double scale = ldexp(1.0, A.fshift);
   const int tauT = A.tau + (int)ceil(kTableMargin * scale);
   const uint32_t FN = __ldg(A.F + A.N);
-  for (long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x; c < cells;
-       c += (long long)gridDim.x * blockDim.x) {
+  const long long step = A.packed ? 2 : 1;
+  for (long long c = ((long long)blockIdx.x * blockDim.x + threadIdx.x) * step; c < cells;
+       c += (long long)gridDim.x * blockDim.x * step) {
     const int i = (int)(c / (lanes * Cq));
     const int rem = (int)(c % (lanes * Cq));
     const int q = rem / (8 * lanes), lane = (rem / 8) % lanes;
     const int t = 8 * q + rem % 8;
     const int j = lane * A.C + t;
-    int thr = 0x10000;  // never
-    if (t < A.C && j < A.n2) {
-      const int K = __ldg(A.rowstart + i + 1);
-      const int n = __ldg(A.ncnt + j);
-      const int a = min(K, n), b = max(K, n);
-      const long long mode = ((long long)(a + 1) * (long long)(b + 1)) / (long long)(A.N + 2);
-      if (lbt_fix(A.F, A.N, FN, K, n, (int)mode, mode, scale) <= tauT) {
-        thr = 0;
-      } else {
-        // invariant: pred(lo) false, pred(hi) true or hi = a + 1
-        int lo = (int)mode, hi = a + 1;
-        while (hi - lo > 1) {
-          int mid = lo + (hi - lo) / 2;
-          if (lbt_fix(A.F, A.N, FN, K, n, mid, mode, scale) <= tauT) hi = mid;
-          else lo = mid;
-        }
-        thr = hi;
-      }
+    if (!A.packed) {
+      const int thr = (t < A.C && j < A.n2) ? table_thr(A, FN, scale, tauT, i, j) : 0x10000;
+      A.kthr[c] = (uint16_t)min(thr, 0xFFFF);
+      continue;
     }
-    A.kthr[c] = A.packed ? (uint16_t)(0x8000 - min(thr, 0x8000)) : (uint16_t)min(thr, 0xFFFF);
+    const int K = __ldg(A.rowstart + i + 1);
+    int k2[2];
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      const int jj = j + h;
+      const int m = __ldg(A.mcnt + min(jj, A.n2 - 1));
+      const int U = min(K, m), L = max(0, K + m - A.N1);
+      const int thr = (t + h < A.C && jj < A.n2) ? table_thr(A, FN, scale, tauT, i, jj) : 0x10000;
+      k2[h] = min(max(thr, L), U + 1);
+    }
+    A.kthr[c] = (uint16_t)((0x8000 - k2[0]) & 0xFFFF);
+    A.kthr[c + 1] = (uint16_t)((0x8000 - k2[1] - (k2[0] > 0x8000 ? 1 : 0)) & 0xFFFF);
   }
 }
 
@@ -930,7 +960,11 @@ __global__ void __launch_bounds__(kTableWarps * 32, 1) table_hw_kernel(const Tab
       if (p >= rs && p < re && lab0 >= 0) add_lab(lab0);
       if (p + 1 >= rs && p + 1 < re && lab1 >= 0) add_lab(lab1);
     };
+    // A half without a task (its slot drained) sweeps no labels: its zero
+    // overlaps lie outside the cells' ranges the table entries assume, so its
+    // "hits" are meaningless and are not recorded.
     auto push_hit = [&](int i, int col, int k) {
+      if (!live) return;
       const int pos = atomicAdd(&st_me->nhits, 1);
       if (pos < hcap) hb_me[pos] = make_int2((i << 16) | (h * C2 + col), k);
     };

@@ -72,6 +72,8 @@ int wave_table(Lane* L, dto_pair* P, int level, int tau, long long* launches) {
   t.fshift = P->fshift;
   t.tau = tau;
   t.packed = 1;
+  t.mcnt = P->dMcnt;
+  t.N1 = (int)P->N1;
   t.kthr = P->dWaveKthr[level];
   P->wave_ok[level] = false;
   LCK(launch_table_build(t, L->ctx->nsm, L->stream));
