@@ -80,9 +80,8 @@ struct Lane {
   // and batch lanes: many pairs, each run once)
   bool use_model = false;
   cudaStream_t stream = nullptr;
-  cudaStream_t side = nullptr;  // first batch, later table levels and fallbacks
+  cudaStream_t side = nullptr;  // first batch, unpermuted task, fallbacks
   cudaEvent_t evSide = nullptr;
-  cudaEvent_t evTables = nullptr;  // the later levels' tables, built on the side stream
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   cudaEvent_t evk[4] = {nullptr, nullptr, nullptr, nullptr};  // perm start/end, grid start/end
   // per-run accounting
@@ -100,10 +99,9 @@ struct Lane {
   int* dWork = nullptr;
   unsigned long long* dRefined = nullptr;
   unsigned* dGuess = nullptr;  // bound histogram shared by the batches of one run
-  // per-warp hit buffers of the table screen: [0] the main stream's, [1 + s]
-  // slot s's side stream's
-  void* dHits[1 + kSlotsMax] = {};
-  size_t hitBytes[1 + kSlotsMax] = {};
+  // per-warp hit buffers of the table sweep (main stream)
+  void* dHits[1] = {};
+  size_t hitBytes[1] = {};
   // Batches of the table-screen pipeline in flight.  A slot is reused only
   // once the side stream has finished its batch; with three, the main stream
   // draws the next batch's labels while the side stream still resolves the
@@ -291,9 +289,9 @@ struct WaveJob {
   dto_summary* out_summary = nullptr;  // nullable
   int tau[3] = {};  // the levels' bounds (set by lane_wave)
 };
-// Runs that a wave takes: the screen, lists over one feature set sharing at
-// most 0x7FFF features (the packed sweep), kWaveMinPerm..kWaveMaxPerm
-// permutations, and a ladder (the pair's own, or the context's model's).
+// Runs that a wave takes: the screen, lists over one feature set,
+// kWaveMinPerm..kWaveMaxPerm permutations, and a ladder (the pair's own, or
+// the context's model's).
 bool wave_eligible(dto_ctx* ctx, dto_pair* P, int64_t n_perm, int precision);
 // Device bytes of labels a wave holds for a job.
 long long wave_label_bytes(const dto_pair* P, int64_t n_perm);

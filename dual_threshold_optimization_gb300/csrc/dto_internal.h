@@ -120,37 +120,23 @@ struct ComposeArgs {
 // kernel runs about 25 % slower.
 constexpr int kTableWarps = 16;
 constexpr int kTableCtasPerSm = 1;
-// Tasks one warp of the 32-bit table sweep runs side by side (sharing the
-// table-row loads and the loop control, interleaving their dependent
-// instruction chains).  Two measured slower than one at N = 20,000 (1.72 M
-// against 2.04 M permutations/s: the two tasks' state does not fit 128
-// registers without spilling); the half-warp packed sweep is the layout that
-// does run two tasks per warp.  Each task has kTableHitCap hit slots.
-constexpr int kTableTasks = 1;
-static_assert(kTableTasks == 1 || kTableTasks == 2, "one or two tasks per warp");
 constexpr int kTableHitCap = 8192;  // hit slots per task
 // hit slots per warp of a table sweep (the half-warp sweep runs two tasks)
 constexpr int kTableWarpHits = 2 * kTableHitCap;
 
-// The packed table sweep holds overlaps in 16-bit halves and tests
-// k >= kthr as the sign bit of k + (0x8000 - kthr): it needs every overlap,
-// hence the number of features the two lists share, to be <= 0x7FFF.
-constexpr long long kPackedMaxCommon = 0xFFFF;
 
 struct TableArgs {
-  int n1, n2, N, C;      // C: columns per lane
-  int lanes;             // 32 (32-bit sweep) or 16 (half-warp packed sweep)
+  int n1, n2, N, C;      // C: columns per lane of the half-warp sweep (2 C of the pair)
   const int* rowstart;   // K_i = rowstart[i+1]
   const int* ncnt;
-  // packed entries: m_j = list-1 positions whose label is <= j (any
-  // permutation: the labels are only moved), and N1 = all list-1 positions;
-  // a cell's overlap lies in [max(0, K_i + m_j - N1), min(K_i, m_j)]
+  // m_j = list-1 positions whose label is <= j (any permutation: the labels
+  // are only moved), and N1 = all list-1 positions; a cell's overlap lies in
+  // [max(0, K_i + m_j - N1), min(K_i, m_j)]
   const int* mcnt;
   int N1;
   const uint32_t* F;
   int fshift;
   int tau;               // fixed-point ln p guess
-  int packed;            // entry form of the packed (16-bit overlap) sweep
   uint16_t* kthr;        // [n1][table_cq(C) / 8][lanes][8]
 };
 
@@ -171,14 +157,13 @@ struct TableGridArgs {
   // again at level l + 1 by the same half-warp, up to nlev levels (the level
   // above sits in kthr, tau, tight*, ntight; levels 1 and 2 below).  Tasks
   // of the last level with no hit go to the fallback list.  nlev = 1: one
-  // level, as the 32-bit sweep always runs.
+  // level.
   int nlev;
   const uint16_t* kthr_up[2];
   int tau_up[2];
   const uint16_t* tight_up[2][3];
   int tight_tau_up[2][3];
   int ntight_up[2];
-  int packed;             // 16-bit overlap sweep (every overlap <= 0x7FFF)
   int route;              // DTO_ROUTE_* written with each result
   int smemF;              // the ln m! table is copied to shared memory
   TaskResult* out;
@@ -204,10 +189,10 @@ struct TableGridArgs {
 cudaError_t raise_smem_limit(const void* kernel, size_t bytes);
 
 size_t grid_smem_bytes(int C, int n1, long long Npop, int smemF);
-// C is the pair's columns per lane of the 32-lane layout; packed pairs use
+// C is the pair's columns per lane of the 32-lane layout; the table sweep is
 // the half-warp sweep (16 lanes of 2 C columns).
-size_t table_smem_bytes(int C, int n1, int n2, long long Npop, int smemF, bool packed);
-size_t table_entries(int C, int n1, bool packed);
+size_t table_smem_bytes(int C, int n1, int n2, long long Npop, int smemF);
+size_t table_entries(int C, int n1);
 cudaError_t launch_table_build(const TableArgs& a, int nsm, cudaStream_t s);
 cudaError_t launch_table_grid(const TableGridArgs& a, int C, int ctas, cudaStream_t s);
 cudaError_t launch_grid(const GridArgs& a, int grid_ctas, cudaStream_t s);

@@ -355,20 +355,16 @@ cudaError_t launch_grid(const GridArgs& a, int ctas, cudaStream_t s) {
   }
 }
 
-size_t table_smem_bytes(int C, int n1, int n2, long long Npop, int smemF, bool packed) {
+size_t table_smem_bytes(int C, int n1, int n2, long long Npop, int smemF) {
   const size_t f = smemF ? (size_t)((Npop + 1 + 3) & ~3LL) * 4 : 0;
   const size_t base = f + (size_t)((n1 + 1 + 3) & ~3) * 4 + (size_t)((n2 + 3) & ~3) * 4;  // n1 = -1, n2 = 0: none
-  if (packed)
-    return base + (size_t)((hw_lut_entries(C) + 7) & ~7) * 2 + (size_t)kTableWarps * hw_warp_ints(2 * C) * 4;
-  return base + (size_t)kTableWarps * table_warp_ints(C) * 4;
+  return base + (size_t)((hw_lut_entries(C) + 7) & ~7) * 2 + (size_t)kTableWarps * hw_warp_ints(2 * C) * 4;
 }
 
-size_t table_entries(int C, int n1, bool packed) {
-  return packed ? (size_t)n1 * 16 * hw_cq(2 * C) : (size_t)n1 * 32 * table_cq(C);
-}
+size_t table_entries(int C, int n1) { return (size_t)n1 * 16 * hw_cq(2 * C); }
 
 cudaError_t launch_table_build(const TableArgs& a, int nsm, cudaStream_t s) {
-  long long cells = (long long)a.n1 * a.lanes * table_cq(a.C);
+  long long cells = (long long)a.n1 * 16 * table_cq(a.C) / 2;  // a thread per pair of entries
   int threads = 128;
   long long blocks = std::min<long long>((cells + threads - 1) / threads, (long long)nsm * 64);
   table_build_kernel<<<(unsigned)blocks, threads, 0, s>>>(a);
@@ -377,8 +373,8 @@ cudaError_t launch_table_build(const TableArgs& a, int nsm, cudaStream_t s) {
 
 cudaError_t launch_table_grid(const TableGridArgs& a, int C, int ctas, cudaStream_t s) {
   // several pairs (segments): no pair tables in shared memory
-  size_t smem = a.segs ? table_smem_bytes(C, -1, 0, 0, 0, true)
-                       : table_smem_bytes(C, a.P.n1, a.P.n2, a.P.Npop, a.smemF, a.packed != 0);
+  size_t smem = a.segs ? table_smem_bytes(C, -1, 0, 0, 0)
+                       : table_smem_bytes(C, a.P.n1, a.P.n2, a.P.Npop, a.smemF);
   switch (C) {
 #define DTO_CASE(CC) \
   case CC:           \

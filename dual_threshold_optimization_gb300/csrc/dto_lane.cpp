@@ -38,12 +38,6 @@ static_assert(kTightTables >= 0 && kTightTables <= 3, "at most three tighter tab
 constexpr int kTightLevels = 3;
 // The first batch's screen with a CTA per task (see grid_kernel).
 constexpr bool kFirstBatchCoop = true;
-// Table levels of the last pipelined batch of the 32-bit sweep (whose levels
-// run as separate launches) before its exhaustive screen (a CTA per task):
-// the table sweeps still beat the exhaustive screen on the hardest tasks (3
-// levels measured 36.9 ms per 100,000 permutations at N = 20,000, 2 levels
-// 38.7 ms, 1 level 44.6 ms).
-constexpr int kLastLevels = 3;
 // How far (in nats of ln p) a run's ladder bound may lie from the pair's
 // stored one before it replaces it.
 constexpr double kLadderSlack = 0.25;
@@ -108,18 +102,16 @@ int lane_create(dto_ctx* ctx, Lane** out, std::string* err_sink) {
   };
   cudaError_t e;
   if ((e = cudaStreamCreateWithFlags(&L->stream, cudaStreamNonBlocking)) != cudaSuccess) return fail(e, "stream");
-  // The side stream runs the fallbacks (and, for the 32-bit sweep, the later
-  // table levels) of a batch while the main stream sweeps the next one, at
-  // the lowest priority: the highest, which lets its CTAs go first whenever
-  // SMs free up, measured neutral at N = 20,000 (the side levels finished
-  // sooner, the next labels later).
+  // The side stream runs a run's first batch or unpermuted task and each
+  // batch's fallbacks while the main stream sweeps the next batch, at the
+  // lowest priority: the highest, which lets its CTAs go first whenever SMs
+  // free up, measured neutral at N = 20,000.
   int prio_least = 0, prio_greatest = 0;
   if ((e = cudaDeviceGetStreamPriorityRange(&prio_least, &prio_greatest)) != cudaSuccess) return fail(e, "stream");
   if ((e = cudaStreamCreateWithPriority(&L->side, cudaStreamNonBlocking, prio_least)) !=
       cudaSuccess)
     return fail(e, "stream");
   if ((e = cudaEventCreateWithFlags(&L->evSide, cudaEventDisableTiming)) != cudaSuccess) return fail(e, "event");
-  if ((e = cudaEventCreateWithFlags(&L->evTables, cudaEventDisableTiming)) != cudaSuccess) return fail(e, "event");
   if ((e = cudaEventCreate(&L->ev0)) != cudaSuccess) return fail(e, "event");
   if ((e = cudaEventCreate(&L->ev1)) != cudaSuccess) return fail(e, "event");
   for (int q = 0; q < 4; ++q)
@@ -173,7 +165,6 @@ void lane_destroy(Lane* L) {
   for (int q = 0; q < 4; ++q)
     if (L->evk[q]) cudaEventDestroy(L->evk[q]);
   if (L->evSide) cudaEventDestroy(L->evSide);
-  if (L->evTables) cudaEventDestroy(L->evTables);
   if (L->side) cudaStreamDestroy(L->side);
   if (L->stream) cudaStreamDestroy(L->stream);
   delete L;
@@ -233,8 +224,8 @@ long long run_device_bytes(const dto_ctx* ctx, const dto_pair* P, int64_t n_perm
   long long b = first * xs * 2 + (long long)(batch + 1) * (long long)sizeof(TaskResult);  // first batch
   if (n_perm > 2048) {
     b += Lane::kSlots * batch * (xs * 2 + (long long)sizeof(TaskResult) + 12);                // batch slots
-    b += (1LL + Lane::kSlots) * kTableCtasPerSm * ctx->nsm * kTableWarps * kTableWarpHits * 8;  // hits
-    b += (long long)Lane::kTables * (long long)table_entries(P->C, P->dev.n1, P->ncommon <= kPackedMaxCommon) * 2;  // tables
+    b += (long long)kTableCtasPerSm * ctx->nsm * kTableWarps * kTableWarpHits * 8;  // hits
+    b += (long long)Lane::kTables * (long long)table_entries(P->C, P->dev.n1) * 2;  // tables
   }
   if (test_mode || !P->same_set) b += 2 * batch * L12 * 4;  // index scratch
   return b;
@@ -275,23 +266,18 @@ int lane_grid_tasks(Lane* L, dto_pair* P, const int16_t* dX, long long xstride, 
 int ensure_table(Lane* L, dto_pair* P, int level, int tau, cudaStream_t stream, bool* built) {
   if (L->kthr_pair[level] == P->serial && L->kthr_tau[level] == tau) return DTO_OK;
   *built = true;
-  const bool packed = P->ncommon <= kPackedMaxCommon;
-  int rc = lane_grow(L, (void**)&L->dKthr[level], &L->kthrBytes[level], table_entries(P->C, P->dev.n1, packed) * 2);
+  int rc = lane_grow(L, (void**)&L->dKthr[level], &L->kthrBytes[level], table_entries(P->C, P->dev.n1) * 2);
   if (rc) return rc;
   TableArgs t{};
   t.n1 = P->dev.n1;
   t.n2 = P->dev.n2;
   t.N = (int)P->npop;
-  // the half-warp packed sweep reads 16 lanes of 2 C columns, the 32-bit
-  // sweep 32 lanes of C
-  t.C = packed ? 2 * P->C : P->C;
-  t.lanes = packed ? 16 : 32;
+  t.C = 2 * P->C;  // the half-warp sweep reads 16 lanes of 2 C columns
   t.rowstart = P->dRow;
   t.ncnt = P->dNcnt;
   t.F = P->dF;
   t.fshift = P->fshift;
   t.tau = tau;
-  t.packed = packed ? 1 : 0;
   t.mcnt = P->dMcnt;
   t.N1 = (int)P->N1;
   t.kthr = L->dKthr[level];
@@ -302,101 +288,58 @@ int ensure_table(Lane* L, dto_pair* P, int level, int tau, cudaStream_t stream, 
   return DTO_OK;
 }
 
-// Levels [lev_begin, lev_end) of the table ladder over tasks [0, ntask) of X,
-// on `stream` with hit buffer `hb`: level l takes the tasks that level l-1
-// could not settle (their minimum lies above its bound); table_exhaustive
-// takes what the last level leaves.  The lists and their counts stay on the
-// device: `fall` holds one list of ntask entries per level, `cnts` 8 task
-// counters then 4 list counts (zeroed by the launch of level 0).  Levels
-// below `tight_levels` switch to their tighter tables.
-int table_levels(Lane* L, dto_pair* P, const int16_t* X, long long xstride, int ntask, TaskResult* dOut,
-                 int lev_begin, int lev_end, int* fall, int* cnts, cudaStream_t stream, int hb, int tight_levels,
-                 bool cascade) {
-  NvtxRange range(lev_begin == 0 ? "dto: table level 0" : "dto: table levels 1-2");
+// The table ladder over tasks [0, ntask) of X, on `stream` with hit buffer
+// `hb`, in one launch: a task with no hit at level l (its minimum lies above
+// the level's bound) is swept at level l + 1 by the same half-warp, and the
+// last level's misses go to the exhaustive screen's list (table_exhaustive).
+// The list and the counts stay on the device: `fall` holds one list of ntask
+// entries per level (the last one used), `cnts` 8 task counters then 4 list
+// counts (zeroed here).  Levels below `tight_levels` switch to their tighter
+// tables.
+int table_levels(Lane* L, dto_pair* P, const int16_t* X, long long xstride, int ntask, TaskResult* dOut, int* fall,
+                 int* cnts, cudaStream_t stream, int hb, int tight_levels) {
+  NvtxRange range("dto: table sweep");
   const int cap = std::max(ntask, 1);
   const int hitcap = kTableWarpHits;
-  const bool packed = P->ncommon <= kPackedMaxCommon;
+  const int nlev = kLadderLevels;
   int rc = lane_grow(L, &L->dHits[hb], &L->hitBytes[hb], (size_t)kTableCtasPerSm * L->ctx->nsm * kTableWarps * hitcap * 8);
   if (rc) return rc;
-  if (lev_begin == 0) LCK(cudaMemsetAsync(cnts, 0, 12 * sizeof(int), stream));
-  if (cascade) {
-    // one launch over levels [0, lev_end): a task with no hit at a level is
-    // swept at the next by the same half-warp; the last level's misses go to
-    // the exhaustive screen's list (level lev_end - 1's fallback list)
-    TableGridArgs a{};
-    a.P = P->dev;
-    a.P.LF = L->ctx->dLF.load();
-    a.X = X;
-    a.xstride = xstride;
-    a.ntask = ntask;
-    a.tau = L->kthr_tau[0];
-    a.kthr = L->dKthr[0];
-    a.ntight = 0 < tight_levels ? kTightTables : 0;
-    for (int q = 0; q < a.ntight; ++q) {
-      a.tight[q] = L->dKthr[tight_slot(0, q)];
-      a.tight_tau[q] = L->kthr_tau[tight_slot(0, q)];
-    }
-    a.nlev = lev_end;
-    for (int l = 1; l < lev_end; ++l) {
-      a.kthr_up[l - 1] = L->dKthr[l];
-      a.tau_up[l - 1] = L->kthr_tau[l];
-      a.ntight_up[l - 1] = l < tight_levels ? kTightTables : 0;
-      for (int q = 0; q < a.ntight_up[l - 1]; ++q) {
-        a.tight_up[l - 1][q] = L->dKthr[tight_slot(l, q)];
-        a.tight_tau_up[l - 1][q] = L->kthr_tau[tight_slot(l, q)];
-      }
-    }
-    a.packed = 1;
-    a.route = DTO_ROUTE_LEVEL0;
-    a.smemF = table_smem_bytes(P->C, P->dev.n1, P->dev.n2, P->npop, 1, true) <= L->ctx->smem_optin ? 1 : 0;
-    a.out = dOut;
-    a.work = cnts;
-    a.n_refined = L->dRefined;
-    a.fallback = fall + (size_t)(lev_end - 1) * cap;
-    a.nfallback = cnts + 8 + lev_end - 1;
-    a.hitbuf = (int2*)L->dHits[hb];
-    a.hitcap = hitcap;
-    const int ctas = std::max(1, std::min(kTableCtasPerSm * L->ctx->nsm, ntask / (kTableWarps * 2) + 1));
-    LCK(launch_table_grid(a, P->C, ctas, stream));
-    L->acc_launches += 1;
-    return DTO_OK;
+  LCK(cudaMemsetAsync(cnts, 0, 12 * sizeof(int), stream));
+  TableGridArgs a{};
+  a.P = P->dev;
+  a.P.LF = L->ctx->dLF.load();
+  a.X = X;
+  a.xstride = xstride;
+  a.ntask = ntask;
+  a.tau = L->kthr_tau[0];
+  a.kthr = L->dKthr[0];
+  a.ntight = 0 < tight_levels ? kTightTables : 0;
+  for (int q = 0; q < a.ntight; ++q) {
+    a.tight[q] = L->dKthr[tight_slot(0, q)];
+    a.tight_tau[q] = L->kthr_tau[tight_slot(0, q)];
   }
-  for (int level = lev_begin; level < lev_end; ++level) {
-    TableGridArgs a{};
-    a.P = P->dev;
-    a.P.LF = L->ctx->dLF.load();
-    a.X = X;
-    a.xstride = xstride;
-    a.ntask = ntask;
-    a.tau = L->kthr_tau[level];
-    a.kthr = L->dKthr[level];
-    a.ntight = level < tight_levels ? kTightTables : 0;
-    for (int q = 0; q < a.ntight; ++q) {
-      a.tight[q] = L->dKthr[tight_slot(level, q)];
-      a.tight_tau[q] = L->kthr_tau[tight_slot(level, q)];
+  a.nlev = nlev;
+  for (int l = 1; l < nlev; ++l) {
+    a.kthr_up[l - 1] = L->dKthr[l];
+    a.tau_up[l - 1] = L->kthr_tau[l];
+    a.ntight_up[l - 1] = l < tight_levels ? kTightTables : 0;
+    for (int q = 0; q < a.ntight_up[l - 1]; ++q) {
+      a.tight_up[l - 1][q] = L->dKthr[tight_slot(l, q)];
+      a.tight_tau_up[l - 1][q] = L->kthr_tau[tight_slot(l, q)];
     }
-    a.packed = packed ? 1 : 0;
-    a.nlev = 1;
-    a.route = DTO_ROUTE_LEVEL0 + level;
-    a.smemF = table_smem_bytes(P->C, P->dev.n1, P->dev.n2, P->npop, 1, packed) <= L->ctx->smem_optin ? 1 : 0;
-    a.out = dOut;
-    a.work = cnts + level;
-    a.n_refined = L->dRefined;
-    a.fallback = fall + (size_t)level * cap;
-    a.nfallback = cnts + 8 + level;
-    a.task_list = level == 0 ? nullptr : fall + (size_t)(level - 1) * cap;
-    a.ntask_dev = level == 0 ? nullptr : cnts + 8 + level - 1;
-    a.hitbuf = (int2*)L->dHits[hb];
-    a.hitcap = hitcap;
-    // a later level sees the tasks the earlier ones left (about 10 % and 1 %
-    // of the batch); one warp per expected task keeps its latency to one sweep
-    const double expect = level == 0 ? 1.0 : level == 1 ? 0.15 : 0.03;
-    const int per_warp = packed ? 2 : kTableTasks;  // tasks a warp sweeps at once
-    const int want = (int)(expect * (double)ntask / (kTableWarps * per_warp)) + 1;
-    const int ctas = std::max(1, std::min(kTableCtasPerSm * L->ctx->nsm, want));
-    LCK(launch_table_grid(a, P->C, ctas, stream));
   }
-  L->acc_launches += lev_end - lev_begin;
+  a.route = DTO_ROUTE_LEVEL0;
+  a.smemF = table_smem_bytes(P->C, P->dev.n1, P->dev.n2, P->npop, 1) <= L->ctx->smem_optin ? 1 : 0;
+  a.out = dOut;
+  a.work = cnts;
+  a.n_refined = L->dRefined;
+  a.fallback = fall + (size_t)(nlev - 1) * cap;
+  a.nfallback = cnts + 8 + nlev - 1;
+  a.hitbuf = (int2*)L->dHits[hb];
+  a.hitcap = hitcap;
+  const int ctas = std::max(1, std::min(kTableCtasPerSm * L->ctx->nsm, ntask / (kTableWarps * 2) + 1));
+  LCK(launch_table_grid(a, P->C, ctas, stream));
+  L->acc_launches += 1;
   return DTO_OK;
 }
 
@@ -854,32 +797,23 @@ int lane_run_range(Lane* L, dto_pair* P, uint32_t perm_first, int64_t n_perm, ui
       if (rc) return rc;
       ladder_of(std::vector<double>(minp.begin(), minp.begin() + cnt0), P->fshift, tau);
     }
-    // The table screens: level 0's on the main stream (the first level-0
-    // sweep needs them), the later levels' on the side stream behind the
-    // first batch (their first sweeps come a level-0 sweep later; each
-    // slot's side stream waits for them).
+    // The table screens, on the main stream: the first sweep cascades
+    // through every level, so it needs all of them.
     const int tight_levels = std::min(n_perm >= kTightAllMin ? kTightLevels : 0, kLadderLevels);
-    // packed pairs sweep all levels in one cascade launch on the main stream,
-    // which needs every level's tables first
-    const bool cascade = P->ncommon <= kPackedMaxCommon;
-    bool built0 = false, built_late = false;
+    bool built = false;
     for (int l = 0; l < kLadderLevels; ++l) {
-      const bool main = l == 0 || cascade;
-      rc = ensure_table(L, P, l, tau[l], main ? L->stream : L->side, main ? &built0 : &built_late);
+      rc = ensure_table(L, P, l, tau[l], L->stream, &built);
       if (rc) return rc;
     }
     for (int l = 0; l < tight_levels; ++l)
       for (int q = 0; q < kTightTables; ++q) {
-        const bool main = l == 0 || cascade;
-        rc = ensure_table(L, P, tight_slot(l, q), tau[tight_slot(l, q)], main ? L->stream : L->side,
-                          main ? &built0 : &built_late);
+        rc = ensure_table(L, P, tight_slot(l, q), tau[tight_slot(l, q)], L->stream, &built);
         if (rc) return rc;
       }
-    if (built_late) LCK(cudaEventRecord(L->evTables, L->side));
     const int nlev = kLadderLevels;
-    // Batches in flight: while batch b's later table levels, exhaustive
-    // fallback and result copy run on its slot's side stream, the next
-    // batches' labels and level-0 table sweeps run on the main stream.
+    // Batches in flight: while batch b's exhaustive fallback and result copy
+    // run on its slot's side stream, the next batches' labels and table
+    // sweeps run on the main stream.
     auto harvest = [&](BatchSlot& sl) -> int {
       NvtxRange range("dto: result copy");
       LCK(cudaEventSynchronize(sl.ev[7]));
@@ -913,21 +847,13 @@ int lane_run_range(Lane* L, dto_pair* P, uint32_t perm_first, int64_t n_perm, ui
       int16_t* X = (int16_t*)sl.dX;
       TaskResult* dR = (TaskResult*)sl.dRes;
       LCK(cudaEventRecord(sl.ev[2], L->stream));
-      rc = table_levels(L, P, X, xs, cnt, dR, 0, cascade ? nlev : 1, (int*)sl.dFall, sl.dCnt, L->stream, 0,
-                        tight_levels, cascade);
+      rc = table_levels(L, P, X, xs, cnt, dR, (int*)sl.dFall, sl.dCnt, L->stream, 0, tight_levels);
       if (rc) return rc;
       LCK(cudaEventRecord(sl.ev[6], L->stream));
       last_l0_end = sl.ev[6];
-      const int si = (int)(it % Lane::kSlots);
       LCK(cudaStreamWaitEvent(sl.side, sl.ev[6], 0));
-      if (built_late) LCK(cudaStreamWaitEvent(sl.side, L->evTables, 0));
       LCK(cudaEventRecord(sl.ev[4], sl.side));
-      const int nl = cascade ? nlev : (it + 1 == npipe ? std::min(nlev, kLastLevels) : nlev);
-      if (!cascade) {
-        rc = table_levels(L, P, X, xs, cnt, dR, 1, nl, (int*)sl.dFall, sl.dCnt, sl.side, 1 + si, tight_levels, false);
-        if (rc) return rc;
-      }
-      rc = table_exhaustive(L, P, X, xs, cnt, dR, nl, (const int*)sl.dFall, sl.dCnt, sl.side);
+      rc = table_exhaustive(L, P, X, xs, cnt, dR, nlev, (const int*)sl.dFall, sl.dCnt, sl.side);
       if (rc) return rc;
       LCK(cudaEventRecord(sl.ev[5], sl.side));
       LCK(cudaMemcpyAsync(sl.hRes, dR, (size_t)cnt * sizeof(TaskResult), cudaMemcpyDeviceToHost, sl.side));

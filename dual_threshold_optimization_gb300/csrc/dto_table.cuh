@@ -26,11 +26,6 @@ constexpr double kTableMargin = 0.002;  // nats added to tau when the table is b
 
 __host__ __device__ constexpr int table_cq(int C) { return (C + 7) & ~7; }
 
-// Lane stride, in 32-bit words, of the packed counters: C/2 words of two
-// 16-bit column counts each, padded to whole 16-byte chunks, an odd number of
-// chunks so that a quarter-warp's 128-bit loads hit distinct banks.
-__host__ __device__ constexpr int table_wp(int C) { return 4 * ((table_cq(C) / 8) | 1); }
-
 // The first overlap k of cell (i, j) whose LBT(k) is <= tauT (binary search
 // over k), 0 when every k passes, min(K, n) + 1 when none does.
 __device__ __forceinline__ int table_thr(const TableArgs& A, uint32_t FN, double scale, int tauT, int i, int j) {
@@ -49,15 +44,12 @@ __device__ __forceinline__ int table_thr(const TableArgs& A, uint32_t FN, double
   return hi;
 }
 
-// Layout [i][q][lane][8] for A.lanes lanes of A.C columns each (32 lanes of C
-// for the 32-bit sweep, 16 lanes of 2 C for the half-warp packed sweep):
-// entry t of a lane's row is in its q = t / 8-th 16-byte chunk, so a load of
-// chunk q by the lanes reads lanes x 16 contiguous bytes.
+// Layout [i][q][lane][8] for 16 lanes of A.C (= 2 C) columns each: entry t
+// of a lane's row is in its q = t / 8-th 16-byte chunk, so a load of chunk q
+// by the lanes reads 16 x 16 contiguous bytes.
 //
-// Plain entries (one thread each) hold kthr (0xFFFF: never).
-//
-// Packed entries come in pairs, the two 16-bit halves of one word of the
-// sweep (columns t, t + 1, t even; one thread a pair).  The sweep holds a
+// Entries come in pairs, the two 16-bit halves of one word of the sweep
+// (columns t, t + 1, t even; one thread a pair).  The sweep holds a
 // cell's overlap o in a 16-bit half (o <= N1 <= 65534) and adds the entry
 // with one 32-bit add to both halves at once; bit 15 (31) of the sum must
 // be set exactly when o >= kthr.  A cell's overlap lies in
@@ -71,25 +63,19 @@ __device__ __forceinline__ int table_thr(const TableArgs& A, uint32_t FN, double
 // entry takes back (it is one less).  A column past the grid (padding) has
 // the overlap of the last column and the entry "never" (kthr = U + 1).
 static __global__ void table_build_kernel(const TableArgs A) {
+  constexpr int lanes = 16;
   const int Cq = table_cq(A.C);
-  const int lanes = A.lanes;
   const long long cells = (long long)A.n1 * lanes * Cq;
   const double scale = ldexp(1.0, A.fshift);
   const int tauT = A.tau + (int)ceil(kTableMargin * scale);
   const uint32_t FN = __ldg(A.F + A.N);
-  const long long step = A.packed ? 2 : 1;
-  for (long long c = ((long long)blockIdx.x * blockDim.x + threadIdx.x) * step; c < cells;
-       c += (long long)gridDim.x * blockDim.x * step) {
+  for (long long c = ((long long)blockIdx.x * blockDim.x + threadIdx.x) * 2; c < cells;
+       c += (long long)gridDim.x * blockDim.x * 2) {
     const int i = (int)(c / (lanes * Cq));
     const int rem = (int)(c % (lanes * Cq));
     const int q = rem / (8 * lanes), lane = (rem / 8) % lanes;
     const int t = 8 * q + rem % 8;
     const int j = lane * A.C + t;
-    if (!A.packed) {
-      const int thr = (t < A.C && j < A.n2) ? table_thr(A, FN, scale, tauT, i, j) : 0x10000;
-      A.kthr[c] = (uint16_t)min(thr, 0xFFFF);
-      continue;
-    }
     const int K = __ldg(A.rowstart + i + 1);
     int k2[2];
 #pragma unroll
@@ -126,20 +112,11 @@ struct WarpTask {
   int pad2;
 };
 
-// Shared memory of one warp: per task the column counters, the lane totals,
-// a WarpTask and the survivors (they outlive a chunked resolve, so each task
-// keeps its own); then the candidate and deferred-FP64 buffers, which hold
-// one task's entries at a time (candidates) or are tagged by task (FP64).
-__host__ __device__ constexpr int table_task_ints(int C) {
-  return grid_cnt_ints(C) + 32 + (int)(sizeof(WarpTask) / 4) + 3 * kTableSurvCap;
-}
-__host__ __device__ constexpr int table_warp_ints(int C) {
-  return kTableTasks * table_task_ints(C) + 2 * kCandCap + 5 * kPend;
-}
-
+// A task's view of its warp's shared memory (hw_warp_mem): its column
+// counters, its WarpTask and survivors, and the warp's candidate and
+// deferred-FP64 buffers.
 struct TableWarpMem {
   int* cnt;
-  int* tot;
   int2* cand;
   int* survCell;
   int* survK;
@@ -151,25 +128,6 @@ struct TableWarpMem {
   int* pendCell;
   int* pendK;
 };
-
-__device__ __forceinline__ TableWarpMem table_warp_mem(int* base, int C, int t) {
-  TableWarpMem m;
-  int* tb = base + t * table_task_ints(C);
-  m.cnt = tb;
-  m.tot = tb + grid_cnt_ints(C);
-  m.st = reinterpret_cast<WarpTask*>(m.tot + 32);
-  m.q = reinterpret_cast<WarpTask*>(base + grid_cnt_ints(C) + 32);
-  m.survCell = reinterpret_cast<int*>(m.st + 1);
-  m.survK = m.survCell + kTableSurvCap;
-  m.survLo = m.survK + kTableSurvCap;
-  int* sh = base + kTableTasks * table_task_ints(C);
-  m.cand = reinterpret_cast<int2*>(sh);
-  m.pendP = reinterpret_cast<double*>(m.cand + kCandCap);
-  m.pendTask = reinterpret_cast<int*>(m.pendP + kPend);
-  m.pendCell = m.pendTask + kPend;
-  m.pendK = m.pendCell + kPend;
-  return m;
-}
 
 // Pair tables one CTA reads in the resolve paths: row sizes K (rowstart),
 // column sizes n and the fixed-point ln m! table, in shared memory when the
@@ -432,293 +390,6 @@ __device__ __forceinline__ int lv_tight_tau(const TableGridArgs& A, int l, int q
   return q == 0 ? A.tight_tau_up[1][0] : q == 1 ? A.tight_tau_up[1][1] : A.tight_tau_up[1][2];
 }
 
-template <int C, bool Packed>
-__global__ void __launch_bounds__(kTableWarps * 32, kTableCtasPerSm) table_grid_kernel(const TableGridArgs A) {
-  constexpr int T = kTableTasks;
-  constexpr int Cp = C | 1;
-  constexpr int Cq = table_cq(C);
-  constexpr int NQ = Cq / 8;  // 16-byte table chunks per lane per row
-  constexpr int NW = C / 2;   // packed counter words per lane
-  constexpr int Wp = table_wp(C);
-  static_assert(C % 2 == 0, "packed columns come in pairs");
-  static_assert(32 * Wp <= grid_cnt_ints(C), "packed counters fit the counter area");
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int n1 = A.P.n1;
-
-  const int Npop = (int)A.P.Npop;
-  uint32_t* sF = reinterpret_cast<uint32_t*>(smem_raw);
-  int* sRow = reinterpret_cast<int*>(sF + (A.smemF ? ((Npop + 1 + 3) & ~3) : 0));
-  int* sNcnt = sRow + ((n1 + 1 + 3) & ~3);
-  int* sWarp = sNcnt + ((A.P.n2 + 3) & ~3);
-  // per task t: counters at wb + t * TTI, lane totals GCI further, then its WarpTask
-  int* const wb = sWarp + warp * table_warp_ints(C);
-  constexpr int TTI = table_task_ints(C), GCI = grid_cnt_ints(C);
-  auto cnt_of = [&](int t) { return wb + t * TTI; };
-  auto tot_of = [&](int t) { return wb + t * TTI + GCI; };
-  auto st_of = [&](int t) { return reinterpret_cast<WarpTask*>(wb + t * TTI + GCI + 32); };
-  for (int q = threadIdx.x; q <= n1; q += blockDim.x) sRow[q] = __ldg(A.P.rowstart + q);
-  for (int q = threadIdx.x; q < A.P.n2; q += blockDim.x) sNcnt[q] = __ldg(A.P.ncnt + q);
-  if (A.smemF)
-    for (int q = threadIdx.x; q <= Npop; q += blockDim.x) sF[q] = __ldg(A.P.F + q);
-  const TabGrid g{sRow, sNcnt, A.smemF ? sF : A.P.F};
-  if (lane == 0) {
-    st_of(0)->n32 = 0;
-    st_of(0)->n64 = 0;
-    st_of(0)->npend = 0;
-  }
-  __syncthreads();
-  const uint4* ktab = reinterpret_cast<const uint4*>(A.kthr);
-  // the warp's hit buffer, split between its tasks
-  const int hcap = A.hitcap / T;
-  int2* hbw = A.hitbuf + (size_t)(blockIdx.x * kTableWarps + warp) * A.hitcap;
-  unsigned long long nfall = 0;
-
-  const int ntask = A.ntask_dev ? *((volatile const int*)A.ntask_dev) : A.ntask;
-  for (;;) {
-    int b0 = 0;
-    if (lane == 0) b0 = atomicAdd(A.work, T);
-    b0 = __shfl_sync(kFull, b0, 0);
-    if (b0 >= ntask) break;
-    // tasks b0 .. b0+T-1 (those below ntask); a missing task sweeps nothing
-    int bt[T];
-    bool live[T];
-    const int* x32[T];
-#pragma unroll
-    for (int t = 0; t < T; ++t) {
-      live[t] = b0 + t < ntask;
-      bt[t] = live[t] ? (A.task_list ? A.task_list[b0 + t] : b0 + t) : -1;
-      x32[t] = reinterpret_cast<const int*>(A.X + (long long)(live[t] ? bt[t] : 0) * A.xstride);
-      if (lane == 0) {
-        WarpTask* st = st_of(t);
-        st->B = A.tau;
-        st->B_valid = 0;
-        st->ncand = 0;
-        st->nsurv = 0;
-        st->nhits = 0;
-        Best z = best_init();
-        st->bp = z.p;
-        st->bk = z.k;
-        st->bi = z.i;
-        st->bj = z.j;
-      }
-      for (int q = lane; q < 32 * Cp; q += 32) cnt_of(t)[q] = 0;
-      tot_of(t)[lane] = 0;
-    }
-    __syncwarp();
-    // Labels are read as 32-bit words (two labels each); a row's words are
-    // prefetched one row ahead, 64 words (128 labels) per warp and task.  X
-    // rows start 16-byte aligned and are padded to a multiple of 8 labels.
-    int s = sRow[0], e = sRow[1];
-    int w0[T], w1[T];
-#pragma unroll
-    for (int t = 0; t < T; ++t) {
-      const int q0 = (s >> 1) + lane;
-      w0[t] = (live[t] && 2 * q0 < e) ? __ldg(x32[t] + q0) : -1;
-      w1[t] = (live[t] && 2 * (q0 + 32) < e) ? __ldg(x32[t] + q0 + 32) : -1;
-    }
-    bool anyhits[T];
-#pragma unroll
-    for (int t = 0; t < T; ++t) anyhits[t] = false;
-    uint4 kt[NQ];
-    // the table this task's rows are compared with (level's own, or tighter)
-    const uint4* ktab_cur = ktab;
-    int cur_tight = -1;
-    // a label is the counter slot lane * Cp + t of its column lane * C + t
-    auto add_lab = [&](int t, int lab) {
-      const int l = lab / Cp;
-      if (Packed) {
-        const int tc = lab - l * Cp;
-        atomicAdd(reinterpret_cast<uint32_t*>(cnt_of(t)) + l * Wp + (tc >> 1), 1u << ((tc & 1) << 4));
-      } else {
-        atomicAdd(&cnt_of(t)[lab], 1);
-      }
-      atomicAdd(&tot_of(t)[l], 1);
-    };
-    auto add_word = [&](int t, int w, int q, int rs, int re) {
-      const int p = 2 * q;
-      const int lab0 = (int)(short)(w & 0xffff), lab1 = w >> 16;  // sign-extended labels
-      if (p >= rs && p < re && lab0 >= 0) add_lab(t, lab0);
-      if (p + 1 >= rs && p + 1 < re && lab1 >= 0) add_lab(t, lab1);
-    };
-    auto push_hit = [&](int t, int i, int tcol, int k) {
-      const int pos = atomicAdd(&st_of(t)->nhits, 1);
-      if (pos < hcap) hbw[t * hcap + pos] = make_int2((i << 16) | (lane * C + tcol), k);
-    };
-    for (int i = 0; i < n1; ++i) {
-      int c0[T], c1[T];
-      const int sN = e;
-      const int eN = (i + 2 <= n1) ? sRow[i + 2] : e;
-#pragma unroll
-      for (int t = 0; t < T; ++t) {
-        c0[t] = w0[t];
-        c1[t] = w1[t];
-        const int q0 = (sN >> 1) + lane;
-        w0[t] = (live[t] && 2 * q0 < eN) ? __ldg(x32[t] + q0) : -1;
-        // the second 64 labels, only for rows that long (uniform branch)
-        w1[t] = -1;
-        if (eN > 2 * (sN >> 1) + 64 && live[t] && 2 * (q0 + 32) < eN) w1[t] = __ldg(x32[t] + q0 + 32);
-      }
-      // this row's table chunks: consumed after the label updates and the scan
-#pragma unroll
-      for (int u = 0; u < NQ; ++u) kt[u] = __ldg(ktab_cur + ((size_t)i * NQ + u) * 32 + lane);
-#pragma unroll
-      for (int t = 0; t < T; ++t) {
-        const int q0 = (s >> 1) + lane;
-        add_word(t, c0[t], q0, s, e);
-        if (e > 2 * (s >> 1) + 64) {  // a row of more than 64 labels (uniform)
-          add_word(t, c1[t], q0 + 32, s, e);
-          if (live[t])
-            for (int q = q0 + 64; 2 * q < e; q += 32) add_word(t, __ldg(x32[t] + q), q, s, e);
-        }
-      }
-      __syncwarp();
-      int excl[T];
-#pragma unroll
-      for (int t = 0; t < T; ++t) {
-        const int mine = tot_of(t)[lane];
-        int incl = mine;
-#pragma unroll
-        for (int d = 1; d < 32; d <<= 1) {
-          int y = __shfl_up_sync(kFull, incl, d);
-          if (lane >= d) incl += y;
-        }
-        excl[t] = incl - mine;  // overlap before this lane's first column
-      }
-      if (Packed) {
-        // y[w] = (overlap of column 2w+1) << 16 | (overlap of column 2w);
-        // R carries the running overlap in both halves
-        uint32_t acc[T];
-        uint32_t R[T];
-#pragma unroll
-        for (int t = 0; t < T; ++t) {
-          R[t] = (uint32_t)excl[t] * 0x10001u;
-          acc[t] = 0;
-        }
-#pragma unroll
-        for (int u = 0; u < NQ; ++u) {
-          uint4 c4[T];
-#pragma unroll
-          for (int t = 0; t < T; ++t)
-            c4[t] = *reinterpret_cast<const uint4*>(reinterpret_cast<const uint32_t*>(cnt_of(t)) + lane * Wp + 4 * u);
-          const uint32_t tv[4] = {kt[u].x, kt[u].y, kt[u].z, kt[u].w};
-#pragma unroll
-          for (int c = 0; c < 4; ++c) {
-            if (4 * u + c < NW) {
-#pragma unroll
-              for (int t = 0; t < T; ++t) {
-                const uint32_t cv = (c == 0) ? c4[t].x : (c == 1) ? c4[t].y : (c == 2) ? c4[t].z : c4[t].w;
-                const uint32_t v = cv * 0x10001u + R[t];
-                R[t] = __byte_perm(v, 0, 0x3232);
-                acc[t] |= v + tv[c];
-              }
-            }
-          }
-        }
-#pragma unroll
-        for (int t = 0; t < T; ++t) {
-          if (acc[t] & 0x80008000u) {
-            // a hit in this lane's columns: redo the chain and record the cells
-            uint32_t Rh = (uint32_t)excl[t] * 0x10001u;
-#pragma unroll
-            for (int u = 0; u < NQ; ++u) {
-              const uint4 c4 = *reinterpret_cast<const uint4*>(reinterpret_cast<const uint32_t*>(cnt_of(t)) + lane * Wp + 4 * u);
-              const uint32_t cvs[4] = {c4.x, c4.y, c4.z, c4.w};
-              const uint32_t tv[4] = {kt[u].x, kt[u].y, kt[u].z, kt[u].w};
-#pragma unroll
-              for (int c = 0; c < 4; ++c) {
-                if (4 * u + c < NW) {
-                  const int w = 4 * u + c;
-                  const uint32_t v = cvs[c] * 0x10001u + Rh;
-                  Rh = __byte_perm(v, 0, 0x3232);
-                  const uint32_t d = v + tv[c];
-                  if (d & 0x8000u) push_hit(t, i, 2 * w, (int)(v & 0xFFFFu));
-                  if (d & 0x80000000u) push_hit(t, i, 2 * w + 1, (int)(v >> 16));
-                }
-              }
-            }
-          }
-        }
-      } else {
-#pragma unroll
-        for (int t = 0; t < T; ++t) {
-          int k = excl[t];
-#pragma unroll
-          for (int tc = 0; tc < C; ++tc) {
-            k += cnt_of(t)[lane * Cp + tc];
-            const uint4 v = kt[tc / 8];
-            const uint32_t w = ((tc % 8) / 2 == 0) ? v.x : ((tc % 8) / 2 == 1) ? v.y : ((tc % 8) / 2 == 2) ? v.z : v.w;
-            const int thr = (tc & 1) ? (int)(w >> 16) : (int)(w & 0xFFFFu);
-            if (k >= thr) push_hit(t, i, tc, k);  // columns past n2 hold 0xFFFF, above any overlap
-          }
-        }
-      }
-      // the next row's counter updates wait for every lane's reads of this row
-      __syncwarp();
-      // every fourth row: could a task's buffer overflow within the next four
-      // rows (hcap leaves room for four full rows)?  Or has a task gathered
-      // kEarlyHits hits while a tighter table is left?  Then
-      // resolve what it holds; the bound B it sets lets the remaining rows be
-      // compared with the tightest table whose bound is still >= B: every
-      // cell with ln p <= B (the final B is lower still) stays a hit.
-      if ((i & 3) == 3) {
-#pragma unroll
-        for (int t = 0; t < T; ++t) {
-          const int nh = st_of(t)->nhits;
-          if (nh > hcap - 4 * 32 * C || (T == 1 && cur_tight + 1 < A.ntight && nh >= kEarlyHits)) {
-            table_resolve(A, g, table_warp_mem(wb, C, t), lane, hbw + t * hcap, nh);
-            anyhits[t] = true;
-            __syncwarp();
-            if (lane == 0) st_of(t)->nhits = 0;
-            if (T == 1 && st_of(t)->B_valid) {
-              const int B = st_of(t)->B;
-              for (int q = A.ntight - 1; q > cur_tight; --q) {
-                if (tight_tau_of(A, q) >= B) {
-                  cur_tight = q;
-                  ktab_cur = reinterpret_cast<const uint4*>(tight_of(A, q));
-                  break;
-                }
-              }
-            }
-            __syncwarp();
-          }
-        }
-      }
-      s = sN;
-      e = eN;
-    }
-    __syncwarp();
-#pragma unroll
-    for (int t = 0; t < T; ++t) {
-      if (!live[t]) continue;
-      const TableWarpMem mt = table_warp_mem(wb, C, t);
-      const int nh = mt.st->nhits;
-      if (nh > 0) table_resolve(A, g, mt, lane, hbw + t * hcap, nh);
-      if ((nh > 0 || anyhits[t]) && mt.st->B_valid) {
-        if (isinf(mt.st->bp)) {
-          // no FP64 tail evaluated yet for this task: queue its survivors
-          table_defer(A, g, mt, lane, bt[t], A.route);
-        } else {
-          table_refine(A, g, mt, lane);
-          if (lane == 0) A.out[bt[t]] = TaskResult{mt.st->bp, mt.st->bi, mt.st->bj, mt.st->bk, A.route};
-        }
-      } else {
-        // no cell reaches the guess: the next level (or the exhaustive
-        // screen) takes the task
-        if (lane == 0) A.fallback[atomicAdd(A.nfallback, 1)] = bt[t];
-        ++nfall;
-      }
-      __syncwarp();
-    }
-  }
-  if (st_of(0)->npend > 0) table_pending_flush(A, g, table_warp_mem(wb, C, 0), lane);
-  if (lane == 0 && A.n_refined) {
-    atomicAdd(A.n_refined, st_of(0)->n64);
-    atomicAdd(A.n_refined + 1, st_of(0)->n32);
-    atomicAdd(A.n_refined + 2, nfall);
-  }
-}
-
 // ---------------------------------------------------------------------------
 // The packed sweep with a half-warp per task.
 //
@@ -734,12 +405,13 @@ __global__ void __launch_bounds__(kTableWarps * 32, kTableCtasPerSm) table_grid_
 //      word's two partial overlaps in registers; the chains' totals give the
 //      lane's total, and a 4-step scan over the half-warp its offset E;
 //   3. overlap + (0x8000 - kthr) sets bit 15 (31) of a half exactly when the
-//      overlap reaches the table's threshold, tested for all words with one
-//      OR; only a lane with a set bit records its hits, straight from the
-//      registers.
-// Overlaps stay below 0x8000 (the lists share at most 0x7FFF features), so no
-// half carries into the other.  The hits, resolves and task ends are those of
-// table_grid_kernel (one task at a time, the whole warp).
+//      overlap reaches the table's threshold (the entries' form, built by
+//      table_build_kernel, keeps every sum inside its half), tested for all
+//      words with one OR; only a lane with a set bit records its hits,
+//      straight from the registers.
+// Overlaps are at most N1 <= 65534, so the counters and partial sums never
+// carry from one half into the other.  The hits are resolved one task at a
+// time by the whole warp.
 // ---------------------------------------------------------------------------
 __host__ __device__ constexpr int hw_cq(int C2) { return (C2 + 7) & ~7; }
 // counter words per lane: C2 / 2 words padded to an odd number of 16-byte
@@ -757,7 +429,6 @@ __device__ __forceinline__ TableWarpMem hw_warp_mem(int* base, int C2, int t) {
   TableWarpMem m;
   int* tb = base + t * hw_task_ints(C2);
   m.cnt = tb;
-  m.tot = nullptr;
   m.st = reinterpret_cast<WarpTask*>(tb + 16 * hw_wp(C2));
   m.q = reinterpret_cast<WarpTask*>(base + 16 * hw_wp(C2));
   m.survCell = reinterpret_cast<int*>(m.st + 1);
@@ -1157,21 +828,12 @@ cudaError_t launch_table_hw_kernel(const TableGridArgs& a, int ctas, size_t smem
   return cudaGetLastError();
 }
 
-template <int C, bool Packed>
-cudaError_t launch_table_grid_kernel(const TableGridArgs& a, int ctas, size_t smem, cudaStream_t s) {
-  cudaError_t e = raise_smem_limit((const void*)table_grid_kernel<C, Packed>, smem);
-  if (e != cudaSuccess) return e;
-  table_grid_kernel<C, Packed><<<ctas, kTableWarps * 32, smem, s>>>(a);
-  return cudaGetLastError();
-}
-
-// Packed pairs take the half-warp sweep (2 C columns per lane), the others
-// the 32-bit sweep of table_grid_kernel.
+// The half-warp sweep of 2 C columns per lane: one pair, or several
+// (segments) of the same C.
 template <int C>
 cudaError_t launch_table_grid_impl(const TableGridArgs& a, int ctas, size_t smem, cudaStream_t s) {
   if (a.segs) return launch_table_hw_kernel<2 * C, true>(a, ctas, smem, s);
-  return a.packed ? launch_table_hw_kernel<2 * C, false>(a, ctas, smem, s)
-                  : launch_table_grid_kernel<C, false>(a, ctas, smem, s);
+  return launch_table_hw_kernel<2 * C, false>(a, ctas, smem, s);
 }
 
 }  // namespace dto

@@ -53,7 +53,7 @@ bool wave_taus(dto_ctx* ctx, dto_pair* P, int tau[kLadderTaus]) {
 int wave_table(Lane* L, dto_pair* P, int level, int tau, long long* launches) {
   if (P->wave_ok[level] && P->wave_tau[level] == tau) return DTO_OK;
   if (!P->dWaveKthr[level]) {
-    const size_t bytes = table_entries(P->C, P->dev.n1, true) * 2;
+    const size_t bytes = table_entries(P->C, P->dev.n1) * 2;
     if (cudaMalloc(&P->dWaveKthr[level], bytes) != cudaSuccess) {
       cudaGetLastError();
       P->dWaveKthr[level] = nullptr;
@@ -65,13 +65,11 @@ int wave_table(Lane* L, dto_pair* P, int level, int tau, long long* launches) {
   t.n2 = P->dev.n2;
   t.N = (int)P->npop;
   t.C = 2 * P->C;  // the half-warp sweep's 16 lanes of 2 C columns
-  t.lanes = 16;
   t.rowstart = P->dRow;
   t.ncnt = P->dNcnt;
   t.F = P->dF;
   t.fshift = P->fshift;
   t.tau = tau;
-  t.packed = 1;
   t.mcnt = P->dMcnt;
   t.N1 = (int)P->N1;
   t.kthr = P->dWaveKthr[level];
@@ -189,7 +187,6 @@ int enqueue_wave(Lane* L, std::vector<WaveJob>& jobs, Wave& wv) {
       a.tau_up[l - 1] = job(k).tau[l];
       a.ntight_up[l - 1] = 0;
     }
-    a.packed = 1;
     a.route = DTO_ROUTE_LEVEL0;
     a.smemF = 0;
     a.out = dRes + wv.roff[(size_t)k] + 1;
@@ -207,7 +204,6 @@ int enqueue_wave(Lane* L, std::vector<WaveJob>& jobs, Wave& wv) {
     NvtxRange sr("dto: wave sweep");
     TableGridArgs la{};
     la.P = job(0).P->dev;
-    la.packed = 1;
     la.hitbuf = (int2*)L->dHits[0];
     la.hitcap = kTableWarpHits;
     la.segs = (const TableGridArgs*)B.dSegs;
@@ -311,7 +307,7 @@ long long wave_label_bytes(const dto_pair* P, int64_t n_perm) { return (n_perm +
 
 bool wave_eligible(dto_ctx* ctx, dto_pair* P, int64_t n_perm, int precision) {
   if (!ctx || !P || P->ctx != ctx) return false;
-  if (precision != DTO_PRECISION_SCREEN || !P->same_set || P->ncommon > kPackedMaxCommon) return false;
+  if (precision != DTO_PRECISION_SCREEN || !P->same_set) return false;
   if (n_perm < kWaveMinPerm || n_perm > kWaveMaxPerm) return false;
   int tau[kLadderTaus];
   return wave_taus(ctx, P, tau);

@@ -245,9 +245,9 @@ DTO_API double dto_fdr(int64_t set1_len, int64_t set2_len, int64_t overlap, int6
  * working set (dto_run_device_bytes) fits under mem_budget bytes next to the
  * requests running (mem_budget 0: no budget; a request larger than the budget
  * runs alone).  A worker that admits a short screen request (1,025 to 32,767
- * permutations of lists over one feature set that share at most 32,767
- * features, with a ladder from an earlier run of the pair or of a pair of its
- * shape) also takes the queued requests of that kind that fit, in arrival
+ * permutations of lists over one feature set, with a ladder from an earlier
+ * run of the pair or of a pair of its shape) also takes the queued requests
+ * of that kind that fit, in arrival
  * order, and sweeps their tasks together in waves (one launch over several
  * pairs).  A request's results equal dto_run_range's for the same arguments,
  * whatever runs beside it. */

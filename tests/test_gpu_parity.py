@@ -209,8 +209,10 @@ def test_pipelined_batches_equal_short_runs(engine, kind):
 
 
 def test_table_sweep_beyond_16_bit_overlaps(engine):
-    # 40,000 shared features: overlaps exceed 0x7FFF, so the table screen takes
-    # its 32-bit sweep; its optima must equal the exhaustive screen's (runs of
+    # 40,000 shared features: overlaps exceed 0x7FFF, so the table entries
+    # wrap in their 16-bit halves (each clamped to its cell's overlap range,
+    # the low half's carry taken back by the high one); the optima must
+    # equal the exhaustive screen's (runs of
     # at most 2,048 permutations take the exhaustive screen alone)
     p = synth.copula_pair(40000, 0.1, seed=59)
     dp = engine.pair(p.ranks1, p.feat1, p.ranks2, p.feat2, p.n_features, p.population)

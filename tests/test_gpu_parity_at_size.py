@@ -10,8 +10,8 @@ screen of what the ladder leaves) is run on the benchmark workloads:
 * 25,000-feature rankings restricted to an 18,000-feature background with
   geometric tie blocks (gapped ranks);
 * two 20,000-feature lists over different feature sets (two shuffles composed);
-* one pair of 60,000 features (700 x 700 thresholds, overlaps beyond 16 bits:
-  the 32-bit table sweep).
+* one pair of 60,000 features (700 x 700 thresholds, overlaps beyond 0x7FFF:
+  table entries that wrap in their 16-bit halves).
 
 For each run, a sample of permutation ids is taken from every route that
 settled tasks (dto_result.route), plus the hardest tasks (largest and smallest
@@ -91,7 +91,7 @@ CASES = [
     ("different_feature_sets_n20000",
      lambda: synth.small_pair(20000, 0.2, seed=58, subset1=19000, subset2=19500), 15_000,
      {SCREEN, LEVEL0}),
-    ("n60000_32bit_overlaps", lambda: synth.copula_pair(60000, 0.15, seed=71), 6_000,
+    ("n60000_overlaps_beyond_0x7fff", lambda: synth.copula_pair(60000, 0.15, seed=71), 6_000,
      {SCREEN, LEVEL0}),
 ]
 
