@@ -214,6 +214,9 @@ int dto_ctx_create(int device, dto_ctx** out) {
     delete ctx;
     return rc;
   }
+  // a new pair of the shape of an earlier one starts from that pair's ladder
+  // (LadderModel): its first run skips the exhaustive first batch
+  ctx->lane0->use_model = true;
   *out = ctx;
   return DTO_OK;
 }

@@ -76,8 +76,8 @@ struct Lane {
   // throughput is higher
   bool coop_first = true;
   // a pair without a ladder of its own starts from the ladder of an earlier
-  // pair of the same shape (LadderModel), skipping its first batch (server
-  // and batch lanes: many pairs, each run once)
+  // pair of the same shape (LadderModel), skipping its first batch (every
+  // lane of a context and its servers)
   bool use_model = false;
   cudaStream_t stream = nullptr;
   cudaStream_t side = nullptr;  // first batch, unpermuted task, fallbacks

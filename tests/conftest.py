@@ -18,3 +18,13 @@ def engine():
     e = Engine(0)
     yield e
     e.close()
+
+
+@pytest.fixture
+def fresh_engine():
+    """A context of its own: no ladders of earlier pairs' shapes, so a new
+    pair's first long run measures its ladder from a first batch."""
+    from dual_threshold_optimization_gb300 import Engine
+    e = Engine(0)
+    yield e
+    e.close()

@@ -97,7 +97,8 @@ CASES = [
 
 
 @pytest.mark.parametrize("name,make,P,must", CASES, ids=[c[0] for c in CASES])
-def test_production_path_vs_oracle_at_size(engine, name, make, P, must):
+def test_production_path_vs_oracle_at_size(fresh_engine, name, make, P, must):
+    engine = fresh_engine
     pair = make()
     dp = engine.pair(pair.ranks1, pair.feat1, pair.ranks2, pair.feat2, pair.n_features,
                      pair.population)
