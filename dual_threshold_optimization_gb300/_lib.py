@@ -27,7 +27,8 @@ PRECISION_SCREEN = 1
 EXPORTS = (
     "dto_version", "dto_status_string", "dto_ctx_create", "dto_ctx_destroy", "dto_last_error",
     "dto_ctx_stream", "dto_generate_thresholds", "dto_rank_order", "dto_pair_create", "dto_pair_destroy",
-    "dto_pair_info", "dto_pair_thresholds", "dto_pair_order", "dto_pair_upload_bytes", "dto_pair_set_stream", "dto_pair_set_ladder", "dto_run", "dto_run_range", "dto_run_range_noalloc",
+    "dto_pair_info", "dto_pair_thresholds", "dto_pair_order", "dto_pair_upload_bytes", "dto_pair_set_stream", "dto_pair_set_ladder",
+    "dto_pair_set_level0_quantile", "dto_pair_tune", "dto_run", "dto_run_range", "dto_run_range_noalloc",
     "dto_optimize",
     "dto_grid_dump", "dto_hypergeom_sf", "dto_export_permutations", "dto_fdr",
     "dto_serve_create", "dto_serve_destroy", "dto_serve_submit", "dto_serve_poll", "dto_serve_wait",
@@ -116,6 +117,10 @@ def lib():
     L.dto_pair_set_stream.restype = C.c_int
     L.dto_pair_set_ladder.argtypes = [_P, _P, C.c_int64]
     L.dto_pair_set_ladder.restype = C.c_int
+    L.dto_pair_set_level0_quantile.argtypes = [_P, C.c_double]
+    L.dto_pair_set_level0_quantile.restype = C.c_int
+    L.dto_pair_tune.argtypes = [_P, _P, C.c_int64, C.c_uint64, C.POINTER(C.c_double)]
+    L.dto_pair_tune.restype = C.c_int
     L.dto_pair_upload_bytes.restype = C.c_int64
     L.dto_run.argtypes = [_P, _P, C.c_int64, C.c_uint64, _P, C.c_int, C.POINTER(DtoResult), _P,
                           _P, C.POINTER(DtoSummary)]

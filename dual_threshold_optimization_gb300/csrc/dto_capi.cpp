@@ -456,10 +456,72 @@ int dto_pair_set_ladder(dto_pair* P, const double* minp, int64_t count) {
   std::lock_guard<std::mutex> g(P->ladder_mu);
   if (count == 0) {
     P->ladder_ok = false;
+    P->ladder_sample.clear();
     return DTO_OK;
   }
-  ladder_of(v, P->fshift, P->ladder_tau);
+  ladder_of(v, P->fshift, P->ladder_tau, P->q0);
   P->ladder_ok = true;
+  P->ladder_sample = v;
+  return DTO_OK;
+}
+
+int dto_pair_set_level0_quantile(dto_pair* P, double q0) {
+  if (!P) return DTO_ERR_INVALID;
+  if (!(q0 >= 0.5 && q0 <= 0.99))
+    return set_err(P->ctx, DTO_ERR_INVALID, "dto_pair_set_level0_quantile: the quantile must lie in [0.5, 0.99]");
+  std::lock_guard<std::mutex> g(P->ladder_mu);
+  P->q0 = q0;
+  // the ladder again from the last run's sample, at the new quantile
+  if (P->ladder_ok && !P->ladder_sample.empty()) ladder_of(P->ladder_sample, P->fshift, P->ladder_tau, q0);
+  return DTO_OK;
+}
+
+int dto_pair_tune(dto_ctx* ctx, dto_pair* P, int64_t n_perm, uint64_t seed, double* best_quantile) {
+  if (int rc = pair_check(ctx, P, "dto_pair_tune")) return rc;
+  if (n_perm <= 1024 || n_perm > 0x7fffffffLL)
+    return set_err(ctx, DTO_ERR_INVALID,
+                   "dto_pair_tune: n_perm must take the table ladder (more than 1,024 permutations)");
+  // the candidates' timed runs, on the context's own lane: one run first
+  // (the ladder, the kernels loaded), then two runs per candidate, the
+  // fastest device time of each counted
+  static const double kCandidates[3] = {0.80, 0.85, 0.90};
+  std::vector<double> minp((size_t)n_perm);
+  dto_result unperm{};
+  dto_summary sum{};
+  auto run = [&](uint64_t s) -> int {
+    std::lock_guard<std::mutex> g(ctx->mu);
+    return lane_run_range(ctx->lane0, P, 1u, n_perm, s, nullptr, DTO_PRECISION_SCREEN, &unperm, minp.data(),
+                          nullptr, &sum);
+  };
+  int rc = run(seed);
+  if (rc) return rc;
+  double best_q = 0.0, best_ms = 1e300;
+  uint64_t s = seed + 1;
+  for (double q : kCandidates) {
+    rc = dto_pair_set_level0_quantile(P, q);
+    if (rc) return rc;
+    double ms = 1e300;
+    for (int r = 0; r < 3; ++r) {
+      rc = run(s++);
+      if (rc) return rc;
+      if (r > 0) ms = std::min(ms, sum.device_ms);  // the first rebuilds the tables
+    }
+    if (ms < best_ms) {
+      best_ms = ms;
+      best_q = q;
+    }
+  }
+  rc = dto_pair_set_level0_quantile(P, best_q);
+  if (rc) return rc;
+  {
+    // pairs of this shape start with it (LadderModel)
+    std::lock_guard<std::mutex> g(P->ladder_mu);
+    LadderShape x = shape_of(P);
+    for (int l = 0; l < kLadderTaus; ++l) x.nats[l] = std::ldexp((double)P->ladder_tau[l], -P->fshift);
+    x.q0 = best_q;
+    ctx->ladders.record(x);
+  }
+  if (best_quantile) *best_quantile = best_q;
   return DTO_OK;
 }
 

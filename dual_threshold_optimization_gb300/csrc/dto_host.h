@@ -150,6 +150,7 @@ struct LadderShape {
   int n1, n2;
   bool same_set;
   double nats[kLadderTaus];
+  double q0;  // the level-0 quantile the ladder was built with
 };
 
 struct LadderModel {
@@ -158,7 +159,7 @@ struct LadderModel {
   static constexpr size_t kMaxShapes = 4096;
   static constexpr double kTol = 0.05;  // relative difference accepted per size
   void record(const LadderShape& x);
-  bool lookup(const LadderShape& want, double nats[kLadderTaus]);
+  bool lookup(const LadderShape& want, double nats[kLadderTaus], double* q0 = nullptr);
 };
 
 }  // namespace dto
@@ -210,6 +211,11 @@ struct dto_pair {
   std::mutex ladder_mu;
   bool ladder_ok = false;
   int ladder_tau[dto::kLadderTaus] = {};
+  // the level-0 quantile of its ladder (0: the default, dto::kLevel0Quantile),
+  // and an evenly strided sample of the last run's minimum p-values, from
+  // which a new quantile rebuilds the ladder (dto_pair_set_level0_quantile)
+  double q0 = 0.0;
+  std::vector<double> ladder_sample;
   // The table screens of levels 0..2 that dto_batch_run's waves built for
   // this pair, kept with it (a wave sweeps several pairs at once, so each
   // needs its own; the next batch finds them).  Guarded by the context mutex.
@@ -263,7 +269,9 @@ int lane_run_range(Lane* L, dto_pair* P, uint32_t perm_first, int64_t n_perm, ui
 
 // The table ladder's bounds (fixed-point ln p, kLadderTaus of them) from a
 // sample of minimum p-values, in ladder order.
-void ladder_of(const std::vector<double>& all, int fshift, int tau[kLadderTaus]);
+void ladder_of(const std::vector<double>& all, int fshift, int tau[kLadderTaus], double q0 = 0.0);
+// The default level-0 quantile (a pair's own, or a tuned one, replaces it).
+extern const double kLevel0QuantileDefault;
 void ladder_order(int tau[kLadderTaus]);
 LadderShape shape_of(const dto_pair* P);
 // A run's ladder after it: bounds that moved by more than the slack replace

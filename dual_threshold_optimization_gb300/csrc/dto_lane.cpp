@@ -25,6 +25,7 @@ namespace dto {
 // 6,000): 0.75 -> 24.2 / 14.4 ms, 0.80 -> 23.8 / 14.2, 0.85 -> 23.7 / 14.5,
 // 0.90 -> 23.9 / 15.3, 0.95 -> 26.8 / 18.1.
 constexpr double kLevel0Quantile = 0.85;
+const double kLevel0QuantileDefault = kLevel0Quantile;
 // Permutations of the first batch, whose minimum p-values set the ladder
 // (cold runs at 100,000 permutations, N = 20,000: 256 -> 47.8 ms, 512 -> 46.9,
 // 1,024 -> 49.3; its slowest tasks and its size both delay the pipeline).
@@ -380,7 +381,7 @@ void LadderModel::record(const LadderShape& x) {
   shapes.push_back(x);
 }
 
-bool LadderModel::lookup(const LadderShape& want, double nats[kLadderTaus]) {
+bool LadderModel::lookup(const LadderShape& want, double nats[kLadderTaus], double* q0) {
   auto rel = [](double a, double b) { return std::fabs(a - b) / std::max(1.0, std::max(a, b)); };
   std::lock_guard<std::mutex> g(mu);
   const LadderShape* best = nullptr;
@@ -403,6 +404,7 @@ bool LadderModel::lookup(const LadderShape& want, double nats[kLadderTaus]) {
   }
   if (!best) return false;
   for (int l = 0; l < kLadderTaus; ++l) nats[l] = best->nats[l];
+  if (q0) *q0 = best->q0;
   return true;
 }
 
@@ -523,7 +525,7 @@ void ladder_order(int tau[kLadderTaus]) {
   }
 }
 
-void ladder_of(const std::vector<double>& all, int fshift, int tau[kLadderTaus]) {
+void ladder_of(const std::vector<double>& all, int fshift, int tau[kLadderTaus], double q0) {
   // the quantiles from an evenly strided sample of at most 16,384 minima
   // (the permutations are in random order), the maximum from all of them
   const size_t stride = (all.size() + 16383) / 16384;
@@ -535,10 +537,10 @@ void ladder_of(const std::vector<double>& all, int fshift, int tau[kLadderTaus])
     std::nth_element(v.begin(), v.begin() + (long)k, v.end());
     return std::max(v[k], 1e-300);
   };
-  const double p90 = q(kLevel0Quantile);
+  const double p0 = q(q0 > 0.0 ? q0 : kLevel0Quantile);
   const double p99 = q(0.99);
   const double pmax = std::max(*std::max_element(all.begin(), all.end()), 1e-300);
-  tau[0] = fixed_log(p90, fshift);
+  tau[0] = fixed_log(p0, fshift);
   tau[1] = fixed_log(p99, fshift);
   tau[2] = (int)std::min(0.0, std::floor((std::log(pmax) + 1.0) * std::ldexp(1.0, fshift)));
   // the tighter tables a sweep switches to once a task's bound is known,
@@ -554,16 +556,23 @@ void ladder_of(const std::vector<double>& all, int fshift, int tau[kLadderTaus])
 }
 
 void ladder_update(dto_ctx* ctx, dto_pair* P, const std::vector<double>& minp) {
-  int t[kLadderTaus];
-  ladder_of(minp, P->fshift, t);
-  const long long slack = (long long)std::ldexp(kLadderSlack, P->fshift);
+  const size_t stride = std::max<size_t>((minp.size() + 16383) / 16384, 1);
+  std::vector<double> sample;
+  sample.reserve(minp.size() / stride + 1);
+  for (size_t i = 0; i < minp.size(); i += stride) sample.push_back(minp[i]);
   std::lock_guard<std::mutex> g(P->ladder_mu);
+  const double q0 = P->q0 > 0.0 ? P->q0 : kLevel0Quantile;
+  int t[kLadderTaus];
+  ladder_of(minp, P->fshift, t, q0);
+  const long long slack = (long long)std::ldexp(kLadderSlack, P->fshift);
   for (int l = 0; l < kLadderTaus; ++l)
     if (!P->ladder_ok || std::llabs((long long)t[l] - P->ladder_tau[l]) > slack) P->ladder_tau[l] = t[l];
   ladder_order(P->ladder_tau);
   P->ladder_ok = true;
+  P->ladder_sample.swap(sample);
   LadderShape x = shape_of(P);
   for (int l = 0; l < kLadderTaus; ++l) x.nats[l] = std::ldexp((double)P->ladder_tau[l], -P->fshift);
+  x.q0 = q0;
   ctx->ladders.record(x);
 }
 
@@ -711,10 +720,15 @@ int lane_run_range(Lane* L, dto_pair* P, uint32_t perm_first, int64_t n_perm, ui
         for (int l = 0; l < kLadderTaus; ++l) tau[l] = P->ladder_tau[l];
       }
     }
-    double model_nats[kLadderTaus];
-    if (!warm && L->use_model && L->ctx->ladders.lookup(shape_of(P), model_nats)) {
-      // a pair of the same shape has run: start from its ladder
+    double model_nats[kLadderTaus], model_q0 = 0.0;
+    if (!warm && L->use_model && L->ctx->ladders.lookup(shape_of(P), model_nats, &model_q0)) {
+      // a pair of the same shape has run: start from its ladder (and its
+      // level-0 quantile, unless this pair has one)
       warm = true;
+      {
+        std::lock_guard<std::mutex> g(P->ladder_mu);
+        if (P->q0 <= 0.0) P->q0 = model_q0;
+      }
       const double scale = std::ldexp(1.0, P->fshift);
       for (int l = 0; l < kLadderTaus; ++l)
         tau[l] = (int)std::max(-2.0e9, std::min(0.0, std::floor(model_nats[l] * scale)));

@@ -40,8 +40,12 @@ bool wave_taus(dto_ctx* ctx, dto_pair* P, int tau[kLadderTaus]) {
       return true;
     }
   }
-  double nats[kLadderTaus];
-  if (!ctx->ladders.lookup(shape_of(P), nats)) return false;
+  double nats[kLadderTaus], q0 = 0.0;
+  if (!ctx->ladders.lookup(shape_of(P), nats, &q0)) return false;
+  {
+    std::lock_guard<std::mutex> g(P->ladder_mu);
+    if (P->q0 <= 0.0) P->q0 = q0;
+  }
   const double scale = std::ldexp(1.0, P->fshift);
   for (int l = 0; l < kLadderTaus; ++l) tau[l] = (int)std::max(-2.0e9, std::min(0.0, std::floor(nats[l] * scale)));
   ladder_order(tau);

@@ -247,6 +247,20 @@ class DevicePair:
         check(lib().dto_pair_set_ladder(self.handle, ptr(a) if a.size else None, a.size),
               self.engine.handle)
 
+    def set_level0_quantile(self, q0):
+        """The quantile of the minimum p-values that sets this pair's level-0
+        table (default 0.85, in [0.5, 0.99]); performance only."""
+        check(lib().dto_pair_set_level0_quantile(self.handle, float(q0)), self.engine.handle)
+
+    def tune(self, n_perm, seed=1):
+        """Picks this pair's level-0 quantile by timed trial runs of n_perm
+        permutations (> 1,024) among 0.80, 0.85 and 0.90, keeps the fastest
+        and records it for the pair's shape (dto_pair_tune).  Returns it."""
+        best = C.c_double(0.0)
+        check(lib().dto_pair_tune(self.engine.handle, self.handle, int(n_perm), int(seed), C.byref(best)),
+              self.engine.handle)
+        return best.value
+
     @property
     def upload_bytes(self):
         """Host-to-device bytes dto_pair_create copied for this pair."""

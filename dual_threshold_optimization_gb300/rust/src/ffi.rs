@@ -103,6 +103,9 @@ extern "C" {
     pub fn dto_pair_thresholds(pair: *const dto_pair, t1: *mut u32, t2: *mut u32) -> c_int;
     pub fn dto_pair_set_stream(pair: *mut dto_pair, stream_id: u32) -> c_int;
     pub fn dto_pair_set_ladder(pair: *mut dto_pair, minp: *const f64, count: i64) -> c_int;
+    pub fn dto_pair_set_level0_quantile(pair: *mut dto_pair, q0: f64) -> c_int;
+    pub fn dto_pair_tune(ctx: *mut dto_ctx, pair: *mut dto_pair, n_perm: i64, seed: u64, best_quantile: *mut f64)
+        -> c_int;
     pub fn dto_pair_upload_bytes(pair: *const dto_pair) -> i64;
     pub fn dto_pair_order(pair: *const dto_pair, order1: *mut i32, order2: *mut i32) -> c_int;
     pub fn dto_run(

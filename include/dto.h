@@ -154,6 +154,18 @@ DTO_API int dto_pair_set_stream(dto_pair* pair, uint32_t stream_id);
  * it from a first batch.  The ladder decides only which path settles a task,
  * never a result.  p-values outside [0, 1] -> DTO_ERR_INVALID. */
 DTO_API int dto_pair_set_ladder(dto_pair* pair, const double* minp, int64_t count);
+/* No counterpart in the reference.  The quantile of the minimum p-values that
+ * sets the pair's level-0 table (default 0.85; [0.5, 0.99], else
+ * DTO_ERR_INVALID).  A pair with a ladder rebuilds it from its last run's
+ * sample at the new quantile.  Performance only: results do not change. */
+DTO_API int dto_pair_set_level0_quantile(dto_pair* pair, double q0);
+/* No counterpart in the reference.  Tunes the pair's level-0 quantile by
+ * timed trials: one run of n_perm permutations (> 1,024), then three runs per
+ * candidate quantile (0.80, 0.85, 0.90), each candidate's fastest device time
+ * of its last two counted; the fastest candidate stays set on the pair and is
+ * recorded for its shape, so that later pairs of that shape (within 5 % in
+ * every size) start with it.  The trial runs' results are discarded. */
+DTO_API int dto_pair_tune(dto_ctx* ctx, dto_pair* pair, int64_t n_perm, uint64_t seed, double* best_quantile);
 /* Host-to-device bytes that dto_pair_create copied (the pair's device tables). */
 DTO_API int64_t dto_pair_upload_bytes(const dto_pair* pair);
 DTO_API int dto_pair_order(const dto_pair* pair, int32_t* order1, int32_t* order2);

@@ -258,6 +258,33 @@ def test_philox_permutations_long_lists_match_spec(engine, N):
     dp.close()
 
 
+def test_tuned_level0_quantile_changes_no_result(fresh_engine):
+    # dto_pair_tune times 0.80, 0.85 and 0.90 and keeps the fastest; the
+    # quantile only moves the level-0 bound, so every optimum stays; a new
+    # pair of the same shape starts with the tuned quantile
+    from dual_threshold_optimization_gb300._lib import DtoError
+    engine = fresh_engine
+    p = synth.copula_pair(6000, 0.3, seed=81, frac_tied2=0.1)
+    dp = engine.pair(p.ranks1, p.feat1, p.ranks2, p.feat2, p.n_features, p.population)
+    ref = dp.run(3000, seed=5, want_records=True)
+    best = dp.tune(3000, seed=100)
+    assert best in (0.80, 0.85, 0.90)
+    again = dp.run(3000, seed=5, want_records=True)
+    assert optimum(again.unpermuted) == optimum(ref.unpermuted)
+    assert same_records(again.records, ref.records)
+    dq = engine.pair(p.ranks1, p.feat1, p.ranks2, p.feat2, p.n_features, p.population)
+    other = dq.run(3000, seed=5, want_records=True)
+    assert same_records(other.records, ref.records)
+    dp.set_level0_quantile(0.7)
+    assert same_records(dp.run(3000, seed=5, want_records=True).records, ref.records)
+    with pytest.raises(DtoError):
+        dp.set_level0_quantile(0.3)
+    with pytest.raises(DtoError):
+        dp.tune(500)
+    dp.close()
+    dq.close()
+
+
 def test_warm_ladder_gives_the_same_results(fresh_engine):
     # the first long run of a pair measures its ladder from a first batch; a
     # later run starts from the ladder the earlier run left, and a new pair
