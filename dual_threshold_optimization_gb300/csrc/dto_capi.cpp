@@ -482,8 +482,10 @@ int dto_pair_tune(dto_ctx* ctx, dto_pair* P, int64_t n_perm, uint64_t seed, doub
     return set_err(ctx, DTO_ERR_INVALID,
                    "dto_pair_tune: n_perm must take the table ladder (more than 1,024 permutations)");
   // the candidates' timed runs, on the context's own lane: one run first
-  // (the ladder, the kernels loaded), then two runs per candidate, the
-  // fastest device time of each counted
+  // (the ladder, the kernels loaded), then three runs per candidate, all of
+  // the same permutations (run-to-run differences of the permutations are as
+  // large as the candidates' differences), the first rebuilding the tables
+  // and the fastest device time of the other two counted
   static const double kCandidates[3] = {0.80, 0.85, 0.90};
   std::vector<double> minp((size_t)n_perm);
   dto_result unperm{};
@@ -496,15 +498,14 @@ int dto_pair_tune(dto_ctx* ctx, dto_pair* P, int64_t n_perm, uint64_t seed, doub
   int rc = run(seed);
   if (rc) return rc;
   double best_q = 0.0, best_ms = 1e300;
-  uint64_t s = seed + 1;
   for (double q : kCandidates) {
     rc = dto_pair_set_level0_quantile(P, q);
     if (rc) return rc;
     double ms = 1e300;
     for (int r = 0; r < 3; ++r) {
-      rc = run(s++);
+      rc = run(seed + 1);
       if (rc) return rc;
-      if (r > 0) ms = std::min(ms, sum.device_ms);  // the first rebuilds the tables
+      if (r > 0) ms = std::min(ms, sum.device_ms);
     }
     if (ms < best_ms) {
       best_ms = ms;

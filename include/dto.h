@@ -161,8 +161,9 @@ DTO_API int dto_pair_set_ladder(dto_pair* pair, const double* minp, int64_t coun
 DTO_API int dto_pair_set_level0_quantile(dto_pair* pair, double q0);
 /* No counterpart in the reference.  Tunes the pair's level-0 quantile by
  * timed trials: one run of n_perm permutations (> 1,024), then three runs per
- * candidate quantile (0.80, 0.85, 0.90), each candidate's fastest device time
- * of its last two counted; the fastest candidate stays set on the pair and is
+ * candidate quantile (0.80, 0.85, 0.90), all of the same permutations, each
+ * candidate's fastest device time of its last two counted (its first rebuilds
+ * the table screens); the fastest candidate stays set on the pair and is
  * recorded for its shape, so that later pairs of that shape (within 5 % in
  * every size) start with it.  The trial runs' results are discarded. */
 DTO_API int dto_pair_tune(dto_ctx* ctx, dto_pair* pair, int64_t n_perm, uint64_t seed, double* best_quantile);
