@@ -312,6 +312,8 @@ __global__ void __launch_bounds__(kGridWarps * 32, 1) grid_kernel(const GridArgs
   constexpr int kCntInts = grid_cnt_ints(C);
   constexpr int kWarpInts = grid_warp_ints(C);
   extern __shared__ __align__(16) unsigned char smem_raw[];
+  // an empty task list (the usual fallback list): nothing to load or sweep
+  if (A.ntask_dev && *((volatile const int*)A.ntask_dev) == 0) return;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int n1 = A.P.n1, n2 = A.P.n2;
   const long long Npop = A.P.Npop;
