@@ -103,10 +103,9 @@ struct Lane {
   void* dHits[1] = {};
   size_t hitBytes[1] = {};
   // Batches of the table-screen pipeline in flight.  A slot is reused only
-  // once the side stream has finished its batch; with three, the main stream
-  // draws the next batch's labels while the side stream still resolves the
-  // batch before last (its later levels get SMs only as the level-0 sweep
-  // on the main stream lets go of them).
+  // once its side stream has finished its batch (fallbacks, result copy);
+  // with three, the main stream draws the next batch's labels while a side
+  // stream still finishes the batch before last.
   static constexpr int kSlots = 3;
   static_assert(kSlots >= 2 && kSlots <= kSlotsMax, "two to four batch slots");
   BatchSlot slot[kSlots];

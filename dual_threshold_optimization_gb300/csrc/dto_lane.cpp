@@ -628,7 +628,7 @@ int lane_run_range(Lane* L, dto_pair* P, uint32_t perm_first, int64_t n_perm, ui
   };
   std::vector<double> minp((size_t)n_perm);
   long long nroute[DTO_ROUTES] = {};
-  cudaEvent_t last_l0_end = nullptr;  // end of the last level-0 sweep (main stream)
+  cudaEvent_t last_l0_end = nullptr;  // end of the last table sweep (main stream)
   TaskResult unperm{};
   // Short runs (and FP64 runs) go through the exhaustive screen in batches,
   // the unpermuted task (task 0) in row 0 of the first.  Long runs go through

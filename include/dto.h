@@ -94,11 +94,12 @@ typedef struct {
     int64_t n_launches;            /* kernels launched */
     int64_t h2d_bytes;             /* host-to-device bytes copied by this call */
     int64_t d2h_bytes;             /* device-to-host bytes copied by this call */
-    double sweep0_ms;              /* CUDA-event time of the level-0 table sweeps (main stream) */
+    double sweep0_ms;              /* CUDA-event time of the table sweeps (levels 0-2 cascaded;
+                                      main stream) */
     int64_t sweep0_launches;       /* their launches */
     int64_t sweep0_tasks;          /* permutations they took */
     int64_t n_route[DTO_ROUTES];   /* tasks (unpermuted included) settled by each DTO_ROUTE_* */
-    double tail_ms;                /* device time from the end of the last level-0 sweep to the end
+    double tail_ms;                /* device time from the end of the last table sweep to the end
                                       of the run (0 when no table sweep ran) */
 } dto_summary;
 
