@@ -271,6 +271,23 @@ impl<'e> Pair<'e> {
         Ok(OptimizationResultRecord::from(&out))
     }
 
+    /// The level-0 table's quantile of this pair (default 0.85, in [0.5, 0.99]);
+    /// performance only.
+    pub fn set_level0_quantile(&self, q0: f64) -> Result<()> {
+        let st = unsafe { ffi::dto_pair_set_level0_quantile(self.ptr, q0) };
+        self.eng.check(st)
+    }
+
+    /// dto_pair_tune: picks the level-0 quantile by timed trial runs of
+    /// `n_perm` permutations (> 1,024) among 0.80, 0.85 and 0.90, keeps the
+    /// fastest for this pair and records it for its shape; returns it.
+    pub fn tune(&self, n_perm: usize, seed: u64) -> Result<f64> {
+        let mut best = 0f64;
+        let st = unsafe { ffi::dto_pair_tune(self.eng.ctx, self.ptr, n_perm as i64, seed, &mut best) };
+        self.eng.check(st)?;
+        Ok(best)
+    }
+
     /// Every cell's record of the unpermuted task (OptimizationResult::Debug).
     pub fn grid_dump(&self) -> Result<Vec<OptimizationResultRecord>> {
         let mut recs = vec![ffi::dto_result::default(); self.thresholds1 * self.thresholds2];
