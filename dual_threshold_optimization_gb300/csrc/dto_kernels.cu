@@ -72,6 +72,7 @@ struct PhiloxStream {
 template <int kPermThreads>
 __device__ __forceinline__ void perm_body(const PermArgs& A, int* cnt, uint16_t* sA, int16_t* sY) {
   __shared__ int warpTot[kPermThreads / 32];
+  __shared__ int nClaim;  // claimed buckets in the list (rows longer than the CTA)
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int L = A.L;
   const uint32_t perm = A.perm_base + blockIdx.x;
@@ -79,6 +80,7 @@ __device__ __forceinline__ void perm_body(const PermArgs& A, int* cnt, uint16_t*
   const uint32_t tagB = 0x10000000u | (A.list_tag << 24);
   constexpr int kPerWarp = kBuckets / (kPermThreads / 32);
   static_assert(kBucketBits == 12, "buckets are the top 12 bits of a 16-bit half");
+  static_assert(4 * kPermThreads <= kBuckets, "the claim list (two ints a row start) fits in the counters");
   auto bucket_in = [](const uint4& w, int e) -> int {
     const int q = (e >> 1) & 3;
     const uint32_t word = q == 0 ? w.x : q == 1 ? w.y : q == 2 ? w.z : w.w;
@@ -243,15 +245,40 @@ __device__ __forceinline__ void perm_body(const PermArgs& A, int* cnt, uint16_t*
     };
     const int2 cl0 = tid <= A.n1 ? claim(tid, 0) : make_int2(-1, 0);
     const int2 cl1 = r1 <= A.n1 ? claim(r1, 1) : make_int2(-1, 0);
-    if (ids) {
-      __syncthreads();  // every claim has read the buckets: the labels may come
+    if (ids && A.n1 + 1 > kPermThreads) {
+      // Some threads hold two row starts: the claimed buckets go to a list
+      // (in the counters, which nothing reads after the claims) so that no
+      // thread shuffles two.  Entry: (start | bucket << 16, size); at most
+      // 2 * kPermThreads entries of two ints, within the kBuckets counters.
+      const int e0 = cl0.x >= 0 ? cnt[cl0.x] : 0, e1 = cl1.x >= 0 ? cnt[cl1.x] : 0;
+      if (tid == 0) nClaim = 0;
+      __syncthreads();  // every claim has read the buckets and the counters
       stage_labels();
-    }
-    if (cl0.x >= 0) shuffle_bucket(cl0.x, cl0.y, cnt[cl0.x] - cl0.y);
-    if (cl1.x >= 0) shuffle_bucket(cl1.x, cl1.y, cnt[cl1.x] - cl1.y);
-    for (int r = tid + 2 * kPermThreads, u = 2; r <= A.n1; r += kPermThreads, ++u) {
-      const int2 c = claim(r, u);
-      if (c.x >= 0) shuffle_bucket(c.x, c.y, cnt[c.x] - c.y);
+      const unsigned m0 = __ballot_sync(0xffffffffu, cl0.x >= 0), m1 = __ballot_sync(0xffffffffu, cl1.x >= 0);
+      int base = 0;
+      if (lane == 0 && (m0 | m1)) base = atomicAdd(&nClaim, __popc(m0) + __popc(m1));
+      base = __shfl_sync(0xffffffffu, base, 0);
+      const unsigned lt = (1u << lane) - 1u;
+      int2* list = reinterpret_cast<int2*>(cnt);
+      if (cl0.x >= 0) list[base + __popc(m0 & lt)] = make_int2(cl0.y | (cl0.x << 16), e0 - cl0.y);
+      if (cl1.x >= 0) list[base + __popc(m0) + __popc(m1 & lt)] = make_int2(cl1.y | (cl1.x << 16), e1 - cl1.y);
+      __syncthreads();
+      const int nc = nClaim;
+      for (int k = tid; k < nc; k += kPermThreads) {
+        const int2 c = list[k];
+        shuffle_bucket(c.x >> 16, c.x & 0xFFFF, c.y);
+      }
+    } else {
+      if (ids) {
+        __syncthreads();  // every claim has read the buckets: the labels may come
+        stage_labels();
+      }
+      if (cl0.x >= 0) shuffle_bucket(cl0.x, cl0.y, cnt[cl0.x] - cl0.y);
+      if (cl1.x >= 0) shuffle_bucket(cl1.x, cl1.y, cnt[cl1.x] - cl1.y);
+      for (int r = tid + 2 * kPermThreads, u = 2; r <= A.n1; r += kPermThreads, ++u) {
+        const int2 c = claim(r, u);
+        if (c.x >= 0) shuffle_bucket(c.x, c.y, cnt[c.x] - c.y);
+      }
     }
   } else {
     if (ids) {
