@@ -78,7 +78,6 @@ __device__ __forceinline__ void perm_body(const PermArgs& A, int* cnt, uint16_t*
   const uint32_t perm = A.perm_base + blockIdx.x;
   const uint32_t k0 = (uint32_t)A.seed, k1 = (uint32_t)(A.seed >> 32);
   const uint32_t tagB = 0x10000000u | (A.list_tag << 24);
-  constexpr int kPerWarp = kBuckets / (kPermThreads / 32);
   static_assert(kBucketBits == 12, "buckets are the top 12 bits of a 16-bit half");
   static_assert(4 * kPermThreads <= kBuckets, "the claim list (two ints a row start) fits in the counters");
   auto bucket_in = [](const uint4& w, int e) -> int {
@@ -144,39 +143,53 @@ __device__ __forceinline__ void perm_body(const PermArgs& A, int* cnt, uint16_t*
     }
   }
   __syncthreads();
-  // exclusive scan of the counters: warp w scans buckets [w*kPerWarp, (w+1)*kPerWarp)
+  // exclusive scan of the counters: thread t holds kPerThread consecutive
+  // counters (a serial prefix), one warp scan of the threads' totals, one of
+  // the warps' totals
   {
-    int carry = 0;
-    for (int r = 0; r < kPerWarp; r += 32) {
-      const int idx = warp * kPerWarp + r + lane;
-      const int v = cnt[idx];
-      int incl = v;
+    constexpr int kPerThread = kBuckets / kPermThreads;
+    static_assert(kPerThread % 4 == 0, "counters a thread: whole int4");
+    int4* c4 = reinterpret_cast<int4*>(cnt) + tid * (kPerThread / 4);
+    int v[kPerThread];
 #pragma unroll
-      for (int d = 1; d < 32; d <<= 1) {
-        int y = __shfl_up_sync(0xffffffffu, incl, d);
-        if (lane >= d) incl += y;
-      }
-      cnt[idx] = carry + incl - v;
-      carry += __shfl_sync(0xffffffffu, incl, 31);
+    for (int k = 0; k < kPerThread / 4; ++k) {
+      const int4 x = c4[k];
+      v[4 * k] = x.x;
+      v[4 * k + 1] = x.y;
+      v[4 * k + 2] = x.z;
+      v[4 * k + 3] = x.w;
     }
-    if (lane == 0) warpTot[warp] = carry;
-  }
-  __syncthreads();
-  if (warp == 0) {
-    constexpr int kWarps = kPermThreads / 32;
-    const int v = lane < kWarps ? warpTot[lane] : 0;
-    int incl = v;
+    int tot = 0;
+#pragma unroll
+    for (int k = 0; k < kPerThread; ++k) {
+      const int x = v[k];
+      v[k] = tot;
+      tot += x;
+    }
+    int incl = tot;
 #pragma unroll
     for (int d = 1; d < 32; d <<= 1) {
       int y = __shfl_up_sync(0xffffffffu, incl, d);
       if (lane >= d) incl += y;
     }
-    if (lane < kWarps) warpTot[lane] = incl - v;
-  }
-  __syncthreads();
-  {
-    const int off = warpTot[warp];
-    for (int r = 0; r < kPerWarp; r += 32) cnt[warp * kPerWarp + r + lane] += off;
+    if (lane == 31) warpTot[warp] = incl;
+    __syncthreads();
+    if (warp == 0) {
+      constexpr int kWarps = kPermThreads / 32;
+      const int w = lane < kWarps ? warpTot[lane] : 0;
+      int wi = w;
+#pragma unroll
+      for (int d = 1; d < 32; d <<= 1) {
+        int y = __shfl_up_sync(0xffffffffu, wi, d);
+        if (lane >= d) wi += y;
+      }
+      if (lane < kWarps) warpTot[lane] = wi - w;
+    }
+    __syncthreads();
+    const int off = warpTot[warp] + incl - tot;
+#pragma unroll
+    for (int k = 0; k < kPerThread / 4; ++k)
+      c4[k] = make_int4(off + v[4 * k], off + v[4 * k + 1], off + v[4 * k + 2], off + v[4 * k + 3]);
   }
   __syncthreads();
   if (ids) {
