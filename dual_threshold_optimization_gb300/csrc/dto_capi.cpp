@@ -454,6 +454,7 @@ int dto_pair_set_ladder(dto_pair* P, const double* minp, int64_t count) {
     v.push_back(minp[q]);
   }
   std::lock_guard<std::mutex> g(P->ladder_mu);
+  P->ladder_pending = false;  // a ladder left by the last run gives way
   if (count == 0) {
     P->ladder_ok = false;
     P->ladder_sample.clear();
@@ -469,6 +470,7 @@ int dto_pair_set_level0_quantile(dto_pair* P, double q0) {
   if (!P) return DTO_ERR_INVALID;
   if (!(q0 >= 0.5 && q0 <= 0.99))
     return set_err(P->ctx, DTO_ERR_INVALID, "dto_pair_set_level0_quantile: the quantile must lie in [0.5, 0.99]");
+  ladder_flush(P->ctx, P);
   std::lock_guard<std::mutex> g(P->ladder_mu);
   P->q0 = q0;
   // the ladder again from the last run's sample, at the new quantile

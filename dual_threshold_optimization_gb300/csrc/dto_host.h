@@ -152,6 +152,20 @@ struct LadderShape {
   double q0;  // the level-0 quantile the ladder was built with
 };
 
+// A run's minimum p-values not yet made into ladder bounds: the context's
+// own lane leaves that work to the pair's next reader (its next run computes
+// the bounds while its labels are drawn).  The context keeps a copy of the
+// last one for its model, so that a new pair of the same shape finds it even
+// if its pair never runs again.
+struct LadderPending {
+  std::vector<double> sample;  // evenly strided, at most 16,384 minima
+  double pmax = 0.0;           // the largest of all the run's minima
+  double q0 = 0.0;             // the level-0 quantile
+  int fshift = 0;
+  LadderShape shape{};         // nats unset
+  unsigned long long serial = 0, gen = 0;  // the pair and its update
+};
+
 struct LadderModel {
   std::mutex mu;
   std::vector<LadderShape> shapes;  // most recent last
@@ -159,6 +173,9 @@ struct LadderModel {
   static constexpr double kTol = 0.05;  // relative difference accepted per size
   void record(const LadderShape& x);
   bool lookup(const LadderShape& want, double nats[kLadderTaus], double* q0 = nullptr);
+  // x stands in for want: the same kind of lists, every size within kTol
+  // (their relative differences' sum in *dist)
+  static bool fits(const LadderShape& x, const LadderShape& want, double* dist = nullptr);
 };
 
 }  // namespace dto
@@ -180,6 +197,12 @@ struct dto_ctx {
   std::atomic<unsigned long long> next_serial{1};
   dto::Lane* lane0 = nullptr;
   dto::LadderModel ladders;
+  // the last run of the context's own lane whose ladder is pending: recorded
+  // into `ladders` when a new pair looks its shape up, unless its pair's own
+  // next reader has done so
+  std::mutex defer_mu;
+  bool deferred = false;
+  dto::LadderPending deferred_rec;
 };
 
 struct dto_pair {
@@ -215,6 +238,11 @@ struct dto_pair {
   // which a new quantile rebuilds the ladder (dto_pair_set_level0_quantile)
   double q0 = 0.0;
   std::vector<double> ladder_sample;
+  // ladder_sample (and the maximum) of the last run, not yet made into
+  // bounds (ladder_flush); `ladder_gen` counts the pair's deferred updates
+  bool ladder_pending = false;
+  double ladder_pmax = 0.0;
+  unsigned long long ladder_gen = 0;
   // The table screens of levels 0..2 that dto_batch_run's waves built for
   // this pair, kept with it (a wave sweeps several pairs at once, so each
   // needs its own; the next batch finds them).  Guarded by the context mutex.
@@ -274,8 +302,18 @@ extern const double kLevel0QuantileDefault;
 void ladder_order(int tau[kLadderTaus]);
 LadderShape shape_of(const dto_pair* P);
 // A run's ladder after it: bounds that moved by more than the slack replace
-// the pair's, and the context's model records the pair's shape.
-void ladder_update(dto_ctx* ctx, dto_pair* P, const std::vector<double>& minp);
+// the pair's, and the context's model records the pair's shape.  With
+// `defer` the bounds are left pending for the pair's next reader.
+void ladder_update(dto_ctx* ctx, dto_pair* P, const std::vector<double>& minp, bool defer = false);
+// The pair's pending ladder made into bounds (nothing if none is pending).
+void ladder_flush(dto_ctx* ctx, dto_pair* P);
+// The context's pending record made into its model's entry.
+void ladder_flush_deferred(dto_ctx* ctx);
+// Does the context's pending record fit a pair of shape `want`?
+bool ladder_deferred_fits(dto_ctx* ctx, const LadderShape& want);
+// The context's pending record, if it fits `want`, made into its model's
+// entry; its bounds (nats) and level-0 quantile returned.
+bool ladder_take_deferred(dto_ctx* ctx, const LadderShape& want, double nats[kLadderTaus], double* q0);
 // Labels of `count` permutations from perm id `first` (or of uploaded index
 // rows dIdx) into X (row stride xs) on the lane's main stream.
 int make_labels_launch(Lane* L, dto_pair* P, uint64_t seed, uint32_t first, int count, const int32_t* dIdx,

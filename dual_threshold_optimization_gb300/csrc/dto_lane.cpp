@@ -381,23 +381,29 @@ void LadderModel::record(const LadderShape& x) {
   shapes.push_back(x);
 }
 
-bool LadderModel::lookup(const LadderShape& want, double nats[kLadderTaus], double* q0) {
+bool LadderModel::fits(const LadderShape& x, const LadderShape& want, double* dist) {
   auto rel = [](double a, double b) { return std::fabs(a - b) / std::max(1.0, std::max(a, b)); };
+  if (x.same_set != want.same_set) return false;
+  const double d[6] = {rel((double)x.npop, (double)want.npop), rel((double)x.N1, (double)want.N1),
+                       rel((double)x.N2, (double)want.N2), rel((double)x.ncommon, (double)want.ncommon),
+                       rel(x.n1, want.n1), rel(x.n2, want.n2)};
+  double sum = 0.0;
+  bool ok = true;
+  for (double v : d) {
+    ok = ok && v <= kTol;
+    sum += v;
+  }
+  if (dist) *dist = sum;
+  return ok;
+}
+
+bool LadderModel::lookup(const LadderShape& want, double nats[kLadderTaus], double* q0) {
   std::lock_guard<std::mutex> g(mu);
   const LadderShape* best = nullptr;
   double best_d = 1e300;
   for (const LadderShape& x : shapes) {
-    if (x.same_set != want.same_set) continue;
-    const double d[6] = {rel((double)x.npop, (double)want.npop), rel((double)x.N1, (double)want.N1),
-                         rel((double)x.N2, (double)want.N2), rel((double)x.ncommon, (double)want.ncommon),
-                         rel(x.n1, want.n1), rel(x.n2, want.n2)};
     double sum = 0.0;
-    bool ok = true;
-    for (double v : d) {
-      ok = ok && v <= kTol;
-      sum += v;
-    }
-    if (ok && sum < best_d) {
+    if (fits(x, want, &sum) && sum < best_d) {
       best_d = sum;
       best = &x;
     }
@@ -525,13 +531,21 @@ void ladder_order(int tau[kLadderTaus]) {
   }
 }
 
-void ladder_of(const std::vector<double>& all, int fshift, int tau[kLadderTaus], double q0) {
-  // the quantiles from an evenly strided sample of at most 16,384 minima
-  // (the permutations are in random order), the maximum from all of them
-  const size_t stride = (all.size() + 16383) / 16384;
+namespace {
+
+// An evenly strided sample of at most 16,384 minima (the permutations are in
+// random order).
+std::vector<double> ladder_sample_of(const std::vector<double>& all) {
+  const size_t stride = std::max<size_t>((all.size() + 16383) / 16384, 1);
   std::vector<double> v;
-  v.reserve(all.size() / std::max<size_t>(stride, 1) + 1);
-  for (size_t i = 0; i < all.size(); i += std::max<size_t>(stride, 1)) v.push_back(all[i]);
+  v.reserve(all.size() / stride + 1);
+  for (size_t i = 0; i < all.size(); i += stride) v.push_back(all[i]);
+  return v;
+}
+
+// The bounds from a sample (reordered by the selections) and the maximum of
+// all the minima.
+void ladder_taus(std::vector<double>& v, double pmax_all, int fshift, int tau[kLadderTaus], double q0) {
   auto q = [&](double f) {
     const size_t k = (size_t)(f * (double)(v.size() - 1));
     std::nth_element(v.begin(), v.begin() + (long)k, v.end());
@@ -539,7 +553,7 @@ void ladder_of(const std::vector<double>& all, int fshift, int tau[kLadderTaus],
   };
   const double p0 = q(q0 > 0.0 ? q0 : kLevel0Quantile);
   const double p99 = q(0.99);
-  const double pmax = std::max(*std::max_element(all.begin(), all.end()), 1e-300);
+  const double pmax = std::max(pmax_all, 1e-300);
   tau[0] = fixed_log(p0, fshift);
   tau[1] = fixed_log(p99, fshift);
   tau[2] = (int)std::min(0.0, std::floor((std::log(pmax) + 1.0) * std::ldexp(1.0, fshift)));
@@ -555,25 +569,108 @@ void ladder_of(const std::vector<double>& all, int fshift, int tau[kLadderTaus],
   ladder_order(tau);
 }
 
-void ladder_update(dto_ctx* ctx, dto_pair* P, const std::vector<double>& minp) {
-  const size_t stride = std::max<size_t>((minp.size() + 16383) / 16384, 1);
-  std::vector<double> sample;
-  sample.reserve(minp.size() / stride + 1);
-  for (size_t i = 0; i < minp.size(); i += stride) sample.push_back(minp[i]);
-  std::lock_guard<std::mutex> g(P->ladder_mu);
-  const double q0 = P->q0 > 0.0 ? P->q0 : kLevel0Quantile;
-  int t[kLadderTaus];
-  ladder_of(minp, P->fshift, t, q0);
+// New bounds t into the pair's ladder (those that moved by more than
+// kLadderSlack nats; the bounds are quantiles of the pair's null
+// distribution, so another seed moves them a little, and a kept bound spares
+// the next run that table's rebuild), and the pair's shape into the
+// context's model.  The caller holds P->ladder_mu.
+void ladder_apply(dto_ctx* ctx, dto_pair* P, const int t[kLadderTaus], double q0) {
   const long long slack = (long long)std::ldexp(kLadderSlack, P->fshift);
   for (int l = 0; l < kLadderTaus; ++l)
     if (!P->ladder_ok || std::llabs((long long)t[l] - P->ladder_tau[l]) > slack) P->ladder_tau[l] = t[l];
   ladder_order(P->ladder_tau);
   P->ladder_ok = true;
-  P->ladder_sample.swap(sample);
   LadderShape x = shape_of(P);
   for (int l = 0; l < kLadderTaus; ++l) x.nats[l] = std::ldexp((double)P->ladder_tau[l], -P->fshift);
   x.q0 = q0;
   ctx->ladders.record(x);
+}
+
+// The context's pending record into its model; its entry returned.  The
+// caller holds ctx->defer_mu.
+LadderShape record_deferred(dto_ctx* ctx) {
+  LadderPending& r = ctx->deferred_rec;
+  int t[kLadderTaus];
+  ladder_taus(r.sample, r.pmax, r.fshift, t, r.q0);
+  LadderShape x = r.shape;
+  for (int l = 0; l < kLadderTaus; ++l) x.nats[l] = std::ldexp((double)t[l], -r.fshift);
+  x.q0 = r.q0;
+  ctx->ladders.record(x);
+  ctx->deferred = false;
+  return x;
+}
+
+}  // namespace
+
+void ladder_of(const std::vector<double>& all, int fshift, int tau[kLadderTaus], double q0) {
+  // the quantiles from a sample, the maximum from all of them
+  std::vector<double> v = ladder_sample_of(all);
+  ladder_taus(v, *std::max_element(all.begin(), all.end()), fshift, tau, q0);
+}
+
+void ladder_update(dto_ctx* ctx, dto_pair* P, const std::vector<double>& minp, bool defer) {
+  std::vector<double> sample = ladder_sample_of(minp);
+  const double pmax = *std::max_element(minp.begin(), minp.end());
+  std::lock_guard<std::mutex> g(P->ladder_mu);
+  const double q0 = P->q0 > 0.0 ? P->q0 : kLevel0Quantile;
+  P->ladder_sample.swap(sample);
+  P->ladder_pmax = pmax;
+  if (!defer) {
+    std::vector<double> v = P->ladder_sample;
+    int t[kLadderTaus];
+    ladder_taus(v, pmax, P->fshift, t, q0);
+    P->ladder_pending = false;
+    ladder_apply(ctx, P, t, q0);
+    return;
+  }
+  P->ladder_pending = true;
+  ++P->ladder_gen;
+  std::lock_guard<std::mutex> d(ctx->defer_mu);
+  // another pair's pending record goes to the model now
+  if (ctx->deferred && ctx->deferred_rec.serial != P->serial) record_deferred(ctx);
+  LadderPending& r = ctx->deferred_rec;
+  r.sample = P->ladder_sample;
+  r.pmax = pmax;
+  r.q0 = q0;
+  r.fshift = P->fshift;
+  r.shape = shape_of(P);
+  r.serial = P->serial;
+  r.gen = P->ladder_gen;
+  ctx->deferred = true;
+}
+
+void ladder_flush(dto_ctx* ctx, dto_pair* P) {
+  std::lock_guard<std::mutex> g(P->ladder_mu);
+  if (!P->ladder_pending) return;
+  std::vector<double> v = P->ladder_sample;
+  const double q0 = P->q0 > 0.0 ? P->q0 : kLevel0Quantile;
+  int t[kLadderTaus];
+  ladder_taus(v, P->ladder_pmax, P->fshift, t, q0);
+  P->ladder_pending = false;
+  ladder_apply(ctx, P, t, q0);
+  // the context's copy of this update is recorded
+  std::lock_guard<std::mutex> d(ctx->defer_mu);
+  if (ctx->deferred && ctx->deferred_rec.serial == P->serial && ctx->deferred_rec.gen == P->ladder_gen)
+    ctx->deferred = false;
+}
+
+void ladder_flush_deferred(dto_ctx* ctx) {
+  std::lock_guard<std::mutex> d(ctx->defer_mu);
+  if (ctx->deferred) record_deferred(ctx);
+}
+
+bool ladder_deferred_fits(dto_ctx* ctx, const LadderShape& want) {
+  std::lock_guard<std::mutex> d(ctx->defer_mu);
+  return ctx->deferred && LadderModel::fits(ctx->deferred_rec.shape, want);
+}
+
+bool ladder_take_deferred(dto_ctx* ctx, const LadderShape& want, double nats[kLadderTaus], double* q0) {
+  std::lock_guard<std::mutex> d(ctx->defer_mu);
+  if (!ctx->deferred || !LadderModel::fits(ctx->deferred_rec.shape, want)) return false;
+  const LadderShape x = record_deferred(ctx);
+  for (int l = 0; l < kLadderTaus; ++l) nats[l] = x.nats[l];
+  *q0 = x.q0;
+  return true;
 }
 
 int lane_run_range(Lane* L, dto_pair* P, uint32_t perm_first, int64_t n_perm, uint64_t seed,
@@ -711,20 +808,24 @@ int lane_run_range(Lane* L, dto_pair* P, uint32_t perm_first, int64_t n_perm, ui
     // first batch's slowest tasks (the permutations with the largest minimum
     // p) take several times a typical task; meanwhile the main stream draws
     // the labels of the first two pipelined batches.
+    // A ladder left pending by the pair's last run is made into bounds once
+    // this run's labels are on their way.
     int tau[kLadderTaus] = {};
-    bool warm = false;
+    bool warm = false, pending = false;
     {
       std::lock_guard<std::mutex> g(P->ladder_mu);
-      if (P->ladder_ok) {
+      if (P->ladder_ok || P->ladder_pending) {
         warm = true;
+        pending = P->ladder_pending;
         for (int l = 0; l < kLadderTaus; ++l) tau[l] = P->ladder_tau[l];
       }
     }
+    // a pair of the same shape has run: start from its ladder (and its
+    // level-0 quantile, unless this pair has one).  When that run's ladder is
+    // still pending, its bounds too are computed once the labels are on
+    // their way.
     double model_nats[kLadderTaus], model_q0 = 0.0;
-    if (!warm && L->use_model && L->ctx->ladders.lookup(shape_of(P), model_nats, &model_q0)) {
-      // a pair of the same shape has run: start from its ladder (and its
-      // level-0 quantile, unless this pair has one)
-      warm = true;
+    auto from_model = [&]() {
       {
         std::lock_guard<std::mutex> g(P->ladder_mu);
         if (P->q0 <= 0.0) P->q0 = model_q0;
@@ -733,6 +834,15 @@ int lane_run_range(Lane* L, dto_pair* P, uint32_t perm_first, int64_t n_perm, ui
       for (int l = 0; l < kLadderTaus; ++l)
         tau[l] = (int)std::max(-2.0e9, std::min(0.0, std::floor(model_nats[l] * scale)));
       ladder_order(tau);
+    };
+    bool model_later = false;
+    if (!warm && L->use_model) {
+      if (ladder_deferred_fits(L->ctx, shape_of(P))) {
+        warm = model_later = true;
+      } else if (L->ctx->ladders.lookup(shape_of(P), model_nats, &model_q0)) {
+        warm = true;
+        from_model();
+      }
     }
     const int cnt0 = warm ? 0 : (int)first_batch;
     if (warm) {
@@ -810,6 +920,22 @@ int lane_run_range(Lane* L, dto_pair* P, uint32_t perm_first, int64_t n_perm, ui
       rc = first_done();
       if (rc) return rc;
       ladder_of(std::vector<double>(minp.begin(), minp.begin() + cnt0), P->fshift, tau);
+    }
+    if (pending) {
+      ladder_flush(L->ctx, P);
+      std::lock_guard<std::mutex> g(P->ladder_mu);
+      for (int l = 0; l < kLadderTaus; ++l) tau[l] = P->ladder_tau[l];
+    }
+    if (model_later) {
+      // the record (or, if another call recorded it meanwhile, the model's
+      // entry); failing both, bounds below every cell leave each task to
+      // the exhaustive screen (the same results, slowly)
+      if (!ladder_take_deferred(L->ctx, shape_of(P), model_nats, &model_q0) &&
+          !L->ctx->ladders.lookup(shape_of(P), model_nats, &model_q0)) {
+        for (double& v : model_nats) v = -1.0e9;
+        model_q0 = 0.0;
+      }
+      from_model();
     }
     // The table screens, on the main stream: the first sweep cascades
     // through every level, so it needs all of them.
@@ -891,13 +1017,12 @@ int lane_run_range(Lane* L, dto_pair* P, uint32_t perm_first, int64_t n_perm, ui
       rc = first_done();
       if (rc) return rc;
     }
-    // this run's minimum p-values set the ladder of the pair's next run.
-    // The bounds are quantiles of the pair's null distribution, so another
-    // seed moves them a little; a bound is replaced only when it has moved
-    // by more than kLadderSlack nats, which spares the next run the rebuild
-    // of that table screen (they are screens: any bounds give the same
-    // results).
-    ladder_update(L->ctx, P, minp);
+    // this run's minimum p-values set the ladder of the pair's next run
+    // (they are screens: any bounds give the same results).  On the
+    // context's own lane the bounds are left to the next reader, which is
+    // most often the pair's next run: it computes them while its labels are
+    // drawn instead of this run's caller waiting for them.
+    ladder_update(L->ctx, P, minp, L == L->ctx->lane0);
     // the main stream's timing event follows the side streams' last work
     LCK(cudaEventRecord(L->evSide, L->side));
     LCK(cudaStreamWaitEvent(L->stream, L->evSide, 0));

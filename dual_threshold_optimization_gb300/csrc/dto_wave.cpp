@@ -33,6 +33,7 @@ constexpr int kWaveLevels = 3;
 // The pair's ladder (levels 0..2): its own from an earlier run, else the
 // context's model's for its shape.
 bool wave_taus(dto_ctx* ctx, dto_pair* P, int tau[kLadderTaus]) {
+  ladder_flush(ctx, P);
   {
     std::lock_guard<std::mutex> g(P->ladder_mu);
     if (P->ladder_ok) {
@@ -40,6 +41,7 @@ bool wave_taus(dto_ctx* ctx, dto_pair* P, int tau[kLadderTaus]) {
       return true;
     }
   }
+  ladder_flush_deferred(ctx);
   double nats[kLadderTaus], q0 = 0.0;
   if (!ctx->ladders.lookup(shape_of(P), nats, &q0)) return false;
   {

@@ -300,5 +300,10 @@ def test_warm_ladder_gives_the_same_results(fresh_engine):
     other = engine.pair(p.ranks1, p.feat1, p.ranks2, p.feat2, p.n_features, p.population)
     shifted = other.run(4000, seed=17, first=5001, want_records=True)  # the shape's ladder, other ids
     assert same_records(shifted.records, cold.records[5000:9000])
+    # warm starts measure no first batch (route 1, the exhaustive screen of
+    # the first permutations): the pair's own later run, and the new pair
+    # from the ladder its shape's last run left
+    for res in (warm, shifted):
+        assert 1 not in set(np.unique(res.records["route"]).tolist())
     dp.close()
     other.close()
