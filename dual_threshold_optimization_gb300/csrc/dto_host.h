@@ -81,6 +81,8 @@ struct Lane {
   bool use_model = false;
   cudaStream_t stream = nullptr;
   cudaStream_t side = nullptr;  // first batch, unpermuted task, fallbacks
+  cudaStream_t tstream = nullptr;  // a run's table screens, beside its labels
+  cudaEvent_t evTab = nullptr;     // the table screens built
   cudaEvent_t evSide = nullptr;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   cudaEvent_t evk[4] = {nullptr, nullptr, nullptr, nullptr};  // perm start/end, grid start/end
@@ -136,6 +138,7 @@ struct Lane {
     cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};  // start, labels done, sweep done, end
   };
   WaveBuf wave[2];
+  std::vector<double> minp;  // a run's minimum p-values (lane_run_range)
 };
 
 // Ladders of the pairs a context has run, by shape, in nats of ln p.  The

@@ -112,6 +112,12 @@ int lane_create(dto_ctx* ctx, Lane** out, std::string* err_sink) {
   if ((e = cudaStreamCreateWithPriority(&L->side, cudaStreamNonBlocking, prio_least)) !=
       cudaSuccess)
     return fail(e, "stream");
+  // the table stream builds a run's table screens while its labels are
+  // drawn, at the highest priority: its blocks take SM room first as
+  // permutation CTAs retire
+  if ((e = cudaStreamCreateWithPriority(&L->tstream, cudaStreamNonBlocking, prio_greatest)) != cudaSuccess)
+    return fail(e, "stream");
+  if ((e = cudaEventCreateWithFlags(&L->evTab, cudaEventDisableTiming)) != cudaSuccess) return fail(e, "event");
   if ((e = cudaEventCreateWithFlags(&L->evSide, cudaEventDisableTiming)) != cudaSuccess) return fail(e, "event");
   if ((e = cudaEventCreate(&L->ev0)) != cudaSuccess) return fail(e, "event");
   if ((e = cudaEventCreate(&L->ev1)) != cudaSuccess) return fail(e, "event");
@@ -128,6 +134,7 @@ void lane_destroy(Lane* L) {
   if (!L) return;
   if (L->stream) cudaStreamSynchronize(L->stream);
   if (L->side) cudaStreamSynchronize(L->side);
+  if (L->tstream) cudaStreamSynchronize(L->tstream);
   cudaFree(L->dX);
   for (Lane::WaveBuf& wb : L->wave) {
     cudaFree(wb.dX);
@@ -166,6 +173,8 @@ void lane_destroy(Lane* L) {
   for (int q = 0; q < 4; ++q)
     if (L->evk[q]) cudaEventDestroy(L->evk[q]);
   if (L->evSide) cudaEventDestroy(L->evSide);
+  if (L->evTab) cudaEventDestroy(L->evTab);
+  if (L->tstream) cudaStreamDestroy(L->tstream);
   if (L->side) cudaStreamDestroy(L->side);
   if (L->stream) cudaStreamDestroy(L->stream);
   delete L;
@@ -723,7 +732,10 @@ int lane_run_range(Lane* L, dto_pair* P, uint32_t perm_first, int64_t n_perm, ui
     }
     return lane_err(L, DTO_ERR_CANCELLED, "the request was cancelled");
   };
-  std::vector<double> minp((size_t)n_perm);
+  // every entry is written before it is read: the lane's buffer is reused
+  // (a run as long as the last one clears nothing)
+  std::vector<double>& minp = L->minp;
+  minp.resize((size_t)n_perm);
   long long nroute[DTO_ROUTES] = {};
   cudaEvent_t last_l0_end = nullptr;  // end of the last table sweep (main stream)
   TaskResult unperm{};
@@ -937,19 +949,26 @@ int lane_run_range(Lane* L, dto_pair* P, uint32_t perm_first, int64_t n_perm, ui
       }
       from_model();
     }
-    // The table screens, on the main stream: the first sweep cascades
-    // through every level, so it needs all of them.
+    // The table screens: the first sweep cascades through every level, so
+    // it needs all of them.  They are built on the table stream, beside the
+    // permutation kernel (a build block fits in what its CTAs leave of an
+    // SM), and the main stream's first sweep waits for them.  The lane's
+    // earlier sweeps, which read the same buffers, ended with its last run.
     const int tight_levels = std::min(n_perm >= kTightAllMin ? kTightLevels : 0, kLadderLevels);
     bool built = false;
     for (int l = 0; l < kLadderLevels; ++l) {
-      rc = ensure_table(L, P, l, tau[l], L->stream, &built);
+      rc = ensure_table(L, P, l, tau[l], L->tstream, &built);
       if (rc) return rc;
     }
     for (int l = 0; l < tight_levels; ++l)
       for (int q = 0; q < kTightTables; ++q) {
-        rc = ensure_table(L, P, tight_slot(l, q), tau[tight_slot(l, q)], L->stream, &built);
+        rc = ensure_table(L, P, tight_slot(l, q), tau[tight_slot(l, q)], L->tstream, &built);
         if (rc) return rc;
       }
+    if (built) {
+      LCK(cudaEventRecord(L->evTab, L->tstream));
+      LCK(cudaStreamWaitEvent(L->stream, L->evTab, 0));
+    }
     const int nlev = kLadderLevels;
     // Batches in flight: while batch b's exhaustive fallback and result copy
     // run on its slot's side stream, the next batches' labels and table
