@@ -720,6 +720,10 @@ int lane_run_range(Lane* L, dto_pair* P, uint32_t perm_first, int64_t n_perm, ui
   LCK(cudaMemsetAsync(L->dRefined, 0, 3 * sizeof(unsigned long long), L->stream));
   LCK(cudaMemsetAsync(L->dGuess, 0, 2048, L->stream));
   LCK(cudaEventRecord(L->ev0, L->stream));
+  // this run's table builds follow whatever earlier calls left on the main
+  // stream (a call that returned early may leave a sweep of the lane's
+  // tables running), not this run's own work
+  LCK(cudaStreamWaitEvent(L->tstream, L->ev0, 0));
   // a server's cancel request, checked between batches: the work in flight
   // drains and the run returns DTO_ERR_CANCELLED
   auto cancelled = [&]() -> int {
@@ -952,8 +956,9 @@ int lane_run_range(Lane* L, dto_pair* P, uint32_t perm_first, int64_t n_perm, ui
     // The table screens: the first sweep cascades through every level, so
     // it needs all of them.  They are built on the table stream, beside the
     // permutation kernel (a build block fits in what its CTAs leave of an
-    // SM), and the main stream's first sweep waits for them.  The lane's
-    // earlier sweeps, which read the same buffers, ended with its last run.
+    // SM), after the main stream's work from before this run (the lane's
+    // earlier sweeps read the same buffers), and the main stream's first
+    // sweep waits for them.
     const int tight_levels = std::min(n_perm >= kTightAllMin ? kTightLevels : 0, kLadderLevels);
     bool built = false;
     for (int l = 0; l < kLadderLevels; ++l) {
