@@ -151,9 +151,12 @@ DTO_API int dto_pair_set_stream(dto_pair* pair, uint32_t stream_id);
 /* No counterpart in the reference.  The pair's table ladder (the bounds that
  * decide which table screen settles each permutation of a long run) from a
  * sample of minimum p-values, e.g. a previous run's out_minp saved by another
- * process; count = 0 forgets the ladder, so that the next long run measures
- * it from a first batch.  The ladder decides only which path settles a task,
- * never a result.  p-values outside [0, 1] -> DTO_ERR_INVALID. */
+ * process; count = 0 forgets the pair's ladder, so that its next long run
+ * starts from the context's ladder for the pair's shape (that of the last
+ * pair of that shape the context ran, within 5 % in every size) or, if there
+ * is none, measures it from a first batch.  The ladder decides only which
+ * path settles a task, never a result.  p-values outside [0, 1] ->
+ * DTO_ERR_INVALID. */
 DTO_API int dto_pair_set_ladder(dto_pair* pair, const double* minp, int64_t count);
 /* No counterpart in the reference.  The quantile of the minimum p-values that
  * sets the pair's level-0 table (default 0.85; [0.5, 0.99], else

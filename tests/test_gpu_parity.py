@@ -285,6 +285,28 @@ def test_tuned_level0_quantile_changes_no_result(fresh_engine):
     dq.close()
 
 
+def test_ladder_left_by_a_closed_pair(fresh_engine):
+    # a run leaves its ladder for the next reader; the pair closed first, a
+    # new pair of its shape still starts from it (no first batch) and gets
+    # the same results
+    engine = fresh_engine
+    p = synth.copula_pair(5000, 0.25, seed=64)
+    dp = engine.pair(p.ranks1, p.feat1, p.ranks2, p.feat2, p.n_features, p.population)
+    cold = dp.run(6000, seed=21, want_records=True)
+    assert 1 in set(np.unique(cold.records["route"]).tolist())
+    dp.close()
+    dq = engine.pair(p.ranks1, p.feat1, p.ranks2, p.feat2, p.n_features, p.population)
+    warm = dq.run(6000, seed=21, want_records=True)
+    assert 1 not in set(np.unique(warm.records["route"]).tolist())
+    assert optimum(warm.unpermuted) == optimum(cold.unpermuted)
+    assert same_records(warm.records, cold.records)
+    # a new quantile applies the ladder the last run left, then rebuilds it
+    dq.set_level0_quantile(0.9)
+    again = dq.run(6000, seed=21, want_records=True)
+    assert same_records(again.records, cold.records)
+    dq.close()
+
+
 def test_warm_ladder_gives_the_same_results(fresh_engine):
     # the first long run of a pair measures its ladder from a first batch; a
     # later run starts from the ladder the earlier run left, and a new pair
