@@ -30,6 +30,7 @@ const double kLevel0QuantileDefault = kLevel0Quantile;
 // (cold runs at 100,000 permutations, N = 20,000: 256 -> 47.8 ms, 512 -> 46.9,
 // 1,024 -> 49.3; its slowest tasks and its size both delay the pipeline).
 constexpr long long kFirstBatch = 512;
+constexpr long long kShortTableMin = 256;  // shortest screen run that takes or leaves a ladder
 // Levels of the table ladder: the level-0 quantile, the 99th percentile and
 // the maximum + 1 nat (a two-level ladder measured much slower).
 constexpr int kLadderLevels = 3;
@@ -747,7 +748,16 @@ int lane_run_range(Lane* L, dto_pair* P, uint32_t perm_first, int64_t n_perm, ui
   // the unpermuted task (task 0) in row 0 of the first.  Long runs go through
   // the table ladder (below).
   const long long first_batch = kFirstBatch;
-  const bool use_table = (mode == kModeScreen) && n_perm > 2 * first_batch;
+  // a short screen run of a pair with a ladder of its own (left by any
+  // earlier run of at least kShortTableMin permutations) goes through the
+  // table sweep as well: no first batch to measure
+  bool own_ladder = false;
+  {
+    std::lock_guard<std::mutex> g(P->ladder_mu);
+    own_ladder = P->ladder_ok || P->ladder_pending;
+  }
+  const bool use_table =
+      (mode == kModeScreen) && (n_perm > 2 * first_batch || (own_ladder && n_perm >= kShortTableMin));
   // every task's result must name a grid cell: a result that does not is a
   // device-side failure and is reported instead of read
   const int nt1 = (int)P->T1.size(), nt2 = (int)P->T2.size();
@@ -810,6 +820,8 @@ int lane_run_range(Lane* L, dto_pair* P, uint32_t perm_first, int64_t n_perm, ui
       rc = take(hRes + row0, b0, cnt);
       if (rc) return rc;
     }
+    // the pair's ladder for its later runs
+    if (mode == kModeScreen && n_perm >= kShortTableMin) ladder_update(L->ctx, P, minp, L == L->ctx->lane0);
   } else {
     // Slots left busy by a call that returned early hold nothing of this call.
     LCK(cudaStreamSynchronize(L->side));

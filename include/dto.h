@@ -48,7 +48,7 @@ extern "C" {
 /* Which search path settled a task (dto_result.route).  Every path returns the
  * same optimum; the code says only which one did the work. */
 #define DTO_ROUTE_NONE 0      /* not recorded */
-#define DTO_ROUTE_SCREEN 1    /* exhaustive screen: short runs, a long run's first batch, task 0 */
+#define DTO_ROUTE_SCREEN 1    /* exhaustive screen: short runs of a pair without a ladder, a long run's first batch, task 0 */
 #define DTO_ROUTE_LEVEL0 2    /* table screen, level 0 of the ladder */
 #define DTO_ROUTE_LEVEL1 3    /* table screen, level 1 */
 #define DTO_ROUTE_LEVEL2 4    /* table screen, level 2 */
@@ -185,7 +185,11 @@ DTO_API int dto_pair_order(const dto_pair* pair, int32_t* order1, int32_t* order
  *   out_unpermuted: the unpermuted optimum (NULL: not run, see dto_run_range).
  *   out_minp:  NULL or [n_perm] per-permutation minimum p-values.
  *   out_perm:  NULL or [n_perm] per-permutation optima.
- *   out_summary: NULL or the empirical p-value, FDR and error bounds. */
+ *   out_summary: NULL or the empirical p-value, FDR and error bounds.
+ * Search path (never the results): a screen run of more than 1,024
+ * permutations, or of at least 256 for a pair with a ladder of its own, goes
+ * through the table ladder; other runs through the exhaustive screen.  A
+ * screen run of at least 256 permutations leaves the pair its ladder. */
 DTO_API int dto_run(dto_ctx* ctx, dto_pair* pair, int64_t n_perm, uint64_t seed, const int32_t* perm_idx,
             int precision, dto_result* out_unpermuted, double* out_minp, dto_result* out_perm,
             dto_summary* out_summary);

@@ -285,6 +285,32 @@ def test_tuned_level0_quantile_changes_no_result(fresh_engine):
     dq.close()
 
 
+def test_short_runs_of_a_pair_with_a_ladder(fresh_engine):
+    # a short screen run (at least 256 permutations) leaves the pair a
+    # ladder; the pair's later short runs go through the table sweep (the
+    # exhaustive screen only for the unpermuted task) with the optima of the
+    # exhaustive screen, which a new pair's first short run still takes
+    engine = fresh_engine
+    p = synth.copula_pair(6000, 0.3, seed=82, frac_tied2=0.1)
+    dp = engine.pair(p.ranks1, p.feat1, p.ranks2, p.feat2, p.n_features, p.population)
+    first = dp.run(1000, seed=5, want_records=True)
+    assert set(np.unique(first.records["route"]).tolist()) == {1}
+    short = dp.run(1000, seed=6, want_records=True)
+    assert 1 not in set(np.unique(short.records["route"]).tolist())
+    assert short.summary["n_route"]["screen"] == 1  # the unpermuted task
+    dq = engine.pair(p.ranks1, p.feat1, p.ranks2, p.feat2, p.n_features, p.population)
+    exhaustive = dq.run(1000, seed=6, want_records=True)
+    assert set(np.unique(exhaustive.records["route"]).tolist()) == {1}
+    assert optimum(short.unpermuted) == optimum(exhaustive.unpermuted)
+    assert same_records(short.records, exhaustive.records)
+    assert short.summary["count_le"] == exhaustive.summary["count_le"]
+    # under 256 permutations: the exhaustive screen
+    tiny = dp.run(200, seed=7, want_records=True)
+    assert set(np.unique(tiny.records["route"]).tolist()) == {1}
+    dp.close()
+    dq.close()
+
+
 def test_ladder_left_by_a_closed_pair(fresh_engine):
     # a run leaves its ladder for the next reader; the pair closed first, a
     # new pair of its shape still starts from it (no first batch) and gets
