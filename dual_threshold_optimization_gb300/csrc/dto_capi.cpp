@@ -347,6 +347,14 @@ int dto_pair_create(dto_ctx* ctx, const uint32_t* ranks1, const int32_t* feat1, 
     }
   }
   for (int j = 1; j < nt2; ++j) mcnt[(size_t)j] += mcnt[(size_t)j - 1];
+  // the same labels in the table sweep's form (the labels a table run draws)
+  auto to_hw = [&](const std::vector<int16_t>& g) {
+    std::vector<int16_t> v(g.size(), -1);
+    for (size_t q = 0; q < g.size(); ++q)
+      if (g[q] >= 0) v[q] = (int16_t)hw_label_of_column(column_of_grid_label(g[q], P->C), P->C);
+    return v;
+  };
+  const std::vector<int16_t> ylabHw = to_hw(P->ylab), lab2Hw = to_hw(P->lab2);
   P->ncommon = common;
   P->same_set = (common == n1 && common == n2);
   // fixed-point fraction bits: |ln pmf| <= N ln 2 must fit in int32 with slack
@@ -368,13 +376,15 @@ int dto_pair_create(dto_ctx* ctx, const uint32_t* ranks1, const int32_t* feat1, 
     size_t bytes;
     void** d;
   };
-  const Part parts[7] = {{row.data(), row.size() * 4, (void**)&P->dRow},
+  const Part parts[9] = {{row.data(), row.size() * 4, (void**)&P->dRow},
                          {P->c2.data(), P->c2.size() * 4, (void**)&P->dNcnt},
                          {F.data(), F.size() * 4, (void**)&P->dF},
                          {P->ylab.data(), P->ylab.size() * 2, (void**)&P->dYlab},
                          {P->lab2.data(), P->lab2.size() * 2, (void**)&P->dLab2},
                          {P->map12.data(), P->map12.size() * 4, (void**)&P->dMap12},
-                         {mcnt.data(), mcnt.size() * 4, (void**)&P->dMcnt}};
+                         {mcnt.data(), mcnt.size() * 4, (void**)&P->dMcnt},
+                         {ylabHw.data(), ylabHw.size() * 2, (void**)&P->dYlabHw},
+                         {lab2Hw.data(), lab2Hw.size() * 2, (void**)&P->dLab2Hw}};
   constexpr int kParts = (int)(sizeof(parts) / sizeof(parts[0]));
   size_t off[kParts], total = 0;
   for (int k = 0; k < kParts; ++k) {

@@ -270,8 +270,11 @@ __device__ __forceinline__ int bound_guess_bin(const unsigned* hist, int lane) {
 // offset; the overlap of cell (i, lane*C + t) is O[t] + excl.
 template <int C, class RowFn>
 __device__ __forceinline__ void sweep(const int16_t* __restrict__ x, const int* __restrict__ sRow, int n1,
-                                      int* cnt, int lane, RowFn&& fn) {
+                                      int* cnt, int lane, bool hwlab, RowFn&& fn) {
   constexpr int Cp = C | 1;
+  // a label's counter: the label itself, or for the table sweep's form its
+  // column's (hwlab: the tasks a table run left)
+  auto slot = [&](int v) { return hwlab ? grid_label_of_column(column_of_hw_label(v, C), C) : v; };
   for (int q = lane; q < 32 * Cp; q += 32) cnt[q] = 0;
   __syncwarp();
   int s = sRow[0], e = sRow[1];
@@ -281,10 +284,10 @@ __device__ __forceinline__ void sweep(const int16_t* __restrict__ x, const int* 
     int sN = e;
     int eN = (i + 2 <= n1) ? sRow[i + 2] : e;
     pre = (sN + lane < eN) ? (int)__ldg(x + sN + lane) : -1;
-    if (cur >= 0) atomicAdd(&cnt[cur], 1);
+    if (cur >= 0) atomicAdd(&cnt[slot(cur)], 1);
     for (int p = s + 32 + lane; p < e; p += 32) {
       int v = __ldg(x + p);
-      if (v >= 0) atomicAdd(&cnt[v], 1);
+      if (v >= 0) atomicAdd(&cnt[slot(v)], 1);
     }
     __syncwarp();
     int O[C];
@@ -386,7 +389,7 @@ __global__ void __launch_bounds__(kGridWarps * 32, 1) grid_kernel(const GridArgs
 
     if (A.mode == kModeFull64 || A.mode == kModeDump) {
       Best best = best_init();
-      sweep<C>(x, sRow, n1, cnt, lane, [&](int i, const int (&O)[C], int excl) {
+      sweep<C>(x, sRow, n1, cnt, lane, A.hwlab != 0, [&](int i, const int (&O)[C], int excl) {
         const int K = sRow[i + 1];
 #pragma unroll
         for (int t = 0; t < C; ++t) {
@@ -504,7 +507,7 @@ __global__ void __launch_bounds__(kGridWarps * 32, 1) grid_kernel(const GridArgs
     };
     // One sweep: cells with LB <= B + slack go to stage 2 (B only decreases).
     auto candidate_sweep = [&]() {
-      sweep<C>(x, sRow, n1, cnt, lane, [&](int i, const int (&O)[C], int excl) {
+      sweep<C>(x, sRow, n1, cnt, lane, A.hwlab != 0, [&](int i, const int (&O)[C], int excl) {
         if (!my_row(i)) return;
         const int K = sRow[i + 1];
         const int NK = N - K;
@@ -577,7 +580,7 @@ __global__ void __launch_bounds__(kGridWarps * 32, 1) grid_kernel(const GridArgs
       // pass A: each lane's cell with the smallest LB, whose stage-2 upper
       // bound seeds B
       int bestLB = 0x7fffffff, bestCell = -1, bestK = 0;
-      sweep<C>(x, sRow, n1, cnt, lane, [&](int i, const int (&O)[C], int excl) {
+      sweep<C>(x, sRow, n1, cnt, lane, A.hwlab != 0, [&](int i, const int (&O)[C], int excl) {
         if (!my_row(i)) return;
         const int K = sRow[i + 1];
         const int NK = N - K;

@@ -227,6 +227,8 @@ struct dto_pair {
   uint32_t* dF = nullptr;
   int16_t* dYlab = nullptr;
   int16_t* dLab2 = nullptr;
+  int16_t* dYlabHw = nullptr;  // dYlab and dLab2 in the table sweep's label form
+  int16_t* dLab2Hw = nullptr;
   int* dMap12 = nullptr;
   int* dMcnt = nullptr;  // [n2]: list-1 positions whose label's column is <= j
   dto::PairDev dev{};
@@ -320,7 +322,7 @@ bool ladder_take_deferred(dto_ctx* ctx, const LadderShape& want, double nats[kLa
 // Labels of `count` permutations from perm id `first` (or of uploaded index
 // rows dIdx) into X (row stride xs) on the lane's main stream.
 int make_labels_launch(Lane* L, dto_pair* P, uint64_t seed, uint32_t first, int count, const int32_t* dIdx,
-                       int16_t* X, long long xs);
+                       int16_t* X, long long xs, bool hwlab = false);
 // The exhaustive screen of what the last table level left, on `stream`.
 int table_exhaustive(Lane* L, dto_pair* P, const int16_t* X, long long xstride, int ntask, TaskResult* dOut,
                      int nlev, const int* fall, int* cnts, cudaStream_t stream,

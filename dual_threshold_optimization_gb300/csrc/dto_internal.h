@@ -61,6 +61,30 @@ struct TaskResult {
 
 enum GridMode { kModeFull64 = 0, kModeScreen = 1, kModeDump = 2 };
 
+// The table sweep's per-lane layout (a half-warp's lane holds C2 = 2 C
+// columns as C words of two 16-bit counts): columns padded to whole 16-byte
+// chunks, and counter words per lane padded to an odd number of 16-byte
+// chunks (a quarter-warp's 128-bit loads hit distinct banks).
+__host__ __device__ constexpr int hw_cq(int C2) { return (C2 + 7) & ~7; }
+__host__ __device__ constexpr int hw_wp(int C2) { return 4 * ((hw_cq(C2) / 8) | 1); }
+
+// Column labels (the list-2 threshold column j of a list-1 position; -1:
+// none) in two forms.  The grid kernel's: (j / C) * (C | 1) + j % C, its
+// counter index (32 lanes of C columns, odd stride).  The table sweep's: the
+// byte offset of the column's 16-bit count among the 16 lanes of a task
+// (lane j / 2C, word (j % 2C) / 2), bit 13 set for the upper half of the
+// word.  Labels drawn for the table sweep are in its form, so it adds them
+// to its counters without a lookup; the grid kernel turns them back when it
+// screens the tasks the sweep left.
+__host__ __device__ constexpr int hw_label_of_column(int j, int C) {
+  return (4 * ((j / (2 * C)) * hw_wp(2 * C) + (j % (2 * C)) / 2)) | ((j % 2) << 13);
+}
+__host__ __device__ constexpr int grid_label_of_column(int j, int C) { return (j / C) * (C | 1) + j % C; }
+__host__ __device__ constexpr int column_of_grid_label(int lab, int C) { return (lab / (C | 1)) * C + lab % (C | 1); }
+__host__ __device__ constexpr int column_of_hw_label(int v, int C) {
+  return ((v & 0x1FFF) / 4 / hw_wp(2 * C)) * (2 * C) + 2 * (((v & 0x1FFF) / 4) % hw_wp(2 * C)) + ((v >> 13) & 1);
+}
+
 struct GridArgs {
   PairDev P;
   const int16_t* X;      // [ntask][xstride] labels per list-1 position
@@ -70,6 +94,7 @@ struct GridArgs {
   int route;             // DTO_ROUTE_* written with each result
   int smemF;             // 1: the fixed-point table is staged in shared memory
   int coop;              // screen mode: the CTA's warps share each task
+  int hwlab;             // 1: X holds the table sweep's labels (a table run's fallbacks)
   TaskResult* out;       // [ntask]
   int* work;             // task counter (zeroed before the launch)
   unsigned long long* n_refined;  // [3]: FP64 tails, FP32 tails, speculative sweeps rejected

@@ -398,7 +398,7 @@ cudaError_t launch_grid(const GridArgs& a, int ctas, cudaStream_t s) {
 size_t table_smem_bytes(int C, int n1, int n2, long long Npop, int smemF) {
   const size_t f = smemF ? (size_t)((Npop + 1 + 3) & ~3LL) * 4 : 0;
   const size_t base = f + (size_t)((n1 + 1 + 3) & ~3) * 4 + (size_t)((n2 + 3) & ~3) * 4;  // n1 = -1, n2 = 0: none
-  return base + (size_t)((hw_lut_entries(C) + 7) & ~7) * 2 + (size_t)kTableWarps * hw_warp_ints(2 * C) * 4;
+  return base + (size_t)kTableWarps * hw_warp_ints(2 * C) * 4;
 }
 
 size_t table_entries(int C, int n1) { return (size_t)n1 * 16 * hw_cq(2 * C); }

@@ -367,6 +367,7 @@ int table_exhaustive(Lane* L, dto_pair* P, const int16_t* X, long long xstride, 
   g.ntask = ntask;
   g.mode = kModeScreen;
   g.route = DTO_ROUTE_FALLBACK;
+  g.hwlab = 1;  // a table run's labels
   g.smemF = grid_smem_bytes(P->C, P->dev.n1, P->npop, 1) <= L->ctx->smem_optin ? 1 : 0;
   g.coop = 1;  // the few tasks left here are the hard ones: a CTA each
   g.out = dOut;
@@ -442,9 +443,6 @@ int fixed_log(double p, int fshift) {
 }
 
 // Labels of n_perm permutations starting at perm id `first` into L->dX.
-int make_labels_launch(Lane* L, dto_pair* P, uint64_t seed, uint32_t first, int count,
-                       const int32_t* dIdx, int16_t* X, long long xs);
-
 int lane_make_labels(Lane* L, dto_pair* P, uint64_t seed, uint32_t first, int count,
                      const int32_t* dIdx /* nullable: test mode, [count][N1+N2] */, int row0) {
   NvtxRange range("dto: labels");
@@ -459,8 +457,10 @@ int lane_make_labels(Lane* L, dto_pair* P, uint64_t seed, uint32_t first, int co
 }
 
 int make_labels_launch(Lane* L, dto_pair* P, uint64_t seed, uint32_t first, int count,
-                       const int32_t* dIdx, int16_t* X, long long xs) {
+                       const int32_t* dIdx, int16_t* X, long long xs, bool hwlab) {
   int rc = DTO_OK;
+  const int16_t* lab1 = hwlab ? P->dYlabHw : P->dYlab;  // the labels' form (hwlab: a table run's)
+  const int16_t* lab2 = hwlab ? P->dLab2Hw : P->dLab2;
   if (dIdx) {
     ComposeArgs c{};
     c.N1 = (int)P->N1;
@@ -469,7 +469,7 @@ int make_labels_launch(Lane* L, dto_pair* P, uint64_t seed, uint32_t first, int 
     c.idx2 = dIdx + P->N1;
     c.stride = P->N1 + P->N2;
     c.map12 = P->dMap12;
-    c.lab2 = P->dLab2;
+    c.lab2 = lab2;
     c.X = X;
     c.xstride = xs;
     LCK(launch_compose(c, count, L->stream));
@@ -486,7 +486,7 @@ int make_labels_launch(Lane* L, dto_pair* P, uint64_t seed, uint32_t first, int 
     // matters: list 1 is shuffled, list 2 kept (idx2 = identity).
     a.L = (int)P->N1;
     a.list_tag = 1;
-    a.Ylab = P->dYlab;
+    a.Ylab = lab1;
     a.X = X;
     a.rowstart = P->dRow;
     a.n1 = P->dev.n1;
@@ -514,7 +514,7 @@ int make_labels_launch(Lane* L, dto_pair* P, uint64_t seed, uint32_t first, int 
   c.idx2 = sig + P->N1;
   c.stride = ss;
   c.map12 = P->dMap12;
-  c.lab2 = P->dLab2;
+  c.lab2 = lab2;
   c.X = X;
   c.xstride = xs;
   LCK(launch_compose(c, count, L->stream));
@@ -921,7 +921,7 @@ int lane_run_range(Lane* L, dto_pair* P, uint32_t perm_first, int64_t n_perm, ui
       if (r) return r;
       NvtxRange range("dto: labels");
       LCK(cudaEventRecord(sl.ev[0], L->stream));
-      r = make_labels_launch(L, P, seed, (uint32_t)(perm_first + b0), cnt, dI, (int16_t*)sl.dX, xs);
+      r = make_labels_launch(L, P, seed, (uint32_t)(perm_first + b0), cnt, dI, (int16_t*)sl.dX, xs, true);
       if (r) return r;
       LCK(cudaEventRecord(sl.ev[1], L->stream));
       sl.b0 = b0;

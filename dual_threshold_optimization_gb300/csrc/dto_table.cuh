@@ -413,17 +413,10 @@ __device__ __forceinline__ int lv_tight_tau(const TableGridArgs& A, int l, int q
 // carry from one half into the other.  The hits are resolved one task at a
 // time by the whole warp.
 // ---------------------------------------------------------------------------
-__host__ __device__ constexpr int hw_cq(int C2) { return (C2 + 7) & ~7; }
-// counter words per lane: C2 / 2 words padded to an odd number of 16-byte
-// chunks (a quarter-warp's 128-bit loads hit distinct banks)
-__host__ __device__ constexpr int hw_wp(int C2) { return 4 * ((hw_cq(C2) / 8) | 1); }
 __host__ __device__ constexpr int hw_task_ints(int C2) {
   return 16 * hw_wp(C2) + (int)(sizeof(WarpTask) / 4) + 3 * kTableSurvCap;
 }
 __host__ __device__ constexpr int hw_warp_ints(int C2) { return 2 * hw_task_ints(C2) + 2 * kCandCap + 5 * kPend; }
-// label -> counter offset table: one entry per counter slot of the 32-lane
-// label encoding (lane * (C | 1) + t)
-__host__ __device__ constexpr int hw_lut_entries(int C) { return 32 * (C | 1); }
 
 __device__ __forceinline__ TableWarpMem hw_warp_mem(int* base, int C2, int t) {
   TableWarpMem m;
@@ -451,8 +444,6 @@ __device__ __forceinline__ TableWarpMem hw_warp_mem(int* base, int C2, int t) {
 // is filled by the warps that have moved on to the next.
 template <int C2, bool Multi>
 __global__ void __launch_bounds__(kTableWarps * 32, 1) table_hw_kernel(const TableGridArgs Ain) {
-  constexpr int C = C2 / 2;        // columns per lane of the 32-lane label encoding
-  constexpr int Cp = C | 1;
   constexpr int NQ = hw_cq(C2) / 8;  // 16-byte table chunks per lane per row
   constexpr int NW = C2 / 2;         // counter words per lane
   constexpr int Wp = hw_wp(C2);
@@ -471,20 +462,13 @@ __global__ void __launch_bounds__(kTableWarps * 32, 1) table_hw_kernel(const Tab
   uint32_t* sF = reinterpret_cast<uint32_t*>(smem_raw);
   int* sRow = reinterpret_cast<int*>(sF + ((!Multi && Ain.smemF) ? ((Npop0 + 1 + 3) & ~3) : 0));
   int* sNcnt = sRow + (Multi ? 0 : ((Ain.P.n1 + 1 + 3) & ~3));
-  uint16_t* sLut = reinterpret_cast<uint16_t*>(sNcnt + (Multi ? 0 : ((Ain.P.n2 + 3) & ~3)));
-  int* sWarp = reinterpret_cast<int*>(sLut + ((hw_lut_entries(C) + 7) & ~7));
+  int* sWarp = sNcnt + (Multi ? 0 : ((Ain.P.n2 + 3) & ~3));
   int* const wb = sWarp + warp * hw_warp_ints(C2);
   if constexpr (!Multi) {
     for (int q = threadIdx.x; q <= Ain.P.n1; q += blockDim.x) sRow[q] = __ldg(Ain.P.rowstart + q);
     for (int q = threadIdx.x; q < Ain.P.n2; q += blockDim.x) sNcnt[q] = __ldg(Ain.P.ncnt + q);
     if (Ain.smemF)
       for (int q = threadIdx.x; q <= Npop0; q += blockDim.x) sF[q] = __ldg(Ain.P.F + q);
-  }
-  for (int q = threadIdx.x; q < hw_lut_entries(C); q += blockDim.x) {
-    const int l = q / Cp, tcol = q - (q / Cp) * Cp;
-    const int j = l * C + min(tcol, C - 1);
-    const int hh = j / C2, tc2 = j - (j / C2) * C2;
-    sLut[q] = (uint16_t)((4 * (hh * Wp + (tc2 >> 1))) | ((tc2 & 1) << 15));
   }
   // the cascade levels' tables and bounds, per warp, indexed by level from
   // shared memory (selecting among the kernel's arguments at run time kept
@@ -620,10 +604,11 @@ __global__ void __launch_bounds__(kTableWarps * 32, 1) table_hw_kernel(const Tab
     bool anyhits[2] = {false, false};
     int cur_tight[2] = {-1, -1};  // the table each task's rows are compared with (uniform)
     const uint4* ktab_me = reinterpret_cast<const uint4*>(sLvTab[lv_me][0]);
-    auto add_lab = [&](int lab) {
-      const uint32_t v = sLut[lab];
-      atomicAdd(reinterpret_cast<uint32_t*>(reinterpret_cast<unsigned char*>(cnt_t) + (v & 0x7FFFu)),
-                1u << ((v >> 11) & 16u));
+    // a label (the sweep's form) is its count's byte offset, bit 13 the
+    // upper half of the word
+    auto add_lab = [&](int v) {
+      atomicAdd(reinterpret_cast<uint32_t*>(reinterpret_cast<unsigned char*>(cnt_t) + (v & 0x1FFF)),
+                1u << ((v >> 9) & 16));
     };
     auto add_word = [&](int w, int q, int rs, int re) {
       const int p = 2 * q;

@@ -152,7 +152,7 @@ int enqueue_wave(Lane* L, std::vector<WaveJob>& jobs, Wave& wv) {
     for (int k = 0; k < nj; ++k) {
       const long long xs = xstride_of(job(k).P->N1);
       rc = make_labels_launch(L, job(k).P, job(k).seed, job(k).first, (int)job(k).n_perm, nullptr,
-                              X + xoff[(size_t)k] + xs, xs);
+                              X + xoff[(size_t)k] + xs, xs, true);
       if (rc) return rc;
       wv.launches[(size_t)k] += 1;
     }
