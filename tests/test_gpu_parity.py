@@ -285,6 +285,32 @@ def test_tuned_level0_quantile_changes_no_result(fresh_engine):
     dq.close()
 
 
+@pytest.mark.parametrize("N,scale2,C", [(100, 1, 4), (600, 1, 8), (1500, 1, 12), (3000, 1, 16),
+                                        (40000, 1, 24), (3000, 100, 28), (3000, 400, 32)])
+def test_table_path_and_fallbacks_at_every_grid_width(engine, N, scale2, C):
+    # Table runs draw labels in the sweep's form (a count's byte offset in a
+    # lane layout that depends on the grid width C); the exhaustive screen
+    # turns them back for the tasks no level settles.  A ladder from the
+    # lowest 30 % of the minima leaves many tasks to it; every optimum must
+    # equal the exhaustive screen's (a new pair's short run).  Sparse list-2
+    # ranks give the widest grids.
+    p = synth.copula_pair(N, 0.3, seed=90 + N + scale2)
+    r2 = p.ranks2 * scale2
+    dq = engine.pair(p.ranks1, p.feat1, r2, p.feat2, p.n_features, p.population)
+    assert min(c for c in (4, 8, 12, 16, 20, 24, 28, 32) if 32 * c >= dq.n2) == C, dq.n2
+    ref = dq.run(1000, seed=31, want_records=True)
+    assert set(np.unique(ref.records["route"]).tolist()) == {1}
+    dq.close()
+    dp = engine.pair(p.ranks1, p.feat1, r2, p.feat2, p.n_features, p.population)
+    dp.set_ladder(np.sort(ref.minp)[:300])
+    res = dp.run(1000, seed=31, want_records=True)
+    routes = set(np.unique(res.records["route"]).tolist())
+    assert 5 in routes and 1 not in routes, routes  # fallbacks; no exhaustive first batch
+    assert optimum(res.unpermuted) == optimum(ref.unpermuted)
+    assert same_records(res.records, ref.records)
+    dp.close()
+
+
 def test_short_runs_of_a_pair_with_a_ladder(fresh_engine):
     # a short screen run (at least 256 permutations) leaves the pair a
     # ladder; the pair's later short runs go through the table sweep (the
