@@ -1043,7 +1043,8 @@ int lane_run_range(Lane* L, dto_pair* P, uint32_t perm_first, int64_t n_perm, ui
       int nb = 0;
       for (BatchSlot& sl : L->slot)
         if (sl.busy) order[nb++] = &sl;
-      std::sort(order, order + nb, [](const BatchSlot* a, const BatchSlot* b) { return a->b0 < b->b0; });
+      for (int x = 1; x < nb; ++x)  // at most kSlots entries, oldest first
+        for (int y = x; y > 0 && order[y]->b0 < order[y - 1]->b0; --y) std::swap(order[y], order[y - 1]);
       for (int k = 0; k < nb; ++k) {
         rc = harvest(*order[k]);
         if (rc) return rc;
