@@ -399,7 +399,8 @@ __device__ __forceinline__ int lv_tight_tau(const TableGridArgs& A, int l, int q
 // control, the table-row loads (both halves read the same 256 bytes) and the
 // scan.  Per row:
 //   1. each label of the row adds 1 to its column's half-word (one shared
-//      atomic; a 2 KB table maps a label to its word and half);
+//      atomic; a table run's labels are the counts' byte offsets, bit 13
+//      the upper half: hw_label_of_column);
 //   2. each lane runs the in-lane prefix of its counts in NG independent
 //      chains (x 0x10001 + R, then the upper half carried), keeping every
 //      word's two partial overlaps in registers; the chains' totals give the
