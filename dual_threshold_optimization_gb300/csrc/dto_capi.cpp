@@ -81,9 +81,11 @@ void lf_table_dd(long long nmax, std::vector<double>& hi, std::vector<double>& l
   }
 }
 
-// round(x * 2^f) of a double-double x, to the nearest integer.
-long long dd_round_scaled(double hi, double lo, int f) {
-  double x = std::ldexp(hi, f), y = std::ldexp(lo, f);
+// round(x * scale) of a double-double x, to the nearest integer; scale is a
+// power of two (2^f), so the products are exact (as ldexp's are, at a sixth
+// of the cost: the table has population + 1 entries per pair).
+long long dd_round_scaled(double hi, double lo, double scale) {
+  double x = hi * scale, y = lo * scale;
   double r = std::nearbyint(x);
   double frac = (x - r) + y;
   if (frac > 0.5) r += 1.0;
@@ -364,8 +366,9 @@ int dto_pair_create(dto_ctx* ctx, const uint32_t* ranks1, const int32_t* feat1, 
   int rc = ensure_lf(ctx, population);
   if (rc) { delete P; return rc; }
   std::vector<uint32_t> F((size_t)population + 1);
+  const double fscale = std::ldexp(1.0, f);
   for (long long m = 0; m <= population; ++m)
-    F[(size_t)m] = (uint32_t)(unsigned long long)dd_round_scaled(ctx->lf_hi[(size_t)m], ctx->lf_lo[(size_t)m], f);
+    F[(size_t)m] = (uint32_t)(unsigned long long)dd_round_scaled(ctx->lf_hi[(size_t)m], ctx->lf_lo[(size_t)m], fscale);
   std::vector<int> row((size_t)nt1 + 1);
   row[0] = 0;
   for (int i = 0; i < nt1; ++i) row[(size_t)i + 1] = P->c1[(size_t)i];
