@@ -349,11 +349,14 @@ int dto_pair_create(dto_ctx* ctx, const uint32_t* ranks1, const int32_t* feat1, 
     }
   }
   for (int j = 1; j < nt2; ++j) mcnt[(size_t)j] += mcnt[(size_t)j - 1];
-  // the same labels in the table sweep's form (the labels a table run draws)
+  // the same labels in the table sweep's form (the labels a table run
+  // draws), through a table over the grid kernel's labels
+  std::vector<int16_t> g2h((size_t)32 * Cp, -1);
+  for (int j = 0; j < 32 * P->C; ++j) g2h[(size_t)grid_label_of_column(j, P->C)] = (int16_t)hw_label_of_column(j, P->C);
   auto to_hw = [&](const std::vector<int16_t>& g) {
     std::vector<int16_t> v(g.size(), -1);
     for (size_t q = 0; q < g.size(); ++q)
-      if (g[q] >= 0) v[q] = (int16_t)hw_label_of_column(column_of_grid_label(g[q], P->C), P->C);
+      if (g[q] >= 0) v[q] = g2h[(size_t)g[q]];
     return v;
   };
   const std::vector<int16_t> ylabHw = to_hw(P->ylab), lab2Hw = to_hw(P->lab2);

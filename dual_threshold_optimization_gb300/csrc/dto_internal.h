@@ -80,7 +80,6 @@ __host__ __device__ constexpr int hw_label_of_column(int j, int C) {
   return (4 * ((j / (2 * C)) * hw_wp(2 * C) + (j % (2 * C)) / 2)) | ((j % 2) << 13);
 }
 __host__ __device__ constexpr int grid_label_of_column(int j, int C) { return (j / C) * (C | 1) + j % C; }
-__host__ __device__ constexpr int column_of_grid_label(int lab, int C) { return (lab / (C | 1)) * C + lab % (C | 1); }
 __host__ __device__ constexpr int column_of_hw_label(int v, int C) {
   return ((v & 0x1FFF) / 4 / hw_wp(2 * C)) * (2 * C) + 2 * (((v & 0x1FFF) / 4) % hw_wp(2 * C)) + ((v >> 13) & 1);
 }
