@@ -226,6 +226,30 @@ def test_table_sweep_beyond_16_bit_overlaps(engine):
     dp.close()
 
 
+@pytest.mark.parametrize("kw", [dict(N=3000, rho=0.2, seed=23),
+                                dict(N=3000, rho=0.2, seed=24, subset1=2600, subset2=2800)])
+def test_test_mode_through_the_table_sweep(engine, kw):
+    # uploaded index arrays through the table sweep (a pair with a ladder):
+    # the compose kernel writes their labels in the sweep's form; with a
+    # ladder tight enough to leave tasks to the exhaustive screen, every
+    # optimum equals the exhaustive screen's for the same permutations
+    p = synth.small_pair(**kw)
+    dq = engine.pair(p.ranks1, p.feat1, p.ranks2, p.feat2, p.n_features, p.population)
+    seed = 0xABCDEF
+    ref = dq.run(1000, seed=seed, want_records=True)
+    assert set(np.unique(ref.records["route"]).tolist()) == {1}
+    i1, i2 = dq.export_permutations(seed, 1, 1000)
+    dq.close()
+    dp = engine.pair(p.ranks1, p.feat1, p.ranks2, p.feat2, p.n_features, p.population)
+    dp.set_ladder(np.sort(ref.minp)[:300])
+    tm = dp.run(1000, perm_idx=np.concatenate([i1, i2], axis=1), want_records=True)
+    routes = set(np.unique(tm.records["route"]).tolist())
+    assert 5 in routes and 1 not in routes, routes
+    assert optimum(tm.unpermuted) == optimum(ref.unpermuted)
+    assert same_records(tm.records, ref.records)
+    dp.close()
+
+
 @pytest.mark.parametrize("N", [3, 7, 8, 9, 17, 33])
 def test_philox_permutations_tiny_lists(engine, N):
     # lists shorter than one 16-byte label chunk and grids of one-element rows:
