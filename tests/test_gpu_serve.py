@@ -69,6 +69,35 @@ def test_batch_run_equals_single_runs(engine):
         dp.close()
 
 
+def test_batch_waves_with_fallbacks(engine):
+    # Pairs whose ladders are too tight leave tasks of a wave's sweep to the
+    # exhaustive screen, which reads the labels in the sweep's form: every
+    # minimum equals the exhaustive screen's for the same permutation ids
+    # (short runs of new pairs, ids 1..1000 and 1001..n).
+    specs = [(synth.copula_pair(6000, 0.2, seed=101), 1500, 31),
+             (synth.copula_pair(7000, 0.25, seed=102), 1800, 32)]
+    refs = []
+    for p, n, s in specs:
+        parts = []
+        for first, count in ((1, 1000), (1001, n - 1000)):
+            dq = engine.pair(p.ranks1, p.feat1, p.ranks2, p.feat2, p.n_features, p.population)
+            parts.append(dq.run(count, seed=s, first=first))
+            dq.close()
+        refs.append((parts[0].unpermuted, np.concatenate([parts[0].minp, parts[1].minp])))
+    dps = [engine.pair(p.ranks1, p.feat1, p.ranks2, p.feat2, p.n_features, p.population) for p, _, _ in specs]
+    for dp, (_, n, _), (_, minp) in zip(dps, specs, refs):
+        dp.set_ladder(np.sort(minp)[: int(0.3 * n)])
+    got = engine.batch_run(dps, [n for _, n, _ in specs], [s for _, _, s in specs])
+    # one wave (both grids 16 columns a lane): one sweep launch for the two
+    assert sum(g.summary["sweep0_launches"] for g in got) == 1
+    for g, (unperm, minp) in zip(got, refs):
+        assert g.summary["n_route"]["fallback"] > 0, g.summary["n_route"]
+        assert optimum(g.unpermuted) == optimum(unperm)
+        assert np.array_equal(g.minp, minp)
+    for dp in dps:
+        dp.close()
+
+
 def test_batch_waves_equal_single_runs(engine):
     # Pairs that have run before (so they have a ladder) and short screen
     # runs go through waves: the tasks of several pairs in one multi-pair
