@@ -313,10 +313,13 @@ def run_reference(args):
     threads = host_threads()
     for _ in range(args.warmup):
         cpu_reference_rate(pair, threads, target_s=2.0)
+    # each step a bounded sample: --ref-seconds, and the timed steps together
+    # about two minutes at most
+    per_step = min(args.ref_seconds, max(2.0, 120.0 / max(args.steps, 1)))
     rates, total = [], 0.0
     sample = ""
     for _ in range(args.steps):
-        r, sample, dt = cpu_reference_rate(pair, threads, target_s=args.ref_seconds)
+        r, sample, dt = cpu_reference_rate(pair, threads, target_s=per_step)
         rates.append(r)
         total += dt
     value = statistics.mean(rates)
